@@ -1,0 +1,246 @@
+/*
+ * eprem_gpu.h -- C ABI of the GB300 (sm_103a) implementation of EPREM's
+ * per-timestep energetic-particle update.
+ *
+ * The reference (predsci/eprem) keeps all state in C globals and exposes the
+ * hot path as four argument-less entry points called from its driver loop
+ * (src/eprem.c:620-671):
+ *
+ *   void updateEnergeticParticles(void);   src/energeticParticles.h:51
+ *   void updateMhd(void);                  src/flow.h:45
+ *   void moveNodes(Scalar_t dt);           src/simCore.h:71
+ *   void masMoveNodes(Scalar_t dt);        src/masInterp.h:186
+ *
+ * This library replaces their bodies.  A host shim (eprem_gb300/host/
+ * eprem_dropin.c) keeps those four symbols, packs the reference globals
+ * (grid[], eParts[], config, egrid/vgrid/...) into the plain arrays below and
+ * calls the functions of this header.  Nothing here uses C++ or torch types:
+ * plain pointers, sizes and status codes only.
+ *
+ * State lives on the device inside an opaque run handle.  Every stream of the
+ * cube-sphere grid is held by one GPU (the reference spreads the nodes of each
+ * stream over MPI ranks, src/mpiInit.c:91-147).
+ *
+ * Layouts (host and device alike):
+ *   f      [stream][node][energy][mu], mu fastest.  For one MPI rank this is
+ *          the reference eParts layout idx_frcsspem (src/global.h:61) with the
+ *          INNER_SHELL ghost (shell 0) removed: node k is shell k+1, stream
+ *          index s = face*ROWS*COLS + row*COLS + col (computeLines order,
+ *          src/unifiedOutput.c:64-92).
+ *   nodes  [field][stream*num_nodes + node], one double per Node_t member
+ *          used by the hot path (src/cubeShellStruct.h:51-93), fields
+ *          enumerated by eprem_node_field below.
+ *
+ * All functions return EPREM_GPU_OK (0) or a negative status; the message of
+ * the last failure on the calling thread is available from
+ * eprem_gpu_last_error().  No exception crosses this boundary.  The library is
+ * not re-entrant for one run handle (the reference is single-threaded per
+ * rank, MPI_THREAD_FUNNELED, src/mpiInit.c:57).
+ */
+#ifndef EPREM_GPU_H
+#define EPREM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EPREM_GPU_OK               0
+#define EPREM_GPU_ERR_ARG         -1  /* bad argument or unsupported size      */
+#define EPREM_GPU_ERR_CUDA        -2  /* CUDA runtime failure                   */
+#define EPREM_GPU_ERR_NAN         -3  /* NaN in f   (reference checkNaN->panic) */
+#define EPREM_GPU_ERR_INF         -4  /* Inf in f   (reference checkInf->panic) */
+#define EPREM_GPU_ERR_DS          -5  /* ds <= 0 (FindSegmentLengths panic)     */
+#define EPREM_GPU_ERR_SUBCYCLES   -6  /* sub-cycle count above params cap       */
+#define EPREM_GPU_ERR_UNSUPPORTED -7  /* option the reference path does not have
+                                         or that this library does not build   */
+#define EPREM_GPU_ERR_STATE       -8  /* stream thinned to fewer than 3 nodes   */
+
+/* ---- arithmetic forms -------------------------------------------------- */
+#define EPREM_FP64 0  /* plain form: every operation in IEEE double          */
+#define EPREM_FP32 1  /* f and the stencil/scattering arithmetic in float;
+                         positions, distances, dt/CFL reductions and
+                         conservation sums in double                         */
+
+/* ---- sizes -------------------------------------------------------------- */
+typedef struct {
+  int32_t num_streams;   /* NUM_STREAMS = 6*numRowsPerFace*numColumnsPerFace */
+  int32_t num_nodes;     /* numNodesPerStream (TOTAL_NUM_SHELLS), >= 3       */
+  int32_t num_species;   /* numSpecies; must be 1 (see DESIGN notes)         */
+  int32_t num_energies;  /* numEnergySteps, 2..64                            */
+  int32_t num_mu;        /* numMuSteps, 2..64                                */
+  int32_t precision;     /* EPREM_FP64 or EPREM_FP32                         */
+} eprem_dims_t;
+
+/* ---- run parameters: the config members the hot path reads -------------
+ * Values are the reference's after setRuntimeConstants()
+ * (src/configuration.c:325-348): times in AU/c, speeds in c, densities in
+ * MHD_DENSITY_NORM, fields in MHD_B_NORM. */
+typedef struct {
+  double  r_scale;                  /* config.rScale                          */
+  double  t_del;                    /* config.tDel (AU/c)                     */
+  int32_t num_ep_steps;             /* config.numEpSteps                      */
+  int32_t use_parallel_diffusion;   /* config.useParallelDiffusion            */
+  int32_t use_adiabatic_focus;      /* config.useAdiabaticFocus               */
+  int32_t use_adiabatic_change;     /* config.useAdiabaticChange              */
+  int32_t check_seed_population;    /* config.checkSeedPopulation             */
+  int32_t use_ep_boundary;          /* config.useEPBoundary                   */
+  int32_t use_boundary_function;    /* config.useBoundaryFunction             */
+  int32_t adiabatic_focus_alg;      /* 1 Euler upwind, 2 RK3 upwind, 3 RK3+WENO3 */
+  int32_t adiabatic_change_alg;     /* same                                   */
+  double  damp_cooling;             /* config.dampCooling                     */
+  double  dsh_min;                  /* config.dsh_min (AU)                    */
+  int32_t mfp_type;                 /* 1: r-scaled, 2: B-scaled               */
+  double  lamo;                     /* config.lamo (AU)                       */
+  double  mfp_radial_power;         /* config.mfpRadialPower                  */
+  double  mfp_b_power;              /* config.mfpBPower                       */
+  double  mhd_bs_au;                /* config.mhdBsAu                         */
+  double  bf_amplitude;             /* config.boundaryFunctAmplitude          */
+  double  bf_xi;                    /* config.boundaryFunctXi                 */
+  double  bf_gamma;                 /* config.boundaryFunctGamma              */
+  double  bf_beta;                  /* config.boundaryFunctBeta               */
+  double  bf_ecutoff;               /* config.boundaryFunctEcutoff (MeV)      */
+  double  bf_r0;                    /* config.boundaryFunctR0 (AU)            */
+  /* analytic background (src/flow.c), used by eprem_gpu_update_mhd */
+  double  mhd_us;                   /* config.mhdUs   (flowMag/C)             */
+  double  mhd_ns_au;                /* config.mhdNsAu                         */
+  double  omega_sun;                /* config.omegaSun                        */
+  int32_t ideal_shock;              /* config.idealShock                      */
+  double  ideal_shock_sharpness;
+  double  ideal_shock_scale_length;
+  double  ideal_shock_jump;
+  double  ideal_shock_falloff;
+  double  ideal_shock_speed;        /* cm/s, as in the config file           */
+  double  ideal_shock_init_time;    /* days, as in the config file           */
+  double  ideal_shock_theta;
+  double  ideal_shock_phi;
+  double  ideal_shock_width;
+  int32_t max_subcycles;            /* cap on any sub-cycle count; above it the
+                                       update stops with ERR_SUBCYCLES (0 means
+                                       1,000,000).  The reference has no cap. */
+} eprem_params_t;
+
+/* ---- 1-D grids built by initEnergeticParticlesGrids
+ *      (src/energeticParticlesInit.c:36-100); host pointers, copied at create */
+typedef struct {
+  const double *egrid;     /* [E] kinetic energy / (mp c^2)                   */
+  const double *vgrid;     /* [E] speed / c                                   */
+  const double *vgrid_i;   /* [E] 1 / vgrid                                   */
+  const double *mugrid;    /* [M] mu cell centres                             */
+  const double *rigidity;  /* [E] rigidity^rigidityPower (species 0)          */
+  double dlnp;             /* ln p spacing                                    */
+  double dmu;              /* mu spacing                                      */
+} eprem_grids_t;
+
+/* ---- per-node fields (Node_t members, src/cubeShellStruct.h:51-93) ------- */
+enum eprem_node_field {
+  EPREM_NODE_RX = 0, EPREM_NODE_RY, EPREM_NODE_RZ, /* r (units of rScale)     */
+  EPREM_NODE_RMAG,                                 /* rmag                    */
+  EPREM_NODE_BMAG,                                 /* mhdBmag                 */
+  EPREM_NODE_DLNB,                                 /* mhdDlnB                 */
+  EPREM_NODE_DLNN,                                 /* mhdDlnN                 */
+  EPREM_NODE_DUPAR,                                /* mhdDuPar                */
+  EPREM_NODE_DS,                                   /* ds          (output)    */
+  EPREM_NODE_BMAG_PLUS,                            /* mhdBmagPlus (output)    */
+  EPREM_NODE_BMAG_MINUS,                           /* mhdBmagMinus (output)   */
+  EPREM_NODE_BR, EPREM_NODE_BTHETA, EPREM_NODE_BPHI,
+  EPREM_NODE_VR, EPREM_NODE_VTHETA, EPREM_NODE_VPHI,
+  EPREM_NODE_VMAG,
+  EPREM_NODE_DENSITY,
+  EPREM_NODE_DIVV,
+  EPREM_NODE_BVEC_X, EPREM_NODE_BVEC_Y, EPREM_NODE_BVEC_Z,
+  EPREM_NODE_VVEC_X, EPREM_NODE_VVEC_Y, EPREM_NODE_VVEC_Z,
+  EPREM_NODE_BMAG_OLD,
+  EPREM_NODE_DENSITY_OLD,
+  EPREM_NODE_VSPH_OLD_R, EPREM_NODE_VSPH_OLD_THETA, EPREM_NODE_VSPH_OLD_PHI,
+  EPREM_NODE_DS_OLD,
+  EPREM_NODE_ROLD_X, EPREM_NODE_ROLD_Y, EPREM_NODE_ROLD_Z,
+  EPREM_NODE_ROLDER_X, EPREM_NODE_ROLDER_Y, EPREM_NODE_ROLDER_Z,
+  EPREM_NODE_NFIELDS
+};
+#define EPREM_NODE_MASK(field) (1ull << (field))
+#define EPREM_NODE_MASK_ALL ((1ull << EPREM_NODE_NFIELDS) - 1ull)
+
+/* ---- per-call statistics (the driver's log line, src/eprem.c:694-716) ---- */
+typedef struct {
+  int32_t max_subcycles_change;    /* maxsubcycles_energychange                */
+  int32_t max_subcycles_focusing;  /* maxsubcycles_focusing                    */
+  int32_t max_substeps_stream;     /* largest DiffuseStreamData nsteps         */
+  int32_t pad;
+  double  min_tau;                 /* min_tau (DBL_MAX when nothing computed)  */
+  double  cell_subcycles;          /* node*E*mu cells times sub-cycles done,
+                                      summed over streaming, focusing, change  */
+} eprem_ep_stats_t;
+
+typedef struct eprem_gpu_run eprem_gpu_run;
+
+/* Create a run on the current CUDA device and allocate its device state.
+ * No counterpart in the reference beyond allocateGlobalVariables()
+ * (src/global.c:80-132) and initMPI_energeticParticlesTypes()
+ * (src/energeticParticlesTypes.c:38-69), which size the same arrays. */
+int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *params,
+                     const eprem_grids_t *grids, eprem_gpu_run **out);
+int eprem_gpu_destroy(eprem_gpu_run *run);
+
+/* f: S*N*E*M doubles from/to host memory (stream-major, mu fastest).
+ * Replaces the MPI gather/scatter of eParts (src/simCore.c:178-318); in the
+ * FP32 form the device copy is float and these convert. */
+int eprem_gpu_upload_f(eprem_gpu_run *run, const double *f_host);
+int eprem_gpu_download_f(eprem_gpu_run *run, double *f_host);
+
+/* nodes: EPREM_NODE_NFIELDS*S*N doubles, [field][stream*N+node]; only the
+ * fields whose bit is set in field_mask are copied. */
+int eprem_gpu_upload_nodes(eprem_gpu_run *run, const double *nodes_host,
+                           uint64_t field_mask);
+int eprem_gpu_download_nodes(eprem_gpu_run *run, double *nodes_host,
+                             uint64_t field_mask);
+
+/* One call of updateEnergeticParticles() (src/energeticParticles.c:70-203):
+ * numEpSteps operator-split sub-steps of streaming + isotropisation
+ * (DiffuseStreamData :2240-2490), adiabatic focusing (:1537-1803) and
+ * adiabatic change (:808-1077), with updateStreamValues
+ * (src/simCore.c:326-435), seedPopulationCheck
+ * (src/energeticParticlesBoundary.c:28-59) and GetStreamList /
+ * FindSegmentLengths (:2150-2234, :2496-2601).  Asynchronous on the run's
+ * stream; device-side failures (NaN, Inf, ds<=0, cap) are reported by the
+ * next eprem_gpu_synchronize / read_stats / download call.  t_global is
+ * accepted for interface fidelity; the MAS-heliospheric switches that read it
+ * are not supported. */
+int eprem_gpu_update_energetic_particles(eprem_gpu_run *run, double t_global);
+
+/* Statistics accumulated since the previous read (then reset), as the driver
+ * prints and resets them once per step (src/eprem.c:694-716).  Synchronizes. */
+int eprem_gpu_read_stats(eprem_gpu_run *run, eprem_ep_stats_t *stats);
+
+/* updateMhd() for the analytic Parker background, with the ideal shock
+ * (src/flow.c:36-154, 241-403, 623-651). */
+int eprem_gpu_update_mhd(eprem_gpu_run *run, double t_global);
+
+/* moveNodes(dt): Euler push of every node but the innermost of each stream by
+ * the node's flow velocity (src/simCore.c:737-785, delrFlow src/flow.c:162-196). */
+int eprem_gpu_move_nodes(eprem_gpu_run *run, double dt);
+
+/* Omnidirectional flux J = 2 E <f>_mu per (stream, node, energy), the
+ * quantity computeFlux writes (src/unifiedOutput.c:153-180), without its
+ * output unit scale.  out: S*N*E doubles, host memory.  Synchronizes. */
+int eprem_gpu_omni_flux(eprem_gpu_run *run, double *out_host);
+
+/* Wait for all work of the run; returns the first device-side failure. */
+int eprem_gpu_synchronize(eprem_gpu_run *run);
+
+/* The cudaStream_t the run launches on (as void*), and how many kernels it has
+ * launched since creation.  Measurement helpers without a reference
+ * counterpart. */
+void    *eprem_gpu_stream(eprem_gpu_run *run);
+uint64_t eprem_gpu_kernel_launches(const eprem_gpu_run *run);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *eprem_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EPREM_GPU_H */

@@ -1,0 +1,1048 @@
+/*
+ * eprem_oracle.c -- CPU restatement of EPREM's per-timestep particle update.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker that tests/, smoke()
+ * and bench.py's cpu_baseline leg compare the CUDA path against; the product
+ * library never links or calls it.
+ *
+ * Every function restates one reference function (cited file:line, paths in
+ * the predsci/eprem tree) keeping its operation order, so that with
+ * -ffp-contract=off it reproduces the reference C bit for bit; the pinning
+ * test runs both on the same states.  Layout: include/eprem_gpu.h.
+ *
+ * Restrictions (shared with the CUDA path): one species, one MPI rank's view
+ * of whole streams, no MAS heliospheric switches, no drift / shell diffusion.
+ */
+#include "eprem_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* Physical constants, src/baseTypes.h:47-86. */
+#define ORC_PI 3.1415926535897932
+#define ORC_MP 1.6726e-24
+#define ORC_MEV 1.6022e-6
+#define ORC_GEV 1.6022e-3
+#define ORC_C 2.99792458e10
+#define ORC_AU 1.495978707e13
+#define ORC_VERYSMALL 1.0e-33
+#define ORC_MZERO (ORC_MP * ORC_C * ORC_C / ORC_GEV)
+#define ORC_TAU (ORC_AU / ORC_C)
+#define ORC_DAY (ORC_TAU / (24.0 * 60.0 * 60.0))
+#define ORC_MHD_DENSITY_NORM 1.0
+#define ORC_MHD_B_NORM (sqrt(ORC_MP * ORC_MHD_DENSITY_NORM) * ORC_C)
+#define ORC_MAS_TIME_NORM 1445.87003080685
+
+/* ------------------------------------------------------------------------ */
+void orc_build_grids(int E, int M, double e_min_mev, double e_max_mev,
+                     double mass, double charge, double rigidity_power,
+                     double *egrid, double *vgrid, double *vgrid_i,
+                     double *pgrid, double *rigidity, double *mugrid,
+                     double *dlnp_out, double *dmu_out) {
+  /* src/energeticParticlesInit.c:52-89 */
+  const double one = 1.0, two = 2.0, half = 0.5;
+  double kin = e_min_mev * ORC_MEV / (ORC_MP * ORC_C * ORC_C);
+  double lnpmin = log(sqrt(kin * kin + two * kin));
+  kin = e_max_mev * ORC_MEV / (ORC_MP * ORC_C * ORC_C);
+  double lnpmax = log(sqrt(kin * kin + two * kin));
+  double dlnp = (lnpmax - lnpmin) / (E - 1.0);
+  for (int e = 0; e < E; e++) {
+    double p = exp(lnpmin + e * dlnp);
+    pgrid[e] = p;
+    egrid[e] = sqrt(one + p * p) - one;
+    vgrid[e] = p / sqrt(one + p * p);
+    vgrid_i[e] = sqrt(one + p * p) / p;
+  }
+  for (int e = 0; e < E; e++) {
+    double p = exp(lnpmin + e * dlnp);
+    rigidity[e] = (mass / charge) * p * ORC_MZERO;
+    rigidity[e] = pow(rigidity[e], rigidity_power);
+  }
+  double dmu = two / (one * M);
+  for (int m = 0; m < M; m++) {
+    double mup = -one + (m + one) * dmu;
+    double mum = -one + m * dmu;
+    mugrid[m] = half * (mup + mum);
+  }
+  *dlnp_out = dlnp;
+  *dmu_out = dmu;
+}
+
+void orc_default_params(eprem_params_t *p) {
+  /* getParams defaults (src/configuration.c:58-217) converted as in
+   * setRuntimeConstants (:325-348). */
+  memset(p, 0, sizeof(*p));
+  p->r_scale = 0.005;
+  p->t_del = 0.01041666666667 / ORC_DAY;
+  p->num_ep_steps = 30;
+  p->use_parallel_diffusion = 1;
+  p->use_adiabatic_focus = 1;
+  p->use_adiabatic_change = 1;
+  p->check_seed_population = 1;
+  p->use_ep_boundary = 1;
+  p->use_boundary_function = 1;
+  p->adiabatic_focus_alg = 1;
+  p->adiabatic_change_alg = 1;
+  p->damp_cooling = 0.0;
+  p->dsh_min = 5.0e-5;
+  p->mfp_type = 1;
+  p->lamo = 1.0;
+  p->mfp_radial_power = 2.0;
+  p->mfp_b_power = 0.75;
+  p->mhd_bs_au = 1.60e-5 / ORC_MHD_B_NORM;
+  p->bf_amplitude = 1.0;
+  p->bf_xi = 1.0;
+  p->bf_gamma = 2.0;
+  p->bf_beta = 1.7;
+  p->bf_ecutoff = 1.0;
+  p->bf_r0 = 1.0;
+  p->mhd_us = 400.0e5 / ORC_C;
+  p->mhd_ns_au = 8.30 / ORC_MHD_DENSITY_NORM;
+  p->omega_sun = (0.004144 / ORC_MAS_TIME_NORM) * ORC_TAU;
+  p->ideal_shock = 0;
+  p->ideal_shock_sharpness = 1.0;
+  p->ideal_shock_scale_length = 0.0046491;
+  p->ideal_shock_jump = 4.0;
+  p->ideal_shock_falloff = 0.0;
+  p->ideal_shock_speed = 1500e5;
+  p->ideal_shock_init_time = 0.0;
+  p->ideal_shock_theta = 1.570796;
+  p->ideal_shock_phi = 0.0;
+  p->ideal_shock_width = 0.0;
+  p->max_subcycles = 0;
+}
+
+/* sepSeedFunction, src/energeticParticlesBoundary.c:67-116. */
+double orc_seed_function(const eprem_params_t *p, double energy, double r) {
+  const double two = 2.0;
+  const double E1 = 1.0;
+  const double efac = ORC_MEV / (ORC_MP * ORC_C * ORC_C);
+  double normJ0 = p->bf_amplitude * (ORC_MP * ORC_C) / (ORC_MHD_DENSITY_NORM * ORC_MEV);
+  double normRadius = p->bf_r0 / p->r_scale;
+  double normE1 = E1 * efac;
+  double normE0 = p->bf_ecutoff * efac;
+  double radialTerm = pow((r / normRadius), -p->bf_beta);
+  double powerLawTerm = pow((energy / normE1), -p->bf_gamma);
+  double expTerm = exp(-(energy / normE0));
+  double normJHe = normJ0 * radialTerm * powerLawTerm * expTerm;
+  double normJ = normJHe / p->bf_xi;
+  double normf = normJ / (two * energy);
+  if (normf < DBL_MIN) normf = DBL_MIN;
+  return normf;
+}
+
+/* meanFreePath, src/meanFreePath.c:13-50 (mfpType 1 or 2). */
+static double orc_mfp(const eprem_params_t *p, const eprem_grids_t *g, int e,
+                      double rmag, double bmag) {
+  if (p->mfp_type == 2)
+    return g->rigidity[e] * p->lamo * pow(p->mhd_bs_au / bmag, p->mfp_b_power);
+  return g->rigidity[e] * p->lamo * pow(rmag * p->r_scale, p->mfp_radial_power);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Per-stream working storage (the reference's streamGrid/shellList/... globals
+ * of src/global.c:21-33, one set per worker thread). */
+typedef struct {
+  int *list, *ref;
+  double *ds_list, *ds_i;
+  double *f_old, *f_new, *iso, *mult, *emt, *del_fac;
+  double *nf, *nf1, *nvel, *nvavg, *ns1, *nflux, *nLP, *nLN, *nalpha;
+} orc_work_t;
+
+typedef struct {
+  const eprem_dims_t *d;
+  const eprem_params_t *p;
+  const eprem_grids_t *g;
+  double *f, *nodes;
+  int s0, s1;
+  eprem_ep_stats_t stats;
+  int status;
+  char err[256];
+} orc_job_t;
+
+#define NODE(field, s, k) nodes[(size_t)(field) * SN + (size_t)(s) * N + (k)]
+#define FIDX(s, k, e, m) ((((size_t)(s) * N + (k)) * E + (e)) * M + (m))
+
+static int orc_fail(orc_job_t *job, int code, const char *what, int s, int k) {
+  if (job->status == EPREM_GPU_OK) {
+    job->status = code;
+    snprintf(job->err, sizeof(job->err), "%s in %s (stream %d, node %d)",
+             code == EPREM_GPU_ERR_NAN   ? "NaN value"
+             : code == EPREM_GPU_ERR_INF ? "Inf value"
+                                         : "failure",
+             what, s, k);
+  }
+  return code;
+}
+
+static int orc_check(orc_job_t *job, double v, const char *what, int s, int k) {
+  /* checkNaN / checkInf, src/error.c:57-102 */
+  if (isnan(v)) return orc_fail(job, EPREM_GPU_ERR_NAN, what, s, k);
+  if (isinf(v)) return orc_fail(job, EPREM_GPU_ERR_INF, what, s, k);
+  return EPREM_GPU_OK;
+}
+
+/* updateStreamValues, src/simCore.c:326-435. */
+static void orc_stream_values(orc_job_t *job, int s) {
+  const int N = job->d->num_nodes;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  double *nodes = job->nodes;
+  const double rs = job->p->r_scale;
+  for (int k = 0; k < N; k++) {
+    double rx = NODE(EPREM_NODE_RX, s, k) * rs, ry = NODE(EPREM_NODE_RY, s, k) * rs,
+           rz = NODE(EPREM_NODE_RZ, s, k) * rs;
+    if (k == 0) {
+      double px = NODE(EPREM_NODE_RX, s, k + 1) * rs, py = NODE(EPREM_NODE_RY, s, k + 1) * rs,
+             pz = NODE(EPREM_NODE_RZ, s, k + 1) * rs;
+      NODE(EPREM_NODE_DS, s, k) =
+          sqrt((px - rx) * (px - rx) + (py - ry) * (py - ry) + (pz - rz) * (pz - rz));
+      NODE(EPREM_NODE_BMAG_MINUS, s, k) = NODE(EPREM_NODE_BMAG, s, k);
+      NODE(EPREM_NODE_BMAG_PLUS, s, k) = NODE(EPREM_NODE_BMAG, s, k + 1);
+    } else if (k == N - 1) {
+      double mx = NODE(EPREM_NODE_RX, s, k - 1) * rs, my = NODE(EPREM_NODE_RY, s, k - 1) * rs,
+             mz = NODE(EPREM_NODE_RZ, s, k - 1) * rs;
+      NODE(EPREM_NODE_DS, s, k) =
+          sqrt((rx - mx) * (rx - mx) + (ry - my) * (ry - my) + (rz - mz) * (rz - mz));
+      NODE(EPREM_NODE_BMAG_MINUS, s, k) = NODE(EPREM_NODE_BMAG, s, k - 1);
+      NODE(EPREM_NODE_BMAG_PLUS, s, k) = NODE(EPREM_NODE_BMAG, s, k);
+    } else {
+      double px = NODE(EPREM_NODE_RX, s, k + 1) * rs, py = NODE(EPREM_NODE_RY, s, k + 1) * rs,
+             pz = NODE(EPREM_NODE_RZ, s, k + 1) * rs;
+      double mx = NODE(EPREM_NODE_RX, s, k - 1) * rs, my = NODE(EPREM_NODE_RY, s, k - 1) * rs,
+             mz = NODE(EPREM_NODE_RZ, s, k - 1) * rs;
+      double dsPlus = sqrt((px - rx) * (px - rx) + (py - ry) * (py - ry) + (pz - rz) * (pz - rz));
+      double dsMinus = sqrt((rx - mx) * (rx - mx) + (ry - my) * (ry - my) + (rz - mz) * (rz - mz));
+      NODE(EPREM_NODE_DS, s, k) = 0.5 * (dsPlus + dsMinus);
+      NODE(EPREM_NODE_BMAG_MINUS, s, k) = NODE(EPREM_NODE_BMAG, s, k - 1);
+      NODE(EPREM_NODE_BMAG_PLUS, s, k) = NODE(EPREM_NODE_BMAG, s, k + 1);
+    }
+  }
+}
+
+/* seedPopulationCheck, src/energeticParticlesBoundary.c:28-59. */
+static void orc_seed_check(orc_job_t *job, int s) {
+  const int N = job->d->num_nodes, E = job->d->num_energies, M = job->d->num_mu;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  double *nodes = job->nodes, *f = job->f;
+  for (int k = 0; k < N; k++)
+    for (int e = 0; e < E; e++) {
+      double seed = orc_seed_function(job->p, job->g->egrid[e], NODE(EPREM_NODE_RMAG, s, k));
+      for (int m = 0; m < M; m++)
+        if (f[FIDX(s, k, e, m)] < seed) f[FIDX(s, k, e, m)] = seed;
+    }
+}
+
+static double orc_dist(const double *nodes, size_t SN, int N, int s, int a, int b,
+                       double rs) {
+  /* |r_a - r_b| with positions scaled to AU first, summed x,y,z in order as in
+   * src/energeticParticles.c:2193-2203 and :2519-2529. */
+  double ax = NODE(EPREM_NODE_RX, s, a) * rs, ay = NODE(EPREM_NODE_RY, s, a) * rs,
+         az = NODE(EPREM_NODE_RZ, s, a) * rs;
+  double bx = NODE(EPREM_NODE_RX, s, b) * rs, by = NODE(EPREM_NODE_RY, s, b) * rs,
+         bz = NODE(EPREM_NODE_RZ, s, b) * rs;
+  return sqrt((ax - bx) * (ax - bx) + (ay - by) * (ay - by) + (az - bz) * (az - bz));
+}
+
+/* GetStreamList (src/energeticParticles.c:2150-2234) and FindSegmentLengths
+ * (:2496-2601).  Returns the list size, or a negative status. */
+static int orc_stream_list(orc_job_t *job, orc_work_t *w, int s, double *dsMin_out) {
+  const int N = job->d->num_nodes;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  const double *nodes = job->nodes;
+  const double rs = job->p->r_scale;
+  const double dshmin = job->p->dsh_min;
+  int L = 0, down = 0, up;
+  for (int shell = 0; shell < N; shell++) {
+    if (shell < N - 1) {
+      up = shell + 1;
+    } else {
+      up = shell;
+      down = shell - 1;
+    }
+    double dsh = orc_dist(nodes, SN, N, s, up, down, rs);
+    if ((dsh > dshmin) || (shell == N - 1)) {
+      w->list[L++] = shell;
+      w->ref[shell] = shell;
+      down = shell + 1;
+    } else {
+      w->ref[shell] = shell + 1;
+      int sp = shell - 1;
+      while ((sp >= 0) && (w->ref[sp] != sp)) {
+        w->ref[sp] = w->ref[sp + 1];
+        sp--;
+      }
+    }
+  }
+  if (L < 3) {
+    orc_fail(job, EPREM_GPU_ERR_STATE, "GetStreamList (fewer than 3 nodes kept)", s, L);
+    return EPREM_GPU_ERR_STATE;
+  }
+  double dsMin = 10000.0 * rs;
+  for (int sl = 0; sl < L; sl++) {
+    int th = w->list[sl];
+    if (sl == 0) {
+      double dsh = orc_dist(nodes, SN, N, s, w->list[sl + 1], th, rs);
+      if (dsh < dsMin) dsMin = dsh;
+      w->ds_list[sl] = dsh;
+    } else if (sl == L - 1) {
+      double dsh = orc_dist(nodes, SN, N, s, th, w->list[sl - 1], rs);
+      if (dsh < dsMin) dsMin = dsh;
+      w->ds_list[sl] = dsh;
+    } else {
+      double ds1 = orc_dist(nodes, SN, N, s, w->list[sl + 1], th, rs);
+      double ds9 = orc_dist(nodes, SN, N, s, th, w->list[sl - 1], rs);
+      if (ds1 < dsMin) dsMin = ds1;
+      if (ds9 < dsMin) dsMin = ds9;
+      w->ds_list[sl] = 0.5 * (ds1 + ds9);
+    }
+    if (dsMin <= 0.0) {
+      orc_fail(job, EPREM_GPU_ERR_DS, "FindSegmentLengths(): Underflow in ds", s, th);
+      return EPREM_GPU_ERR_DS;
+    }
+    w->ds_i[sl] = 1.0 / w->ds_list[sl];
+  }
+  *dsMin_out = dsMin;
+  return L;
+}
+
+/* DiffuseStreamData, src/energeticParticles.c:2240-2490 (species 0). */
+static int orc_diffuse_stream(orc_job_t *job, orc_work_t *w, int s, int L, double dsMin,
+                              double dt) {
+  const eprem_params_t *p = job->p;
+  const eprem_grids_t *g = job->g;
+  const int N = job->d->num_nodes, E = job->d->num_energies, M = job->d->num_mu;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  double *nodes = job->nodes, *f = job->f;
+  const double one = 1.0;
+  const double NUM_MUSTEPS_I = one / M;
+  const int cap = p->max_subcycles > 0 ? p->max_subcycles : 1000000;
+  double *f_old = w->f_old, *f_new = w->f_new, *iso_vec = w->iso;
+  double sep_seed_vec[3];
+  for (int e = 0; e < E; e++) {
+    double v = g->vgrid[e], vi = g->vgrid_i[e];
+    double dtMin = 0.4 * dsMin * vi;
+    double nst = floor(dt / dtMin + one);
+    if (!(nst <= (double)cap))
+      return orc_fail(job, EPREM_GPU_ERR_SUBCYCLES, "DiffuseStreamData", s, e);
+    int nsteps = (int)nst;
+    if (nsteps > job->stats.max_substeps_stream) job->stats.max_substeps_stream = nsteps;
+    double dtProp = dt / (one * nsteps);
+    double dtProp_i = one / dtProp;
+    for (int sl = 0; sl < L; sl++) {
+      int sh = w->list[sl];
+      double tau = vi * orc_mfp(p, g, e, NODE(EPREM_NODE_RMAG, s, sh), NODE(EPREM_NODE_BMAG, s, sh));
+      if (dtProp > tau)
+        w->mult[sl] = w->ds_i[sl] * tau * dtProp_i;
+      else
+        w->mult[sl] = w->ds_i[sl] * one;
+      w->emt[sl] = exp(-dtProp / tau);
+    }
+    for (int sl = 0; sl < 3; sl++)
+      sep_seed_vec[sl] = orc_seed_function(p, g->egrid[e], NODE(EPREM_NODE_RMAG, s, w->list[sl]));
+    for (int m = 0; m < M; m++) w->del_fac[m] = v * dtProp * g->mugrid[m];
+    for (int m = 0; m < M; m++)
+      for (int sl = 0; sl < L; sl++) f_old[(size_t)L * m + sl] = f[FIDX(s, w->list[sl], e, m)];
+    for (int step = 0; step < nsteps; step++) {
+      if ((p->use_ep_boundary > 0) && (p->use_boundary_function > 0))
+        for (int m = 0; m < M; m++)
+          for (int sl = 0; sl < 3; sl++) f_old[(size_t)L * m + sl] = sep_seed_vec[sl];
+      for (int m = 0; m < M; m++) {
+        double del_fac = w->del_fac[m];
+        double *fo = f_old + (size_t)L * m, *fn = f_new + (size_t)L * m;
+        if (g->mugrid[m] >= 0.0) {
+          fn[0] = fo[0];
+          for (int sl = 1; sl < L; sl++)
+            fn[sl] = fo[sl] + w->mult[sl] * del_fac * (fo[sl - 1] - fo[sl]);
+        } else {
+          fn[L - 1] = fo[L - 1];
+          for (int sl = 0; sl < L - 1; sl++)
+            fn[sl] = fo[sl] + w->mult[sl] * del_fac * (fo[sl] - fo[sl + 1]);
+        }
+      }
+      for (int sl = 0; sl < L; sl++) iso_vec[sl] = 0.0;
+      for (int m = 0; m < M; m++)
+        for (int sl = 0; sl < L; sl++) iso_vec[sl] = iso_vec[sl] + f_new[(size_t)L * m + sl];
+      for (int m = 0; m < M; m++)
+        for (int sl = 0; sl < L; sl++) {
+          double iso = NUM_MUSTEPS_I * iso_vec[sl];
+          f_old[(size_t)L * m + sl] = iso + (f_new[(size_t)L * m + sl] - iso) * w->emt[sl];
+        }
+    }
+    job->stats.cell_subcycles += (double)nsteps * L * M;
+    for (int m = 0; m < M; m++)
+      for (int sl = 0; sl < L; sl++) f[FIDX(s, w->list[sl], e, m)] = f_old[(size_t)L * m + sl];
+    for (int m = 0; m < M; m++)
+      for (int sh = 0; sh < N; sh++) {
+        if (sh != w->ref[sh]) f[FIDX(s, sh, e, m)] = f[FIDX(s, w->ref[sh], e, m)];
+        double val = f[FIDX(s, sh, e, m)];
+        if (orc_check(job, val, "Diffuse Stream Data", s, sh)) return job->status;
+        if (val < DBL_MIN) f[FIDX(s, sh, e, m)] = DBL_MIN;
+      }
+  }
+  return EPREM_GPU_OK;
+}
+
+/* AdiabaticFocusing_Operator_Upwind, src/energeticParticles.c:1809-1895, for
+ * one node: f, f1 [E][M]; v_avg [E][M+1]. */
+static void orc_focus_op_upwind(double *f1, const double *f, const double *v_avg,
+                                double *flux, int E, int M, double dmu) {
+  const double upwind = 1.0;
+  double dmu_i = 1.0 / dmu;
+  for (int e = 0; e < E; e++)
+    for (int m = 1; m < M; m++) {
+      double va = v_avg[e * (M + 1) + m];
+      double cce = copysign(upwind, va);
+      flux[e * (M + 1) + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[e * M + m - 1]);
+    }
+  for (int e = 0; e < E; e++)
+    for (int m = 1; m < M - 1; m++)
+      f1[e * M + m] = (flux[e * (M + 1) + m + 1] - flux[e * (M + 1) + m]) * dmu_i;
+  for (int e = 0; e < E; e++) {
+    double va = v_avg[e * (M + 1) + 1];
+    if (va <= 0)
+      f1[e * M + 0] = va * f[e * M + 1] * dmu_i;
+    else
+      f1[e * M + 0] = va * f[e * M + 0] * dmu_i;
+    va = v_avg[e * (M + 1) + M - 1];
+    if (va >= 0)
+      f1[e * M + M - 1] = va * (-f[e * M + M - 2]) * dmu_i;
+    else
+      f1[e * M + M - 1] = va * (-f[e * M + M - 1]) * dmu_i;
+  }
+}
+
+/* WENO3 building blocks shared by both operators
+ * (src/energeticParticles.c:1311-1346 and :2031-2066). */
+static double orc_weno_flux(double LNm2, double LNm1, double LN0, double LP_1, double LP0,
+                            double LPp1, double cc, double cp, double mt, double cpt,
+                            double pt, double mct, double eps) {
+  /* cc = D_C_CPt, (...) names follow the reference's D_* constants */
+  double D_C_CPt = cc, D_C_MCt = cp, D_M_Tt = mt, D_CP_Tt = cpt, D_P_Tt = pt, D_MC_Tt = mct;
+  double p0m = (1.0 + D_C_MCt) * LNm1 - D_C_MCt * LNm2;
+  double p1m = D_C_MCt * LNm1 + D_C_CPt * LN0;
+  double p0p = (1.0 + D_C_CPt) * LP0 - D_C_CPt * LPp1;
+  double p1p = D_C_CPt * LP0 + D_C_MCt * LP_1;
+  double B0m = 4.0 * pow((D_C_MCt * (LNm1 - LNm2)), 2);
+  double B1m = 4.0 * pow((D_C_CPt * (LN0 - LNm1)), 2);
+  double B0p = 4.0 * pow((D_C_CPt * (LPp1 - LP0)), 2);
+  double B1p = 4.0 * pow((D_C_MCt * (LP0 - LP_1)), 2);
+  double w0m = D_P_Tt / pow((eps + B0m), 2);
+  double w1m = D_MC_Tt / pow((eps + B1m), 2);
+  double w0p = D_M_Tt / pow((eps + B0p), 2);
+  double w1p = D_CP_Tt / pow((eps + B1p), 2);
+  double wm_sum = w0m + w1m;
+  double wp_sum = w0p + w1p;
+  double OM0m = w0m / wm_sum, OM1m = w1m / wm_sum, OM0p = w0p / wp_sum, OM1p = w1p / wp_sum;
+  double um = OM0m * p0m + OM1m * p1m;
+  double up = OM0p * p0p + OM1p * p1p;
+  return up + um;
+}
+
+/* max |v| over v_avg[i] for i in [lo, hi] (inclusive), the alpha of the WENO3
+ * operators; max is order-independent so the reference's unrolled
+ * comparisons (:1237-1295, :1957-2015) reduce to this. */
+static double orc_alpha(const double *va, int stride, int lo, int hi) {
+  double a = 0.0;
+  for (int i = lo; i <= hi; i++) {
+    double x = fabs(va[i * stride]);
+    if (i == lo || x > a) a = x;
+  }
+  return a;
+}
+
+/* AdiabaticFocusing_Operator_WENO3, src/energeticParticles.c:1902-2144. */
+static void orc_focus_op_weno3(double *f1, const double *f, const double *v_avg, double *flux,
+                               double *LP, double *LN, double *alpha, int E, int M, double dmu) {
+  const double upwind = 1.0;
+  const double D_C_CPt = 1 / 2.0, D_C_MCt = 1 / 2.0, D_M_Tt = 1 / 3.0, D_CP_Tt = 2 / 3.0,
+               D_P_Tt = 1 / 3.0, D_MC_Tt = 2 / 3.0;
+  const double weno_eps = 10.0 * sqrt(DBL_MIN);
+  for (int e = 0; e < E; e++) {
+    const double *va = v_avg + e * (M + 1);
+    for (int m = 2; m < M - 2; m++) alpha[e * M + m] = orc_alpha(va, 1, m - 2, m + 3);
+    alpha[e * M + 0] = orc_alpha(va, 1, 0, 3);
+    alpha[e * M + 1] = orc_alpha(va, 1, 0, 4);
+    alpha[e * M + M - 2] = orc_alpha(va, 1, M - 4, M);
+    alpha[e * M + M - 1] = orc_alpha(va, 1, M - 3, M);
+  }
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      LP[e * M + m] = 0.5 * f[e * M + m] * v_avg[e * (M + 1) + m + 1] - alpha[e * M + m];
+      LN[e * M + m] = 0.5 * f[e * M + m] * v_avg[e * (M + 1) + m] + alpha[e * M + m];
+    }
+  for (int e = 0; e < E; e++)
+    for (int m = 2; m < M - 1; m++) {
+      const double *ln = LN + e * M, *lp = LP + e * M;
+      flux[e * (M + 1) + m] = orc_weno_flux(ln[m - 2], ln[m - 1], ln[m], lp[m - 1], lp[m], lp[m + 1],
+                                            D_C_CPt, D_C_MCt, D_M_Tt, D_CP_Tt, D_P_Tt, D_MC_Tt,
+                                            weno_eps);
+    }
+  for (int e = 0; e < E; e++) {
+    int m = 1;
+    double va = v_avg[e * (M + 1) + m];
+    double cce = copysign(upwind, va);
+    flux[e * (M + 1) + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[e * M + m - 1]);
+    m = M - 1;
+    va = v_avg[e * (M + 1) + m];
+    cce = copysign(upwind, va);
+    flux[e * (M + 1) + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[e * M + m - 1]);
+  }
+  for (int e = 0; e < E; e++)
+    for (int m = 1; m < M - 1; m++)
+      f1[e * M + m] = (flux[e * (M + 1) + m + 1] - flux[e * (M + 1) + m]) / dmu;
+  for (int e = 0; e < E; e++) {
+    double va = v_avg[e * (M + 1) + 1];
+    if (va <= 0)
+      f1[e * M + 0] = va * f[e * M + 1] / dmu;
+    else
+      f1[e * M + 0] = va * f[e * M + 0] / dmu;
+    va = v_avg[e * (M + 1) + M - 1];
+    if (va >= 0)
+      f1[e * M + M - 1] = va * (-f[e * M + M - 2]) / dmu;
+    else
+      f1[e * M + M - 1] = va * (-f[e * M + M - 1]) / dmu;
+  }
+}
+
+/* One RK3-TVD or Euler advance of f over n sub-cycles of length dts, with the
+ * operator chosen by alg, as in the sub-cycle loops of AdiabaticFocusing
+ * (:1677-1763) and AdiabaticChange (:952-1038). */
+typedef void (*orc_op_fn)(void *ctx, double *f1, const double *f);
+
+static void orc_subcycle(int alg, int n, double dts, double *f, double *f1, double *s1,
+                         int cells, orc_op_fn op, void *ctx) {
+  if (alg == 2 || alg == 3) {
+    for (int s = 0; s < n; s++) {
+      op(ctx, f1, f);
+      for (int i = 0; i < cells; i++) s1[i] = f[i] - dts * f1[i];
+      op(ctx, f1, s1);
+      for (int i = 0; i < cells; i++)
+        s1[i] = (3.0 / 4.0) * f[i] + (1.0 / 4.0) * s1[i] - (1.0 / 4.0) * dts * f1[i];
+      op(ctx, f1, s1);
+      for (int i = 0; i < cells; i++)
+        f[i] = (1.0 / 3.0) * f[i] + (2.0 / 3.0) * s1[i] - (2.0 / 3.0) * dts * f1[i];
+    }
+  } else {
+    for (int s = 0; s < n; s++) {
+      op(ctx, f1, f);
+      for (int i = 0; i < cells; i++) f[i] = f[i] - dts * f1[i];
+    }
+  }
+}
+
+typedef struct {
+  orc_work_t *w;
+  int alg, E, M;
+  double d;           /* dmu or dlnp */
+  double bc0, bc1;    /* change only: log seed at E0 and E_last */
+  const eprem_params_t *p;
+  const eprem_grids_t *g;
+  double rmag;
+} orc_opctx_t;
+
+static void orc_focus_op(void *vctx, double *f1, const double *f) {
+  orc_opctx_t *c = (orc_opctx_t *)vctx;
+  if (c->alg == 3)
+    orc_focus_op_weno3(f1, f, c->w->nvavg, c->w->nflux, c->w->nLP, c->w->nLN, c->w->nalpha,
+                       c->E, c->M, c->d);
+  else
+    orc_focus_op_upwind(f1, f, c->w->nvavg, c->w->nflux, c->E, c->M, c->d);
+}
+
+/* AdiabaticChange_Operator_Upwind, src/energeticParticles.c:1084-1176:
+ * arrays [E][M], v_avg [E+1][M]. */
+static void orc_change_op_upwind(double *f1, const double *f, const double *v_avg, double *flux,
+                                 int E, int M, double dlnp, double bc_val0, double bc_val1) {
+  const double upwind = 1.0;
+  double dlnp_i = 1.0 / dlnp;
+  for (int e = 1; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      double va = v_avg[e * M + m];
+      double cce = copysign(upwind, va);
+      flux[e * M + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[(e - 1) * M + m]);
+    }
+  for (int e = 1; e < E - 1; e++)
+    for (int m = 0; m < M; m++)
+      f1[e * M + m] = (flux[(e + 1) * M + m] - flux[e * M + m]) * dlnp_i;
+  for (int m = 0; m < M; m++) {
+    double va = v_avg[1 * M + m];
+    if (va <= 0)
+      f1[m] = va * (f[1 * M + m] - f[m]) * dlnp_i;
+    else
+      f1[m] = va * (f[m] - bc_val0) * dlnp_i;
+    va = v_avg[(E - 1) * M + m];
+    if (va >= 0)
+      f1[(E - 1) * M + m] = va * (f[(E - 1) * M + m] - f[(E - 2) * M + m]) * dlnp_i;
+    else
+      f1[(E - 1) * M + m] = va * (bc_val1 - f[(E - 1) * M + m]) * dlnp_i;
+  }
+}
+
+/* AdiabaticChange_Operator_WENO3, src/energeticParticles.c:1182-1427. */
+static void orc_change_op_weno3(double *f1, const double *f, const double *v_avg, double *flux,
+                                double *LP, double *LN, double *alpha, int E, int M, double dlnp,
+                                double bc_val0, double bc_val1) {
+  const double upwind = 1.0;
+  const double D_C_CPt = 0.5, D_C_MCt = 0.5, D_M_Tt = 1.0 / 3.0, D_CP_Tt = 2.0 / 3.0,
+               D_P_Tt = 1.0 / 3.0, D_MC_Tt = 2.0 / 3.0;
+  const double weno_eps = 10.0 * sqrt(DBL_MIN);
+  for (int m = 0; m < M; m++) {
+    const double *va = v_avg + m;
+    for (int e = 2; e < E - 2; e++) alpha[e * M + m] = orc_alpha(va, M, e - 2, e + 3);
+    alpha[0 * M + m] = orc_alpha(va, M, 0, 3);
+    alpha[1 * M + m] = orc_alpha(va, M, 0, 4);
+    alpha[(E - 2) * M + m] = orc_alpha(va, M, E - 4, E);
+    alpha[(E - 1) * M + m] = orc_alpha(va, M, E - 3, E);
+  }
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      LP[e * M + m] = 0.5 * f[e * M + m] * v_avg[(e + 1) * M + m] - alpha[e * M + m];
+      LN[e * M + m] = 0.5 * f[e * M + m] * v_avg[e * M + m] + alpha[e * M + m];
+    }
+  for (int e = 2; e < E - 1; e++)
+    for (int m = 0; m < M; m++)
+      flux[e * M + m] = orc_weno_flux(LN[(e - 2) * M + m], LN[(e - 1) * M + m], LN[e * M + m],
+                                      LP[(e - 1) * M + m], LP[e * M + m], LP[(e + 1) * M + m],
+                                      D_C_CPt, D_C_MCt, D_M_Tt, D_CP_Tt, D_P_Tt, D_MC_Tt, weno_eps);
+  for (int m = 0; m < M; m++) {
+    int e = 1;
+    double va = v_avg[e * M + m];
+    double cce = copysign(upwind, va);
+    flux[e * M + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[(e - 1) * M + m]);
+    e = E - 1;
+    va = v_avg[e * M + m];
+    cce = copysign(upwind, va);
+    flux[e * M + m] = va * 0.5 * ((1.0 - cce) * f[e * M + m] + (1.0 + cce) * f[(e - 1) * M + m]);
+  }
+  for (int e = 1; e < E - 1; e++)
+    for (int m = 0; m < M; m++) f1[e * M + m] = (flux[(e + 1) * M + m] - flux[e * M + m]) / dlnp;
+  for (int m = 0; m < M; m++) {
+    double va = v_avg[1 * M + m];
+    if (va <= 0)
+      f1[m] = va * (f[1 * M + m] - f[m]) / dlnp;
+    else
+      f1[m] = va * (f[m] - bc_val0) / dlnp;
+    va = v_avg[(E - 1) * M + m];
+    if (va >= 0)
+      f1[(E - 1) * M + m] = va * (f[(E - 1) * M + m] - f[(E - 2) * M + m]) / dlnp;
+    else
+      f1[(E - 1) * M + m] = va * (bc_val1 - f[(E - 1) * M + m]) / dlnp;
+  }
+}
+
+static void orc_change_op(void *vctx, double *f1, const double *f) {
+  orc_opctx_t *c = (orc_opctx_t *)vctx;
+  if (c->alg == 3)
+    orc_change_op_weno3(f1, f, c->w->nvavg, c->w->nflux, c->w->nLP, c->w->nLN, c->w->nalpha, c->E,
+                        c->M, c->d, c->bc0, c->bc1);
+  else
+    orc_change_op_upwind(f1, f, c->w->nvavg, c->w->nflux, c->E, c->M, c->d, c->bc0, c->bc1);
+}
+
+/* AdiabaticFocusing for one node, src/energeticParticles.c:1581-1792. */
+static int orc_focus_node(orc_job_t *job, orc_work_t *w, int s, int k, double dt) {
+  const eprem_params_t *p = job->p;
+  const eprem_grids_t *g = job->g;
+  const int N = job->d->num_nodes, E = job->d->num_energies, M = job->d->num_mu;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  double *nodes = job->nodes, *f = job->f;
+  const double safety_factor = 0.9, half = 0.5, one = 1.0, two = 2.0, three = 3.0;
+  const int cap = p->max_subcycles > 0 ? p->max_subcycles : 1000000;
+  double dt_full = dt * p->num_ep_steps;
+  double DuParDt = NODE(EPREM_NODE_DUPAR, s, k) / dt_full;
+  double b = two * (NODE(EPREM_NODE_DLNN, s, k) / dt_full) - three * (NODE(EPREM_NODE_DLNB, s, k) / dt_full);
+  double bp = NODE(EPREM_NODE_BMAG_PLUS, s, k), bm = NODE(EPREM_NODE_BMAG_MINUS, s, k);
+  double dlnBds;
+  if ((bp == 0.0) || (bm == 0.0))
+    dlnBds = 0.0;
+  else
+    dlnBds = (log(bp) - log(bm)) / (two * NODE(EPREM_NODE_DS, s, k) + DBL_MIN);
+  double vel_abs_max = 0.0;
+  double *fn = w->nf, *vel = w->nvel, *v_avg = w->nvavg;
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      fn[e * M + m] = f[FIDX(s, k, e, m)];
+      double muval = g->mugrid[m];
+      double a = -g->vgrid[e] * dlnBds - (two / g->vgrid[e]) * DuParDt;
+      vel[e * M + m] = half * (one - muval * muval) * (a + muval * b);
+    }
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M - 1; m++) {
+      double va = half * (vel[e * M + m + 1] + vel[e * M + m]);
+      v_avg[e * (M + 1) + m + 1] = va;
+      if (fabs(va) > vel_abs_max) vel_abs_max = fabs(va);
+    }
+  for (int e = 0; e < E; e++) {
+    v_avg[e * (M + 1) + 0] = v_avg[e * (M + 1) + 1];
+    v_avg[e * (M + 1) + M] = v_avg[e * (M + 1) + M - 1];
+  }
+  double dt_stable = safety_factor * g->dmu / vel_abs_max;
+  double nsub = ceil(dt / dt_stable);
+  if (!(nsub <= (double)cap))
+    return orc_fail(job, EPREM_GPU_ERR_SUBCYCLES, "Adiabatic Focusing", s, k);
+  int N_sub = (int)nsub;
+  if (N_sub > job->stats.max_subcycles_focusing) job->stats.max_subcycles_focusing = N_sub;
+  double dt_sub = dt / N_sub;
+  orc_opctx_t ctx = {w, p->adiabatic_focus_alg, E, M, g->dmu, 0.0, 0.0, p, g, 0.0};
+  orc_subcycle(p->adiabatic_focus_alg, N_sub, dt_sub, fn, w->nf1, w->ns1, E * M, orc_focus_op, &ctx);
+  job->stats.cell_subcycles += (double)N_sub * E * M;
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      double val = fn[e * M + m];
+      f[FIDX(s, k, e, m)] = val;
+      if (orc_check(job, val, "Adiabatic Focusing", s, k)) return job->status;
+      if (val < DBL_MIN) f[FIDX(s, k, e, m)] = DBL_MIN;
+    }
+  return EPREM_GPU_OK;
+}
+
+/* AdiabaticChange for one node, src/energeticParticles.c:843-1069. */
+static int orc_change_node(orc_job_t *job, orc_work_t *w, int s, int k, double dt) {
+  const eprem_params_t *p = job->p;
+  const eprem_grids_t *g = job->g;
+  const int N = job->d->num_nodes, E = job->d->num_energies, M = job->d->num_mu;
+  const size_t SN = (size_t)job->d->num_streams * N;
+  double *nodes = job->nodes, *f = job->f;
+  const double safety_factor = 0.9, half = 0.5, one = 1.0;
+  const int cap = p->max_subcycles > 0 ? p->max_subcycles : 1000000;
+  double vel_abs_max = 0.0;
+  double dt_full = dt * p->num_ep_steps;
+  double DlnBDt = NODE(EPREM_NODE_DLNB, s, k) / dt_full;
+  double DlnNDt = NODE(EPREM_NODE_DLNN, s, k) / dt_full;
+  double cool_damp_fac = (DlnNDt < 0) ? 1.0 - p->damp_cooling : 1.0;
+  double DuParDt = NODE(EPREM_NODE_DUPAR, s, k) / dt_full;
+  double *fl = w->nf, *vel = w->nvel, *v_avg = w->nvavg;
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      fl[e * M + m] = log(f[FIDX(s, k, e, m)]);
+      double muval = g->mugrid[m];
+      double a = -muval * DuParDt;
+      double b = muval * muval * (DlnNDt - DlnBDt) + half * (one - muval * muval) * DlnBDt;
+      vel[e * M + m] = cool_damp_fac * (a * g->vgrid_i[e] + b);
+      if (fabs(vel[e * M + m]) > vel_abs_max) vel_abs_max = fabs(vel[e * M + m]);
+    }
+  for (int e = 0; e < E - 1; e++)
+    for (int m = 0; m < M; m++)
+      v_avg[(e + 1) * M + m] = half * (vel[(e + 1) * M + m] + vel[e * M + m]);
+  for (int m = 0; m < M; m++) {
+    v_avg[0 * M + m] = v_avg[1 * M + m];
+    v_avg[E * M + m] = v_avg[(E - 1) * M + m];
+  }
+  double dt_stable = safety_factor * g->dlnp / vel_abs_max;
+  double nsub = ceil(dt / dt_stable);
+  if (!(nsub <= (double)cap))
+    return orc_fail(job, EPREM_GPU_ERR_SUBCYCLES, "Adiabatic Change", s, k);
+  int N_sub = (int)nsub;
+  if (N_sub > job->stats.max_subcycles_change) job->stats.max_subcycles_change = N_sub;
+  double dt_sub = dt / N_sub;
+  double rmag = NODE(EPREM_NODE_RMAG, s, k);
+  orc_opctx_t ctx = {w, p->adiabatic_change_alg, E, M, g->dlnp,
+                     log(orc_seed_function(p, g->egrid[0], rmag)),
+                     log(orc_seed_function(p, g->egrid[E - 1], rmag)), p, g, rmag};
+  orc_subcycle(p->adiabatic_change_alg, N_sub, dt_sub, fl, w->nf1, w->ns1, E * M, orc_change_op, &ctx);
+  job->stats.cell_subcycles += (double)N_sub * E * M;
+  for (int e = 0; e < E; e++)
+    for (int m = 0; m < M; m++) {
+      double val = exp(fl[e * M + m]);
+      f[FIDX(s, k, e, m)] = val;
+      if (orc_check(job, val, "Adiabatic Change", s, k)) return job->status;
+      if (val < DBL_MIN) f[FIDX(s, k, e, m)] = DBL_MIN;
+    }
+  return EPREM_GPU_OK;
+}
+
+static void orc_work_alloc(orc_work_t *w, int N, int E, int M) {
+  size_t nm = (size_t)N * M, em = (size_t)(E + 1) * (M + 1);
+  w->list = (int *)malloc(sizeof(int) * N);
+  w->ref = (int *)malloc(sizeof(int) * N);
+  w->ds_list = (double *)malloc(sizeof(double) * N);
+  w->ds_i = (double *)malloc(sizeof(double) * N);
+  w->f_old = (double *)malloc(sizeof(double) * nm);
+  w->f_new = (double *)malloc(sizeof(double) * nm);
+  w->iso = (double *)malloc(sizeof(double) * N);
+  w->mult = (double *)malloc(sizeof(double) * N);
+  w->emt = (double *)malloc(sizeof(double) * N);
+  w->del_fac = (double *)malloc(sizeof(double) * M);
+  w->nf = (double *)malloc(sizeof(double) * em);
+  w->nf1 = (double *)malloc(sizeof(double) * em);
+  w->nvel = (double *)malloc(sizeof(double) * em);
+  w->nvavg = (double *)malloc(sizeof(double) * em);
+  w->ns1 = (double *)malloc(sizeof(double) * em);
+  w->nflux = (double *)malloc(sizeof(double) * em);
+  w->nLP = (double *)malloc(sizeof(double) * em);
+  w->nLN = (double *)malloc(sizeof(double) * em);
+  w->nalpha = (double *)malloc(sizeof(double) * em);
+}
+
+static void orc_work_free(orc_work_t *w) {
+  free(w->list); free(w->ref); free(w->ds_list); free(w->ds_i); free(w->f_old);
+  free(w->f_new); free(w->iso); free(w->mult); free(w->emt); free(w->del_fac);
+  free(w->nf); free(w->nf1); free(w->nvel); free(w->nvavg); free(w->ns1);
+  free(w->nflux); free(w->nLP); free(w->nLN); free(w->nalpha);
+}
+
+/* updateEnergeticParticles (src/energeticParticles.c:70-203) for the streams
+ * of one job.  The reference loops sub-steps outermost and, inside each,
+ * streams all streams before focusing/changing them; the streams share no
+ * data, so running each stream's sub-steps back to back gives the same
+ * values. */
+static void *orc_job_run(void *arg) {
+  orc_job_t *job = (orc_job_t *)arg;
+  const eprem_dims_t *d = job->d;
+  const eprem_params_t *p = job->p;
+  const eprem_grids_t *g = job->g;
+  const int N = d->num_nodes, E = d->num_energies;
+  const size_t SN = (size_t)d->num_streams * N;
+  double *nodes = job->nodes;
+  orc_work_t w;
+  orc_work_alloc(&w, N, E, d->num_mu);
+  double dt = p->t_del / (1.0 * p->num_ep_steps);
+  for (int s = job->s0; s < job->s1 && job->status == EPREM_GPU_OK; s++) {
+    for (int step = 0; step < p->num_ep_steps; step++) {
+      orc_stream_values(job, s);
+      if (p->check_seed_population > 0) orc_seed_check(job, s);
+      if (p->use_parallel_diffusion > 0) {
+        double dsMin;
+        int L = orc_stream_list(job, &w, s, &dsMin);
+        if (L < 0) break;
+        if (orc_diffuse_stream(job, &w, s, L, dsMin, dt)) break;
+      }
+      for (int e = 0; e < E; e++)
+        for (int k = 1; k < N; k++) {
+          double tau = orc_mfp(p, g, e, NODE(EPREM_NODE_RMAG, s, k), NODE(EPREM_NODE_BMAG, s, k)) *
+                       g->vgrid_i[e];
+          if (tau < job->stats.min_tau) job->stats.min_tau = tau;
+        }
+      if (p->use_adiabatic_focus > 0)
+        for (int k = 1; k < N; k++)
+          if (orc_focus_node(job, &w, s, k, dt)) break;
+      if (job->status) break;
+      if (p->use_adiabatic_change > 0)
+        for (int k = 1; k < N; k++)
+          if (orc_change_node(job, &w, s, k, dt)) break;
+      if (job->status) break;
+    }
+  }
+  orc_work_free(&w);
+  return NULL;
+}
+
+static int orc_validate(const eprem_dims_t *d, const eprem_params_t *p, char *errbuf) {
+  const char *why = NULL;
+  if (d->num_species != 1) why = "num_species must be 1";
+  else if (d->num_nodes < 3) why = "num_nodes must be >= 3";
+  else if (d->num_energies < 2 || d->num_mu < 2) why = "num_energies and num_mu must be >= 2";
+  else if ((p->adiabatic_focus_alg == 3 && d->num_mu < 4) ||
+           (p->adiabatic_change_alg == 3 && d->num_energies < 4))
+    why = "WENO3 needs at least 4 cells along its axis";
+  else if (p->mfp_type != 1 && p->mfp_type != 2) why = "mfp_type must be 1 or 2";
+  else if (p->num_ep_steps < 1) why = "num_ep_steps must be >= 1";
+  if (why) {
+    if (errbuf) snprintf(errbuf, 256, "%s", why);
+    return EPREM_GPU_ERR_ARG;
+  }
+  return EPREM_GPU_OK;
+}
+
+int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_params_t *p,
+                                         const eprem_grids_t *g, double *f, double *nodes,
+                                         int s0, int s1, eprem_ep_stats_t *stats, int nthreads,
+                                         char *errbuf) {
+  int rc = orc_validate(d, p, errbuf);
+  if (rc) return rc;
+  if (s0 < 0) s0 = 0;
+  if (s1 > d->num_streams) s1 = d->num_streams;
+  int ns = s1 - s0;
+  if (ns <= 0) return EPREM_GPU_OK;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > ns) nthreads = ns;
+  orc_job_t *jobs = (orc_job_t *)calloc(nthreads, sizeof(orc_job_t));
+  pthread_t *th = (pthread_t *)calloc(nthreads, sizeof(pthread_t));
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].d = d; jobs[t].p = p; jobs[t].g = g; jobs[t].f = f; jobs[t].nodes = nodes;
+    jobs[t].s0 = s0 + (int)((long)ns * t / nthreads);
+    jobs[t].s1 = s0 + (int)((long)ns * (t + 1) / nthreads);
+    jobs[t].stats.min_tau = DBL_MAX;
+    jobs[t].status = EPREM_GPU_OK;
+  }
+  if (nthreads == 1) {
+    orc_job_run(&jobs[0]);
+  } else {
+    for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, orc_job_run, &jobs[t]);
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  }
+  rc = EPREM_GPU_OK;
+  for (int t = 0; t < nthreads; t++) {
+    eprem_ep_stats_t *js = &jobs[t].stats;
+    if (js->max_subcycles_change > stats->max_subcycles_change)
+      stats->max_subcycles_change = js->max_subcycles_change;
+    if (js->max_subcycles_focusing > stats->max_subcycles_focusing)
+      stats->max_subcycles_focusing = js->max_subcycles_focusing;
+    if (js->max_substeps_stream > stats->max_substeps_stream)
+      stats->max_substeps_stream = js->max_substeps_stream;
+    if (js->min_tau < stats->min_tau) stats->min_tau = js->min_tau;
+    stats->cell_subcycles += js->cell_subcycles;
+    if (rc == EPREM_GPU_OK && jobs[t].status != EPREM_GPU_OK) {
+      rc = jobs[t].status;
+      if (errbuf) snprintf(errbuf, 256, "%s", jobs[t].err);
+    }
+  }
+  free(jobs);
+  free(th);
+  return rc;
+}
+
+int orc_update_energetic_particles(const eprem_dims_t *d, const eprem_params_t *p,
+                                   const eprem_grids_t *g, double *f, double *nodes,
+                                   eprem_ep_stats_t *stats, int nthreads, char *errbuf) {
+  return orc_update_energetic_particles_range(d, p, g, f, nodes, 0, d->num_streams, stats,
+                                              nthreads, errbuf);
+}
+
+/* ------------------------------------------------------------------------ */
+/* idealShockFactor, src/flow.c:623-651. */
+static double orc_shock_factor(const eprem_params_t *p, double r, double t_global) {
+  double exponent = exp(2.0 * (p->ideal_shock_sharpness / p->ideal_shock_scale_length) *
+                        (r - ((p->ideal_shock_speed / ORC_C) *
+                                  (t_global - p->ideal_shock_init_time / ORC_DAY) +
+                              p->r_scale)));
+  double ratio;
+  if (exponent >= 1.0e8)
+    ratio = 1.0;
+  else if (exponent <= 1.0e-8)
+    ratio = -1.0;
+  else
+    ratio = (exponent - 1.0) / (exponent + 1.0);
+  double factor = (1.0 + ((1.0 - ratio) * 0.5 * (p->ideal_shock_jump - 1.0)));
+  double falloff = exp(p->ideal_shock_falloff *
+                       (r - ((p->ideal_shock_speed / ORC_C) *
+                                 (t_global - p->ideal_shock_init_time / ORC_DAY) +
+                             p->r_scale)));
+  return 1 + (factor - 1) * falloff;
+}
+
+/* updateMhd with mhdGridStatus == MHD_DEFAULT (src/flow.c:36-154), including
+ * mhdDensity (:241-275), mhdV (:356-403), mhdB (:281-350). */
+int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                   double t_global) {
+  const int N = d->num_nodes;
+  const size_t SN = (size_t)d->num_streams * N;
+  const double rs = p->r_scale;
+  for (int s = 0; s < d->num_streams; s++)
+    for (int k = 0; k < N; k++) {
+      NODE(EPREM_NODE_BMAG_OLD, s, k) = NODE(EPREM_NODE_BMAG, s, k);
+      NODE(EPREM_NODE_DENSITY_OLD, s, k) = NODE(EPREM_NODE_DENSITY, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_R, s, k) = NODE(EPREM_NODE_VR, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_THETA, s, k) = NODE(EPREM_NODE_VTHETA, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_PHI, s, k) = NODE(EPREM_NODE_VPHI, s, k);
+      NODE(EPREM_NODE_DS_OLD, s, k) = NODE(EPREM_NODE_DS, s, k);
+      NODE(EPREM_NODE_ROLDER_X, s, k) = NODE(EPREM_NODE_RX, s, k);
+      NODE(EPREM_NODE_ROLDER_Y, s, k) = NODE(EPREM_NODE_RY, s, k);
+      NODE(EPREM_NODE_ROLDER_Z, s, k) = NODE(EPREM_NODE_RZ, s, k);
+      double x = NODE(EPREM_NODE_RX, s, k), y = NODE(EPREM_NODE_RY, s, k),
+             z = NODE(EPREM_NODE_RZ, s, k), rmag = NODE(EPREM_NODE_RMAG, s, k);
+      int isn = 0;
+      if (p->ideal_shock > 0) {
+        /* cartToSphPosAu, src/geometry.c:131-150 */
+        double ax = x * rs, ay = y * rs, az = z * rs;
+        double rr = sqrt(ax * ax + ay * ay + az * az);
+        double th = acos(az / rr);
+        double ph = atan2(ay, ax);
+        while (ph < 0.0) ph += (2.0 * ORC_PI);
+        if (rr <= p->ideal_shock_speed * t_global) {
+          if (p->ideal_shock_width == 0.0)
+            isn = 1;
+          else if ((fmin((2 * ORC_PI) - fabs(ph - p->ideal_shock_phi), fabs(ph - p->ideal_shock_phi)) <
+                    (p->ideal_shock_width / (double)2.0)) &&
+                   (fabs(th - p->ideal_shock_theta) < (p->ideal_shock_width / 2.0)))
+            isn = 1;
+        }
+      }
+      double rr = rmag * rs;
+      double dens = p->mhd_ns_au / (rr * rr);
+      if ((p->ideal_shock > 0) && (isn > 0)) dens *= orc_shock_factor(p, rr, t_global);
+      NODE(EPREM_NODE_DENSITY, s, k) = dens;
+      if (dens <= 0.0)
+        NODE(EPREM_NODE_DIVV, s, k) = 0.0;
+      else
+        NODE(EPREM_NODE_DIVV, s, k) = -1.0 * log(dens / NODE(EPREM_NODE_DENSITY_OLD, s, k)) / p->t_del;
+      double theta = acos(z / rmag);
+      double phi = atan2(y, x);
+      double Vr = p->mhd_us;
+      if ((p->ideal_shock > 0) && (isn > 0)) Vr *= orc_shock_factor(p, rmag * rs, t_global);
+      double Vt = 0.0, Vp = 0.0;
+      NODE(EPREM_NODE_VR, s, k) = Vr;
+      NODE(EPREM_NODE_VTHETA, s, k) = Vt;
+      NODE(EPREM_NODE_VPHI, s, k) = Vp;
+      NODE(EPREM_NODE_VMAG, s, k) = sqrt(Vr * Vr + Vt * Vt + Vp * Vp);
+      NODE(EPREM_NODE_VVEC_X, s, k) = Vr * sin(theta) * cos(phi) + Vt * cos(theta) * cos(phi) - Vp * sin(phi);
+      NODE(EPREM_NODE_VVEC_Y, s, k) = Vr * sin(theta) * sin(phi) + Vt * cos(theta) * sin(phi) + Vp * cos(phi);
+      NODE(EPREM_NODE_VVEC_Z, s, k) = Vr * cos(theta) - Vt * sin(theta);
+      double Br = p->mhd_bs_au / (rr * rr);
+      double Bt = 0.0;
+      double Bp = -1.0 * rr * Br * (p->omega_sun / (Vr + ORC_VERYSMALL)) * sin(theta);
+      NODE(EPREM_NODE_BR, s, k) = Br;
+      NODE(EPREM_NODE_BTHETA, s, k) = Bt;
+      NODE(EPREM_NODE_BPHI, s, k) = Bp;
+      double Bmag = sqrt(Br * Br + Bt * Bt + Bp * Bp);
+      NODE(EPREM_NODE_BMAG, s, k) = Bmag;
+      NODE(EPREM_NODE_BVEC_X, s, k) = Br * sin(theta) * cos(phi) + Bt * cos(theta) * cos(phi) - Bp * sin(phi);
+      NODE(EPREM_NODE_BVEC_Y, s, k) = Br * sin(theta) * sin(phi) + Bt * cos(theta) * sin(phi) + Bp * cos(phi);
+      NODE(EPREM_NODE_BVEC_Z, s, k) = Br * cos(theta) - Bt * sin(theta);
+      if (k == 0) {
+        NODE(EPREM_NODE_DUPAR, s, k) = 0.0;
+        NODE(EPREM_NODE_DLNB, s, k) = 0.0;
+        NODE(EPREM_NODE_DLNN, s, k) = 0.0;
+      } else {
+        double dupar = (Vr - NODE(EPREM_NODE_VSPH_OLD_R, s, k)) * Br +
+                       (Vt - NODE(EPREM_NODE_VSPH_OLD_THETA, s, k)) * Bt +
+                       (Vp - NODE(EPREM_NODE_VSPH_OLD_PHI, s, k)) * Bp;
+        dupar /= Bmag;
+        NODE(EPREM_NODE_DUPAR, s, k) = dupar;
+        NODE(EPREM_NODE_DLNB, s, k) = log(Bmag / NODE(EPREM_NODE_BMAG_OLD, s, k));
+        NODE(EPREM_NODE_DLNN, s, k) = log(dens / NODE(EPREM_NODE_DENSITY_OLD, s, k));
+      }
+    }
+  return EPREM_GPU_OK;
+}
+
+/* moveNodes, src/simCore.c:737-785 (MHD_DEFAULT branch of delrFlow). */
+int orc_move_nodes(const eprem_dims_t *d, const eprem_params_t *p, double *nodes, double dt) {
+  const int N = d->num_nodes;
+  const size_t SN = (size_t)d->num_streams * N;
+  for (int s = 0; s < d->num_streams; s++)
+    for (int k = 1; k < N; k++) {
+      double x = NODE(EPREM_NODE_RX, s, k), y = NODE(EPREM_NODE_RY, s, k), z = NODE(EPREM_NODE_RZ, s, k);
+      double dx = dt * NODE(EPREM_NODE_VVEC_X, s, k) / p->r_scale;
+      double dy = dt * NODE(EPREM_NODE_VVEC_Y, s, k) / p->r_scale;
+      double dz = dt * NODE(EPREM_NODE_VVEC_Z, s, k) / p->r_scale;
+      NODE(EPREM_NODE_ROLD_X, s, k) = x;
+      NODE(EPREM_NODE_ROLD_Y, s, k) = y;
+      NODE(EPREM_NODE_ROLD_Z, s, k) = z;
+      x += dx;
+      y += dy;
+      z += dz;
+      NODE(EPREM_NODE_RX, s, k) = x;
+      NODE(EPREM_NODE_RY, s, k) = y;
+      NODE(EPREM_NODE_RZ, s, k) = z;
+      NODE(EPREM_NODE_RMAG, s, k) = sqrt((x * x) + (y * y) + (z * z));
+    }
+  return EPREM_GPU_OK;
+}
+
+/* computeFlux without the output unit scale, src/unifiedOutput.c:153-180. */
+void orc_omni_flux(const eprem_dims_t *d, const eprem_grids_t *g, const double *f, double *out) {
+  const int N = d->num_nodes, E = d->num_energies, M = d->num_mu;
+  for (int s = 0; s < d->num_streams; s++)
+    for (int k = 0; k < N; k++)
+      for (int e = 0; e < E; e++) {
+        double iso = 0.0;
+        for (int m = 0; m < M; m++) iso += f[FIDX(s, k, e, m)];
+        iso /= M;
+        out[((size_t)s * N + k) * E + e] = 2.0 * g->egrid[e] * iso;
+      }
+}

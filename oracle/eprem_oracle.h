@@ -1,0 +1,76 @@
+/*
+ * eprem_oracle.h -- CPU restatement of EPREM's per-timestep energetic-particle
+ * update, used ONLY as the checker in tests/, in __graft_entry__.smoke() and
+ * as bench.py's CPU baseline.  It is test infrastructure: no product code path
+ * calls it, links it or falls back to it.
+ *
+ * It follows the reference C operation by operation (each function cites the
+ * reference file:line it restates) so that, compiled with
+ * -ffp-contract=off, it reproduces the reference bit for bit.  That claim is
+ * checked in tests/test_oracle_vs_reference.py against the reference's own
+ * functions compiled from source (oracle/Makefile -> oracle/_ref/).
+ *
+ * Data layout and parameter structs are those of include/eprem_gpu.h.
+ */
+#ifndef EPREM_ORACLE_H
+#define EPREM_ORACLE_H
+
+#include "../include/eprem_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* initEnergeticParticlesGrids (src/energeticParticlesInit.c:36-100):
+ * fills egrid/vgrid/vgrid_i/pgrid [E], rigidity [E], mugrid [M]; returns
+ * dlnp and dmu through the pointers. */
+void orc_build_grids(int num_energies, int num_mu, double e_min_mev,
+                     double e_max_mev, double mass, double charge,
+                     double rigidity_power, double *egrid, double *vgrid,
+                     double *vgrid_i, double *pgrid, double *rigidity,
+                     double *mugrid, double *dlnp, double *dmu);
+
+/* sepSeedFunction (src/energeticParticlesBoundary.c:67-116). */
+double orc_seed_function(const eprem_params_t *p, double energy, double r);
+
+/* setRuntimeConstants-style defaults of the reference getParams
+ * (src/configuration.c:58-217, 325-348) for the members of eprem_params_t. */
+void orc_default_params(eprem_params_t *p);
+
+/* updateEnergeticParticles (src/energeticParticles.c:70-203) over all streams.
+ * f: S*N*E*M, nodes: EPREM_NODE_NFIELDS*S*N (fields RX..DUPAR read; DS,
+ * BMAG_PLUS, BMAG_MINUS written).  stats accumulate (max / min) into *stats,
+ * which the caller initialises.  nthreads > 1 splits the streams across
+ * POSIX threads (the streams are independent when drift and shell diffusion
+ * are off, which this path requires).  Returns EPREM_GPU_OK or a status; the
+ * failing location is written to errbuf (if non-NULL, 256 bytes). */
+int orc_update_energetic_particles(const eprem_dims_t *d, const eprem_params_t *p,
+                                   const eprem_grids_t *g, double *f, double *nodes,
+                                   eprem_ep_stats_t *stats, int nthreads,
+                                   char *errbuf);
+
+/* Same, restricted to streams [s0, s1) -- the unit the CPU baseline times. */
+int orc_update_energetic_particles_range(const eprem_dims_t *d,
+                                         const eprem_params_t *p,
+                                         const eprem_grids_t *g, double *f,
+                                         double *nodes, int s0, int s1,
+                                         eprem_ep_stats_t *stats, int nthreads,
+                                         char *errbuf);
+
+/* updateMhd for the analytic background (src/flow.c:36-154). */
+int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p,
+                   double *nodes, double t_global);
+
+/* moveNodes (src/simCore.c:737-785) with delrFlow (src/flow.c:162-196). */
+int orc_move_nodes(const eprem_dims_t *d, const eprem_params_t *p,
+                   double *nodes, double dt);
+
+/* 2 E mean_mu f per (stream,node,E) (src/unifiedOutput.c:153-180 without the
+ * unit scale). out: S*N*E. */
+void orc_omni_flux(const eprem_dims_t *d, const eprem_grids_t *g,
+                   const double *f, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,143 @@
+"""ctypes access to the oracle libraries -- TEST INFRASTRUCTURE ONLY.
+
+* ``Oracle``    -> oracle/liboracle.so, the CPU restatement (eprem_oracle.c);
+* ``Reference`` -> oracle/_ref/libeprem_ref.so, the reference's own C compiled
+  from its source tree (only present where that tree exists).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, and only to check or time against it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from eprem_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libeprem_ref.so")
+DP = C.POINTER(C.c_double)
+
+
+def build(ref: bool = False, reference_root: str = "/root/reference") -> None:
+    """Compile liboracle.so (and the reference harness when asked and the
+    reference tree is present)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if ref and os.path.isdir(os.path.join(reference_root, "src")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"])
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(DP)
+
+
+class Oracle:
+    def __init__(self, path: str = LIB):
+        if not os.path.exists(path):
+            build()
+        lib = C.CDLL(path)
+        lib.orc_update_energetic_particles_range.argtypes = [
+            C.POINTER(abi.Dims), C.POINTER(abi.Params), C.POINTER(abi.Grids), DP, DP, C.c_int,
+            C.c_int, C.POINTER(abi.EpStats), C.c_int, C.c_char_p]
+        lib.orc_update_energetic_particles_range.restype = C.c_int
+        lib.orc_update_mhd.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
+        lib.orc_move_nodes.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
+        lib.orc_omni_flux.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Grids), DP, DP]
+        lib.orc_omni_flux.restype = None
+        lib.orc_seed_function.argtypes = [C.POINTER(abi.Params), C.c_double, C.c_double]
+        lib.orc_seed_function.restype = C.c_double
+        lib.orc_build_grids.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_double, DP, DP, DP, DP, DP, DP, DP, DP]
+        lib.orc_build_grids.restype = None
+        self.lib = lib
+
+    def grids(self, E, M, e_min, e_max, mass=1.0, charge=1.0, rigidity_power=1.0 / 3.0):
+        out = {k: np.zeros(E) for k in ("egrid", "vgrid", "vgrid_i", "pgrid", "rigidity")}
+        out["mugrid"] = np.zeros(M)
+        dl, dm = C.c_double(), C.c_double()
+        self.lib.orc_build_grids(E, M, e_min, e_max, mass, charge, rigidity_power,
+                                 _dp(out["egrid"]), _dp(out["vgrid"]), _dp(out["vgrid_i"]),
+                                 _dp(out["pgrid"]), _dp(out["rigidity"]), _dp(out["mugrid"]),
+                                 C.byref(dl), C.byref(dm))
+        out["dlnp"], out["dmu"] = dl.value, dm.value
+        return out
+
+    def update_energetic_particles(self, dims, params, grids_s, f, nodes, nthreads=1,
+                                   streams=None):
+        st = abi.EpStats()
+        st.min_tau = np.finfo(np.float64).max
+        err = C.create_string_buffer(256)
+        s0, s1 = (0, dims.num_streams) if streams is None else streams
+        rc = self.lib.orc_update_energetic_particles_range(
+            C.byref(dims), C.byref(params), C.byref(grids_s), _dp(f), _dp(nodes), s0, s1,
+            C.byref(st), nthreads, err)
+        return rc, st, err.value.decode()
+
+    def update_mhd(self, dims, params, nodes, t_global):
+        return self.lib.orc_update_mhd(C.byref(dims), C.byref(params), _dp(nodes), t_global)
+
+    def move_nodes(self, dims, params, nodes, dt):
+        return self.lib.orc_move_nodes(C.byref(dims), C.byref(params), _dp(nodes), dt)
+
+    def omni_flux(self, dims, grids_s, f):
+        out = np.zeros(dims.num_streams * dims.num_nodes * dims.num_energies)
+        self.lib.orc_omni_flux(C.byref(dims), C.byref(grids_s), _dp(f), _dp(out))
+        return out
+
+    def seed_function(self, params, energy, r):
+        return self.lib.orc_seed_function(C.byref(params), energy, r)
+
+
+class Reference:
+    """The reference's own updateEnergeticParticles / updateMhd / moveNodes.
+    The reference allocates its globals once per process, so one process can
+    host one configuration; tests run it in a child process."""
+
+    def __init__(self, path: str = REF_LIB):
+        lib = C.CDLL(path)
+        lib.ref_setup.argtypes = [C.c_int, C.c_int, C.POINTER(abi.Dims), C.POINTER(abi.Params),
+                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+        lib.ref_get_grids.argtypes = [DP] * 5 + [DP, DP]
+        lib.ref_load.argtypes = [DP, DP]
+        lib.ref_store.argtypes = [DP, DP]
+        lib.ref_update_energetic_particles.argtypes = [C.c_double, C.POINTER(abi.EpStats)]
+        lib.ref_update_mhd.argtypes = [C.c_double]
+        lib.ref_move_nodes.argtypes = [C.c_double]
+        self.lib = lib
+
+    def setup(self, w, precision=abi.EPREM_FP64):
+        d = w.dims(precision)
+        rc = self.lib.ref_setup(w.rows, w.cols, C.byref(d), C.byref(w.params), w.e_min, w.e_max,
+                                w.mass, w.charge, w.rigidity_power)
+        if rc:
+            raise RuntimeError(f"ref_setup failed: {rc}")
+        E, M = w.num_energies, w.num_mu
+        g = {k: np.zeros(E) for k in ("egrid", "vgrid", "vgrid_i", "rigidity")}
+        g["mugrid"] = np.zeros(M)
+        dl, dm = C.c_double(), C.c_double()
+        self.lib.ref_get_grids(_dp(g["egrid"]), _dp(g["vgrid"]), _dp(g["vgrid_i"]),
+                               _dp(g["mugrid"]), _dp(g["rigidity"]), C.byref(dl), C.byref(dm))
+        g["dlnp"], g["dmu"] = dl.value, dm.value
+        return g
+
+    def load(self, f, nodes):
+        self.lib.ref_load(_dp(f), _dp(nodes))
+
+    def store(self, f, nodes):
+        self.lib.ref_store(_dp(f), _dp(nodes))
+
+    def update_energetic_particles(self, t_global=0.0):
+        st = abi.EpStats()
+        rc = self.lib.ref_update_energetic_particles(t_global, C.byref(st))
+        return rc, st
+
+    def update_mhd(self, t_global):
+        self.lib.ref_update_mhd(t_global)
+
+    def move_nodes(self, dt):
+        self.lib.ref_move_nodes(dt)
