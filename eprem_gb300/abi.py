@@ -104,17 +104,20 @@ class EpStats(C.Structure):
         ("max_substeps_stream", C.c_int32),
         ("pad", C.c_int32),
         ("min_tau", C.c_double),
-        ("cell_subcycles", C.c_double),
+        ("stream_cell_subcycles", C.c_double),
+        ("focus_cell_subcycles", C.c_double),
+        ("change_cell_subcycles", C.c_double),
     ]
 
     def as_dict(self):
-        return {
-            "max_subcycles_change": self.max_subcycles_change,
-            "max_subcycles_focusing": self.max_subcycles_focusing,
-            "max_substeps_stream": self.max_substeps_stream,
-            "min_tau": self.min_tau,
-            "cell_subcycles": self.cell_subcycles,
-        }
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "pad"}
+
+
+KERNEL_KINDS = ["geometry", "stream", "node", "seed_check", "mhd", "move", "flux", "convert"]
+
+
+class KernelTime(C.Structure):
+    _fields_ = [("launches", C.c_int32), ("pad", C.c_int32), ("total_ms", C.c_double)]
 
 
 # enum eprem_node_field, in header order

@@ -1,0 +1,497 @@
+// eprem_gpu.cu -- the C ABI of include/eprem_gpu.h.
+//
+// Owns the device state of a run and sequences the kernels the way the
+// reference's entry points sequence their loops:
+//   updateEnergeticParticles (src/energeticParticles.c:70-203)
+//     geometry once per call (positions are fixed during the call), then per
+//     EP sub-step: streaming (+ seed check) over all (stream, energy) slabs,
+//     then focusing + change over all nodes;
+//   updateMhd (src/flow.c:36-154), moveNodes (src/simCore.c:737-785).
+// Device failures (NaN/Inf, ds <= 0, sub-cycle cap) land in a status block
+// that the synchronising calls read and turn into the reference's panic text.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace eprem;
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(EPREM_GPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t _e = (call);                       \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+const double kEfac = kMev / (kMp * kC * kC);
+}  // namespace
+
+struct eprem_gpu_run {
+  eprem_dims_t dims;
+  eprem_params_t params;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  RunView v{};
+  MhdParams mhd{};
+  StreamPlan splan{};
+  NodePlan nplan{};
+  int m0 = 0;
+  double norm_radius = 0, neg_beta = 0;
+  void *d_f = nullptr;
+  double *d_nodes = nullptr, *d_mugrid = nullptr;
+  EnergyConsts *d_ec = nullptr;
+  int *d_list = nullptr, *d_list_size = nullptr;
+  double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;
+  DevStatus *d_status = nullptr, *h_status = nullptr;
+  double *d_stage = nullptr;
+  size_t stage_elems = 0;
+  double *d_flux = nullptr;
+  uint64_t launches = 0;
+  // optional per-launch timing: events recorded around each kernel launch
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> ev_pending;  // (kind, index of start event)
+  size_t ev_used = 0;
+  size_t cells() const {
+    return (size_t)dims.num_streams * dims.num_nodes * dims.num_energies * dims.num_mu;
+  }
+  size_t sn() const { return (size_t)dims.num_streams * dims.num_nodes; }
+};
+
+// Runs one launch helper, bracketed by events when timing is on.
+template <typename Fn>
+static int timed(eprem_gpu_run *r, int kind, Fn &&launch) {
+  if (!r->timing) return launch();
+  if (r->ev_used + 2 > r->ev_pool.size()) {
+    for (int i = 0; i < 64; i++) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) return EPREM_GPU_ERR_CUDA;
+      r->ev_pool.push_back(ev);
+    }
+  }
+  const size_t i0 = r->ev_used;
+  r->ev_used += 2;
+  cudaEventRecord(r->ev_pool[i0], r->stream);
+  int rc = launch();
+  cudaEventRecord(r->ev_pool[i0 + 1], r->stream);
+  r->ev_pending.push_back({kind, (int)i0});
+  return rc;
+}
+
+static int reset_status(eprem_gpu_run *r) {
+  DevStatus init{};
+  { const double big = DBL_MAX; memcpy(&init.min_tau_bits, &big, sizeof(big)); }
+  CK(cudaMemcpyAsync(r->d_status, &init, sizeof(init), cudaMemcpyHostToDevice, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  return EPREM_GPU_OK;
+}
+
+static const char *where_name(int w) {
+  switch (w) {
+    case 1: return "Diffuse Stream Data";
+    case 2: return "Adiabatic Focusing";
+    case 3: return "Adiabatic Change";
+    case 4: return "stream geometry";
+    default: return "energetic-particle update";
+  }
+}
+
+// Reads the status block (synchronising) and reports a device failure.
+static int check_status(eprem_gpu_run *r, bool reset_stats, eprem_ep_stats_t *stats) {
+  CK(cudaMemcpyAsync(r->h_status, r->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                     r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  const DevStatus st = *r->h_status;
+  if (stats) {
+    stats->max_subcycles_change = st.max_change;
+    stats->max_subcycles_focusing = st.max_focus;
+    stats->max_substeps_stream = st.max_stream;
+    stats->pad = 0;
+    memcpy(&stats->min_tau, &st.min_tau_bits, sizeof(double));
+    stats->stream_cell_subcycles = (double)st.stream_cs;
+    stats->focus_cell_subcycles = (double)st.focus_cs;
+    stats->change_cell_subcycles = (double)st.change_cs;
+  }
+  if (reset_stats || st.code) {
+    int rc = reset_status(r);
+    if (rc) return rc;
+  }
+  if (st.code) {
+    char buf[256];
+    const char *what = st.code == EPREM_GPU_ERR_NAN       ? "NaN value in"
+                       : st.code == EPREM_GPU_ERR_INF     ? "Inf value in"
+                       : st.code == EPREM_GPU_ERR_DS      ? "FindSegmentLengths(): Underflow in ds,"
+                       : st.code == EPREM_GPU_ERR_SUBCYCLES ? "sub-cycle cap exceeded in"
+                       : st.code == EPREM_GPU_ERR_STATE   ? "fewer than 3 nodes left after thinning in"
+                                                          : "failure in";
+    snprintf(buf, sizeof(buf), "%s %s (stream %d, node %d, energy %d, mu %d)", what,
+             where_name(st.where), st.stream, st.node, st.energy, st.mu);
+    return fail(st.code, buf);
+  }
+  return EPREM_GPU_OK;
+}
+
+static int validate(const eprem_dims_t *d, const eprem_params_t *p, const eprem_grids_t *g) {
+  if (!d || !p || !g) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  if (d->num_species != 1)
+    return fail(EPREM_GPU_ERR_UNSUPPORTED,
+                "num_species must be 1 (the reference indexes egrid by species*E beyond its "
+                "length for species > 0)");
+  if (d->num_streams < 1 || d->num_streams > 65535) return fail(EPREM_GPU_ERR_ARG, "num_streams out of range");
+  if (d->num_nodes < 3) return fail(EPREM_GPU_ERR_ARG, "num_nodes must be >= 3");
+  if (d->num_energies < 2 || d->num_energies > 64) return fail(EPREM_GPU_ERR_ARG, "num_energies must be 2..64");
+  if (d->num_mu < 2 || d->num_mu > 64) return fail(EPREM_GPU_ERR_ARG, "num_mu must be 2..64");
+  if (d->precision != EPREM_FP64 && d->precision != EPREM_FP32) return fail(EPREM_GPU_ERR_ARG, "unknown precision");
+  if (p->num_ep_steps < 1) return fail(EPREM_GPU_ERR_ARG, "num_ep_steps must be >= 1");
+  if (p->adiabatic_focus_alg < 1 || p->adiabatic_focus_alg > 3 || p->adiabatic_change_alg < 1 ||
+      p->adiabatic_change_alg > 3)
+    return fail(EPREM_GPU_ERR_ARG, "adiabatic algorithms must be 1, 2 or 3");
+  if ((p->adiabatic_focus_alg == 3 && d->num_mu < 4) ||
+      (p->adiabatic_change_alg == 3 && d->num_energies < 4))
+    return fail(EPREM_GPU_ERR_ARG, "WENO3 needs at least 4 cells along its axis");
+  if (p->mfp_type != 1 && p->mfp_type != 2) return fail(EPREM_GPU_ERR_ARG, "mfp_type must be 1 or 2");
+  if (!g->egrid || !g->vgrid || !g->vgrid_i || !g->mugrid || !g->rigidity)
+    return fail(EPREM_GPU_ERR_ARG, "null grid array");
+  return EPREM_GPU_OK;
+}
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t n) {
+  return cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T) + 16);
+}
+
+extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *params,
+                                const eprem_grids_t *grids, eprem_gpu_run **out) {
+  if (!out) return fail(EPREM_GPU_ERR_ARG, "null output handle");
+  *out = nullptr;
+  int rc = validate(dims, params, grids);
+  if (rc) return rc;
+  const int S = dims->num_streams, N = dims->num_nodes, E = dims->num_energies,
+            M = dims->num_mu;
+  // mu split: cells with mugrid >= 0 take their upwind value from the inner
+  // neighbour (src/energeticParticles.c:2379); the grid must be ordered.
+  int m0 = M;
+  for (int m = 0; m < M; m++)
+    if (grids->mugrid[m] >= 0.0) { m0 = m; break; }
+  for (int m = 0; m < M; m++)
+    if ((grids->mugrid[m] >= 0.0) != (m >= m0))
+      return fail(EPREM_GPU_ERR_ARG, "mugrid must be increasing");
+  auto *r = new eprem_gpu_run();
+  r->dims = *dims;
+  r->params = *params;
+  r->m0 = m0;
+  if (r->params.max_subcycles <= 0) r->params.max_subcycles = 1000000;
+  if (plan_stream(dims->precision, N, M, &r->splan) ||
+      plan_node(dims->precision, E, M, &r->nplan)) {
+    delete r;
+    return fail(EPREM_GPU_ERR_ARG, "sizes exceed the supported kernel shapes "
+                                   "(num_nodes per stream or E*M too large)");
+  }
+  cudaError_t e = cudaGetDevice(&r->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+  const size_t SN = r->sn(), cells = r->cells();
+  const size_t fbytes = dims->precision == EPREM_FP64 ? sizeof(double) : sizeof(float);
+  if (e == cudaSuccess) e = cudaMalloc(&r->d_f, cells * fbytes + 16);
+  if (e == cudaSuccess) e = dalloc(&r->d_nodes, (size_t)EPREM_NODE_NFIELDS * SN);
+  if (e == cudaSuccess) e = dalloc(&r->d_mugrid, (size_t)M);
+  if (e == cudaSuccess) e = dalloc(&r->d_ec, (size_t)E);
+  if (e == cudaSuccess) e = dalloc(&r->d_list, SN);
+  if (e == cudaSuccess) e = dalloc(&r->d_list_size, (size_t)S);
+  if (e == cudaSuccess) e = dalloc(&r->d_ds_i, SN);
+  if (e == cudaSuccess) e = dalloc(&r->d_ds_min, (size_t)S);
+  if (e == cudaSuccess) e = dalloc(&r->d_seed_radial, SN);
+  if (e == cudaSuccess) e = dalloc(&r->d_mfp_node, SN);
+  if (e == cudaSuccess) e = dalloc(&r->d_status, 1);
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void **>(&r->h_status), sizeof(DevStatus));
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->d_list, 0, SN * sizeof(int), r->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->d_list_size, 0, S * sizeof(int), r->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->d_nodes, 0, EPREM_NODE_NFIELDS * SN * sizeof(double), r->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->d_f, 0, cells * fbytes, r->stream);
+  if (e != cudaSuccess) {
+    eprem_gpu_destroy(r);
+    return cuda_fail(e, "eprem_gpu_create allocation");
+  }
+  // Per-energy constants with the host libm, as the reference computes them.
+  const eprem_params_t &p = r->params;
+  std::vector<EnergyConsts> ec(E);
+  const double normE1 = 1.0 * kEfac, normE0 = p.bf_ecutoff * kEfac;
+  for (int i = 0; i < E; i++) {
+    ec[i].egrid = grids->egrid[i];
+    ec[i].vgrid = grids->vgrid[i];
+    ec[i].vgrid_i = grids->vgrid_i[i];
+    ec[i].rig_lamo = grids->rigidity[i] * p.lamo;
+    ec[i].seed_power = pow((grids->egrid[i] / normE1), -p.bf_gamma);
+    ec[i].seed_exp = exp(-(grids->egrid[i] / normE0));
+  }
+  e = cudaMemcpyAsync(r->d_ec, ec.data(), E * sizeof(EnergyConsts), cudaMemcpyHostToDevice, r->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(r->d_mugrid, grids->mugrid, M * sizeof(double), cudaMemcpyHostToDevice, r->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+  if (e != cudaSuccess) {
+    eprem_gpu_destroy(r);
+    return cuda_fail(e, "eprem_gpu_create upload");
+  }
+  rc = setup_geometry_attrs(N);
+  if (rc) {
+    eprem_gpu_destroy(r);
+    return fail(rc, "cannot reserve shared memory for the stream-list kernel");
+  }
+  r->norm_radius = p.bf_r0 / p.r_scale;
+  r->neg_beta = -p.bf_beta;
+  RunView &v = r->v;
+  v.S = S; v.N = N; v.E = E; v.M = M;
+  v.precision = dims->precision;
+  v.f = r->d_f;
+  v.nodes = r->d_nodes;
+  v.mugrid = r->d_mugrid;
+  v.ec = r->d_ec;
+  v.list = r->d_list;
+  v.list_size = r->d_list_size;
+  v.ds_i = r->d_ds_i;
+  v.ds_min = r->d_ds_min;
+  v.seed_radial = r->d_seed_radial;
+  v.mfp_node = r->d_mfp_node;
+  v.status = r->d_status;
+  v.r_scale = p.r_scale;
+  v.dt = p.t_del / (1.0 * p.num_ep_steps);  // src/energeticParticles.c:99
+  v.dt_full = v.dt * p.num_ep_steps;        // :861, :1582
+  v.dmu = grids->dmu;
+  v.dlnp = grids->dlnp;
+  v.norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);
+  v.bf_xi = p.bf_xi;
+  v.dsh_min = p.dsh_min;
+  v.damp_cooling = p.damp_cooling;
+  v.num_ep_steps = p.num_ep_steps;
+  v.max_subcycles = p.max_subcycles;
+  v.check_seed = p.check_seed_population > 0;
+  v.use_bc = (p.use_ep_boundary > 0) && (p.use_boundary_function > 0);
+  v.use_stream = p.use_parallel_diffusion > 0;
+  v.use_focus = p.use_adiabatic_focus > 0;
+  v.use_change = p.use_adiabatic_change > 0;
+  v.focus_alg = p.adiabatic_focus_alg;
+  v.change_alg = p.adiabatic_change_alg;
+  MhdParams &mh = r->mhd;
+  mh.r_scale = p.r_scale; mh.t_del = p.t_del; mh.mhd_us = p.mhd_us; mh.mhd_ns_au = p.mhd_ns_au;
+  mh.mhd_bs_au = p.mhd_bs_au; mh.omega_sun = p.omega_sun; mh.ideal_shock = p.ideal_shock;
+  mh.sharp = p.ideal_shock_sharpness; mh.scale_len = p.ideal_shock_scale_length;
+  mh.jump = p.ideal_shock_jump; mh.falloff = p.ideal_shock_falloff;
+  mh.speed = p.ideal_shock_speed; mh.init_time = p.ideal_shock_init_time;
+  mh.theta = p.ideal_shock_theta; mh.phi = p.ideal_shock_phi; mh.width = p.ideal_shock_width;
+  rc = reset_status(r);
+  if (rc) {
+    eprem_gpu_destroy(r);
+    return rc;
+  }
+  *out = r;
+  g_last_error.clear();
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
+  if (!r) return EPREM_GPU_OK;
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  cudaFree(r->d_f);
+  cudaFree(r->d_nodes);
+  cudaFree(r->d_mugrid);
+  cudaFree(r->d_ec);
+  cudaFree(r->d_list);
+  cudaFree(r->d_list_size);
+  cudaFree(r->d_ds_i);
+  cudaFree(r->d_ds_min);
+  cudaFree(r->d_seed_radial);
+  cudaFree(r->d_mfp_node);
+  cudaFree(r->d_status);
+  cudaFree(r->d_stage);
+  cudaFree(r->d_flux);
+  for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
+  if (r->h_status) cudaFreeHost(r->h_status);
+  if (r->stream) cudaStreamDestroy(r->stream);
+  delete r;
+  return EPREM_GPU_OK;
+}
+
+static int ensure_stage(eprem_gpu_run *r, size_t elems) {
+  if (r->stage_elems >= elems) return EPREM_GPU_OK;
+  cudaFree(r->d_stage);
+  r->d_stage = nullptr;
+  r->stage_elems = 0;
+  CK(cudaMalloc(&r->d_stage, elems * sizeof(double)));
+  r->stage_elems = elems;
+  return EPREM_GPU_OK;
+}
+
+// Chunk of doubles staged at a time when converting f for the FP32 form.
+static const size_t kStageChunk = (size_t)1 << 27;
+
+extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
+  if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t n = r->cells();
+  if (r->dims.precision == EPREM_FP64) {
+    CK(cudaMemcpyAsync(r->d_f, f, n * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    return EPREM_GPU_OK;
+  }
+  const size_t chunk = n < kStageChunk ? n : kStageChunk;
+  int rc = ensure_stage(r, chunk);
+  if (rc) return rc;
+  for (size_t off = 0; off < n; off += chunk) {
+    const size_t c = (n - off) < chunk ? (n - off) : chunk;
+    CK(cudaMemcpyAsync(r->d_stage, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    rc = launch_convert_f(r->v, r->d_stage,
+                          reinterpret_cast<double *>(static_cast<float *>(r->d_f) + off), 1, c,
+                          r->stream, &r->launches);
+    if (rc) return fail(rc, "conversion kernel launch failed");
+  }
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
+  if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t n = r->cells();
+  if (r->dims.precision == EPREM_FP64) {
+    CK(cudaMemcpyAsync(f, r->d_f, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  } else {
+    const size_t chunk = n < kStageChunk ? n : kStageChunk;
+    int rc = ensure_stage(r, chunk);
+    if (rc) return rc;
+    for (size_t off = 0; off < n; off += chunk) {
+      const size_t c = (n - off) < chunk ? (n - off) : chunk;
+      rc = launch_convert_f(r->v,
+                            reinterpret_cast<const double *>(static_cast<const float *>(r->d_f) + off),
+                            r->d_stage, 0, c, r->stream, &r->launches);
+      if (rc) return fail(rc, "conversion kernel launch failed");
+      CK(cudaMemcpyAsync(f + off, r->d_stage, c * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+    }
+  }
+  return check_status(r, false, nullptr);
+}
+
+extern "C" int eprem_gpu_upload_nodes(eprem_gpu_run *r, const double *nodes, uint64_t mask) {
+  if (!r || !nodes) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t SN = r->sn();
+  for (int fld = 0; fld < EPREM_NODE_NFIELDS; fld++)
+    if (mask & (1ull << fld))
+      CK(cudaMemcpyAsync(r->d_nodes + fld * SN, nodes + fld * SN, SN * sizeof(double),
+                         cudaMemcpyHostToDevice, r->stream));
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_download_nodes(eprem_gpu_run *r, double *nodes, uint64_t mask) {
+  if (!r || !nodes) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t SN = r->sn();
+  for (int fld = 0; fld < EPREM_NODE_NFIELDS; fld++)
+    if (mask & (1ull << fld))
+      CK(cudaMemcpyAsync(nodes + fld * SN, r->d_nodes + fld * SN, SN * sizeof(double),
+                         cudaMemcpyDeviceToHost, r->stream));
+  return check_status(r, false, nullptr);
+}
+
+extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
+  (void)t_global;
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  const eprem_params_t &p = r->params;
+  int rc = timed(r, EPREM_KERNEL_GEOMETRY, [&] {
+    return launch_geometry(r->v, r->stream, r->norm_radius, r->neg_beta, p.mfp_type,
+                           p.mfp_type == 2 ? p.mfp_b_power : p.mfp_radial_power, p.mhd_bs_au,
+                           &r->launches);
+  });
+  if (rc) return cuda_fail(cudaGetLastError(), "geometry launch");
+  for (int step = 0; step < p.num_ep_steps; step++) {
+    if (r->v.use_stream)
+      rc = timed(r, EPREM_KERNEL_STREAM,
+                 [&] { return launch_stream(r->v, r->splan, r->m0, r->stream, &r->launches); });
+    else if (r->v.check_seed)
+      rc = timed(r, EPREM_KERNEL_SEED_CHECK,
+                 [&] { return launch_seed_check(r->v, r->stream, &r->launches); });
+    if (rc) return cuda_fail(cudaGetLastError(), "streaming launch");
+    if (r->v.use_focus || r->v.use_change) {
+      rc = timed(r, EPREM_KERNEL_NODE,
+                 [&] { return launch_node(r->v, r->nplan, r->stream, &r->launches); });
+      if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
+    }
+  }
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *stats) {
+  if (!r || !stats) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  return check_status(r, true, stats);
+}
+
+extern "C" int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (timed(r, EPREM_KERNEL_MHD,
+            [&] { return launch_update_mhd(r->v, r->mhd, t_global, r->stream, &r->launches); }))
+    return cuda_fail(cudaGetLastError(), "updateMhd launch");
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (timed(r, EPREM_KERNEL_MOVE,
+            [&] { return launch_move_nodes(r->v, dt, r->stream, &r->launches); }))
+    return cuda_fail(cudaGetLastError(), "moveNodes launch");
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_omni_flux(eprem_gpu_run *r, double *out) {
+  if (!r || !out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t n = r->sn() * r->dims.num_energies;
+  if (!r->d_flux) CK(cudaMalloc(&r->d_flux, n * sizeof(double)));
+  if (timed(r, EPREM_KERNEL_FLUX,
+            [&] { return launch_omni_flux(r->v, r->d_flux, r->stream, &r->launches); }))
+    return cuda_fail(cudaGetLastError(), "flux launch");
+  CK(cudaMemcpyAsync(out, r->d_flux, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  return check_status(r, false, nullptr);
+}
+
+extern "C" int eprem_gpu_synchronize(eprem_gpu_run *r) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  return check_status(r, false, nullptr);
+}
+
+extern "C" int eprem_gpu_set_kernel_timing(eprem_gpu_run *r, int enable) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  CK(cudaStreamSynchronize(r->stream));
+  r->timing = enable != 0;
+  r->ev_pending.clear();
+  r->ev_used = 0;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_read_kernel_timing(eprem_gpu_run *r, eprem_kernel_time_t *out) {
+  if (!r || !out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  CK(cudaStreamSynchronize(r->stream));
+  for (int k = 0; k < EPREM_KERNEL_NKINDS; k++) out[k] = eprem_kernel_time_t{0, 0, 0.0};
+  for (const auto &pe : r->ev_pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, r->ev_pool[pe.second], r->ev_pool[pe.second + 1]));
+    out[pe.first].launches += 1;
+    out[pe.first].total_ms += ms;
+  }
+  r->ev_pending.clear();
+  r->ev_used = 0;
+  return EPREM_GPU_OK;
+}
+
+extern "C" void *eprem_gpu_stream(eprem_gpu_run *r) { return r ? (void *)r->stream : nullptr; }
+
+extern "C" uint64_t eprem_gpu_kernel_launches(const eprem_gpu_run *r) {
+  return r ? r->launches : 0;
+}
+
+extern "C" const char *eprem_gpu_last_error(void) { return g_last_error.c_str(); }

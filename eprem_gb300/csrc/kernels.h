@@ -1,0 +1,49 @@
+// kernels.h -- host-side launch entry points of the kernels (one per .cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace eprem {
+
+// geometry.cu
+int launch_geometry(const RunView &r, cudaStream_t st, double norm_radius, double neg_beta,
+                    int mfp_type, double mfp_power, double bs_au, uint64_t *launches);
+int setup_geometry_attrs(int N);
+
+// stream.cu -- DiffuseStreamData (+ seedPopulationCheck)
+struct StreamPlan {
+  int mmax;      // register slots per thread (>= M)
+  int threads;   // threads per CTA
+  int cluster;   // CTAs per (stream, energy) slab
+};
+int plan_stream(int precision, int N, int M, StreamPlan *plan);
+int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
+                  uint64_t *launches);
+int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
+
+// node.cu -- AdiabaticFocusing + AdiabaticChange
+struct NodePlan {
+  int pmax;        // register slots per thread (>= max(E, M))
+  int threads;     // threads per CTA
+  int nodes;       // nodes per CTA
+  size_t smem;     // dynamic shared memory bytes
+};
+int plan_node(int precision, int E, int M, NodePlan *plan);
+int launch_node(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_t *launches);
+
+// mhd.cu -- updateMhd (analytic), moveNodes, omnidirectional flux, f conversion
+struct MhdParams {
+  double r_scale, t_del, mhd_us, mhd_ns_au, mhd_bs_au, omega_sun;
+  int ideal_shock;
+  double sharp, scale_len, jump, falloff, speed, init_time, theta, phi, width;
+};
+int launch_update_mhd(const RunView &r, const MhdParams &p, double t_global, cudaStream_t st,
+                      uint64_t *launches);
+int launch_move_nodes(const RunView &r, double dt, cudaStream_t st, uint64_t *launches);
+int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *launches);
+int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
+                     size_t count, cudaStream_t st, uint64_t *launches);
+
+}  // namespace eprem

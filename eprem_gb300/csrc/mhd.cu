@@ -1,0 +1,200 @@
+// mhd.cu -- analytic MHD background on the nodes, node advection, flux,
+// and the host-format conversions of f.
+//
+//   k_update_mhd : updateMhd for mhdGridStatus == MHD_DEFAULT
+//                  (src/flow.c:36-154 with mhdDensity :241-275, mhdV :356-403,
+//                  mhdB :281-350, idealShockFactor :623-651,
+//                  cartToSphPosAu src/geometry.c:131-150)
+//   k_move_nodes : moveNodes (src/simCore.c:737-785) with the MHD_DEFAULT
+//                  branch of delrFlow (src/flow.c:162-196)
+//   k_omni_flux  : computeFlux without its unit scale (src/unifiedOutput.c:153-180)
+// All FP64, one thread per node.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace eprem {
+
+__device__ double shock_factor(const MhdParams &p, double r, double tg) {
+  const double front = (p.speed / kC) * (tg - p.init_time / kDay) + p.r_scale;
+  const double exponent = exp(2.0 * (p.sharp / p.scale_len) * (r - front));
+  double ratio;
+  if (exponent >= 1.0e8)
+    ratio = 1.0;
+  else if (exponent <= 1.0e-8)
+    ratio = -1.0;
+  else
+    ratio = (exponent - 1.0) / (exponent + 1.0);
+  const double factor = (1.0 + ((1.0 - ratio) * 0.5 * (p.jump - 1.0)));
+  const double falloff = exp(p.falloff * (r - front));
+  return 1 + (factor - 1) * falloff;
+}
+
+__global__ void k_update_mhd(RunView r, MhdParams p, double tg) {
+  const size_t SN = (size_t)r.S * r.N;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < SN;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(g % r.N);
+    auto F = [&](int field) -> double & { return node_field(r, field)[g]; };
+    F(EPREM_NODE_BMAG_OLD) = F(EPREM_NODE_BMAG);
+    F(EPREM_NODE_DENSITY_OLD) = F(EPREM_NODE_DENSITY);
+    F(EPREM_NODE_VSPH_OLD_R) = F(EPREM_NODE_VR);
+    F(EPREM_NODE_VSPH_OLD_THETA) = F(EPREM_NODE_VTHETA);
+    F(EPREM_NODE_VSPH_OLD_PHI) = F(EPREM_NODE_VPHI);
+    F(EPREM_NODE_DS_OLD) = F(EPREM_NODE_DS);
+    F(EPREM_NODE_ROLDER_X) = F(EPREM_NODE_RX);
+    F(EPREM_NODE_ROLDER_Y) = F(EPREM_NODE_RY);
+    F(EPREM_NODE_ROLDER_Z) = F(EPREM_NODE_RZ);
+    const double x = F(EPREM_NODE_RX), y = F(EPREM_NODE_RY), z = F(EPREM_NODE_RZ);
+    const double rmag = F(EPREM_NODE_RMAG);
+    int isn = 0;
+    if (p.ideal_shock > 0) {
+      const double ax = x * p.r_scale, ay = y * p.r_scale, az = z * p.r_scale;
+      const double rr = sqrt(ax * ax + ay * ay + az * az);
+      const double th = acos(az / rr);
+      double ph = atan2(ay, ax);
+      while (ph < 0.0) ph += (2.0 * kPi);
+      if (rr <= p.speed * tg) {
+        if (p.width == 0.0)
+          isn = 1;
+        else if ((fmin((2 * kPi) - fabs(ph - p.phi), fabs(ph - p.phi)) < (p.width / 2.0)) &&
+                 (fabs(th - p.theta) < (p.width / 2.0)))
+          isn = 1;
+      }
+    }
+    const double rr = rmag * p.r_scale;
+    double dens = p.mhd_ns_au / (rr * rr);
+    if (p.ideal_shock > 0 && isn > 0) dens *= shock_factor(p, rr, tg);
+    F(EPREM_NODE_DENSITY) = dens;
+    F(EPREM_NODE_DIVV) = (dens <= 0.0) ? 0.0 : -1.0 * log(dens / F(EPREM_NODE_DENSITY_OLD)) / p.t_del;
+    const double theta = acos(z / rmag);
+    const double phi = atan2(y, x);
+    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    double Vr = p.mhd_us;
+    if (p.ideal_shock > 0 && isn > 0) Vr *= shock_factor(p, rmag * p.r_scale, tg);
+    const double Vt = 0.0, Vp = 0.0;
+    F(EPREM_NODE_VR) = Vr;
+    F(EPREM_NODE_VTHETA) = Vt;
+    F(EPREM_NODE_VPHI) = Vp;
+    F(EPREM_NODE_VMAG) = sqrt(Vr * Vr + Vt * Vt + Vp * Vp);
+    F(EPREM_NODE_VVEC_X) = Vr * st * cp + Vt * ct * cp - Vp * sp;
+    F(EPREM_NODE_VVEC_Y) = Vr * st * sp + Vt * ct * sp + Vp * cp;
+    F(EPREM_NODE_VVEC_Z) = Vr * ct - Vt * st;
+    const double Br = p.mhd_bs_au / (rr * rr);
+    const double Bt = 0.0;
+    const double Bp = -1.0 * rr * Br * (p.omega_sun / (Vr + kVerySmall)) * st;
+    F(EPREM_NODE_BR) = Br;
+    F(EPREM_NODE_BTHETA) = Bt;
+    F(EPREM_NODE_BPHI) = Bp;
+    const double Bmag = sqrt(Br * Br + Bt * Bt + Bp * Bp);
+    F(EPREM_NODE_BMAG) = Bmag;
+    F(EPREM_NODE_BVEC_X) = Br * st * cp + Bt * ct * cp - Bp * sp;
+    F(EPREM_NODE_BVEC_Y) = Br * st * sp + Bt * ct * sp + Bp * cp;
+    F(EPREM_NODE_BVEC_Z) = Br * ct - Bt * st;
+    if (k == 0) {  // rank-0 INNER_ACTIVE_SHELL (src/flow.c:131-137)
+      F(EPREM_NODE_DUPAR) = 0.0;
+      F(EPREM_NODE_DLNB) = 0.0;
+      F(EPREM_NODE_DLNN) = 0.0;
+    } else {
+      double dupar = (Vr - F(EPREM_NODE_VSPH_OLD_R)) * Br +
+                     (Vt - F(EPREM_NODE_VSPH_OLD_THETA)) * Bt +
+                     (Vp - F(EPREM_NODE_VSPH_OLD_PHI)) * Bp;
+      F(EPREM_NODE_DUPAR) = dupar / Bmag;
+      F(EPREM_NODE_DLNB) = log(Bmag / F(EPREM_NODE_BMAG_OLD));
+      F(EPREM_NODE_DLNN) = log(dens / F(EPREM_NODE_DENSITY_OLD));
+    }
+  }
+}
+
+__global__ void k_move_nodes(RunView r, double dt) {
+  const size_t SN = (size_t)r.S * r.N;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < SN;
+       g += (size_t)gridDim.x * blockDim.x) {
+    if (g % r.N == 0) continue;  // the innermost node stays on the inner boundary
+    double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
+           *rz = node_field(r, EPREM_NODE_RZ);
+    double x = rx[g], y = ry[g], z = rz[g];
+    const double dx = dt * node_field(r, EPREM_NODE_VVEC_X)[g] / r.r_scale;
+    const double dy = dt * node_field(r, EPREM_NODE_VVEC_Y)[g] / r.r_scale;
+    const double dz = dt * node_field(r, EPREM_NODE_VVEC_Z)[g] / r.r_scale;
+    node_field(r, EPREM_NODE_ROLD_X)[g] = x;
+    node_field(r, EPREM_NODE_ROLD_Y)[g] = y;
+    node_field(r, EPREM_NODE_ROLD_Z)[g] = z;
+    x += dx;
+    y += dy;
+    z += dz;
+    rx[g] = x;
+    ry[g] = y;
+    rz[g] = z;
+    node_field(r, EPREM_NODE_RMAG)[g] = sqrt((x * x) + (y * y) + (z * z));
+  }
+}
+
+template <typename Real>
+__global__ void k_omni_flux(RunView r, double *out) {
+  const size_t items = (size_t)r.S * r.N * r.E;
+  for (size_t it = blockIdx.x * (size_t)blockDim.x + threadIdx.x; it < items;
+       it += (size_t)gridDim.x * blockDim.x) {
+    const Real *fp = reinterpret_cast<const Real *>(r.f) + it * r.M;
+    double iso = 0.0;
+    for (int m = 0; m < r.M; ++m) iso += (double)fp[m];
+    iso /= r.M;
+    out[it] = 2.0 * r.ec[it % r.E].egrid * iso;
+  }
+}
+
+// double staging buffer <-> device f (float in the FP32 form)
+__global__ void k_f64_to_f32(const double *src, float *dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float v = (float)src[i];
+    dst[i] = v < FLT_MIN ? FLT_MIN : v;
+  }
+}
+__global__ void k_f32_to_f64(const float *src, double *dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+static int grid_for(size_t n) {
+  size_t b = (n + 255) / 256;
+  return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+}
+
+int launch_update_mhd(const RunView &r, const MhdParams &p, double tg, cudaStream_t st,
+                      uint64_t *launches) {
+  k_update_mhd<<<grid_for((size_t)r.S * r.N), 256, 0, st>>>(r, p, tg);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+int launch_move_nodes(const RunView &r, double dt, cudaStream_t st, uint64_t *launches) {
+  k_move_nodes<<<grid_for((size_t)r.S * r.N), 256, 0, st>>>(r, dt);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *launches) {
+  const size_t items = (size_t)r.S * r.N * r.E;
+  if (r.precision == EPREM_FP64)
+    k_omni_flux<double><<<grid_for(items), 256, 0, st>>>(r, out);
+  else
+    k_omni_flux<float><<<grid_for(items), 256, 0, st>>>(r, out);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+// to_device_real: staging (double) -> f (float); else f (float) -> staging.
+int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
+                     size_t count, cudaStream_t st, uint64_t *launches) {
+  (void)r;
+  if (to_device_real)
+    k_f64_to_f32<<<grid_for(count), 256, 0, st>>>(src64, reinterpret_cast<float *>(dst64), count);
+  else
+    k_f32_to_f64<<<grid_for(count), 256, 0, st>>>(reinterpret_cast<const float *>(src64), dst64,
+                                                  count);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+}  // namespace eprem

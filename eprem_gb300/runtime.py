@@ -1,0 +1,183 @@
+"""Host-side mirror of the reference's hot-path entry points over the C ABI.
+
+The reference drives the path through argument-less C functions acting on
+globals (updateEnergeticParticles, updateMhd, moveNodes; see
+include/eprem_gpu.h).  ``EpremRun`` keeps the same verbs, backed by
+libeprem_gpu.so through ctypes: state is uploaded once, the verbs run on the
+GPU, and results are downloaded when the caller asks.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is present,
+construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libeprem_gpu.so")
+DP = C.POINTER(C.c_double)
+
+# Every entry point of include/eprem_gpu.h: (name, restype, argtypes)
+EXPORTS = [
+    ("eprem_gpu_create", C.c_int,
+     [C.POINTER(abi.Dims), C.POINTER(abi.Params), C.POINTER(abi.Grids), C.POINTER(C.c_void_p)]),
+    ("eprem_gpu_destroy", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_upload_f", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_download_f", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_upload_nodes", C.c_int, [C.c_void_p, DP, C.c_uint64]),
+    ("eprem_gpu_download_nodes", C.c_int, [C.c_void_p, DP, C.c_uint64]),
+    ("eprem_gpu_update_energetic_particles", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_read_stats", C.c_int, [C.c_void_p, C.POINTER(abi.EpStats)]),
+    ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_synchronize", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_stream", C.c_void_p, [C.c_void_p]),
+    ("eprem_gpu_kernel_launches", C.c_uint64, [C.c_void_p]),
+    ("eprem_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("eprem_gpu_read_kernel_timing", C.c_int, [C.c_void_p, C.POINTER(abi.KernelTime)]),
+    ("eprem_gpu_last_error", C.c_char_p, []),
+]
+
+_lib = None
+
+
+class EpremGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libeprem_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    for name, res, args in EXPORTS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def _dp(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(DP)
+
+
+class EpremRun:
+    """One set of streams resident on the current GPU."""
+
+    def __init__(self, dims: abi.Dims, params: abi.Params, grids: dict):
+        self.lib = load_library()
+        self.dims = dims
+        self.params = params
+        self._grids_keep = {k: np.ascontiguousarray(grids[k], dtype=np.float64)
+                            for k in ("egrid", "vgrid", "vgrid_i", "mugrid", "rigidity")}
+        g = abi.Grids(*(self._grids_keep[k].ctypes.data_as(DP)
+                        for k in ("egrid", "vgrid", "vgrid_i", "mugrid", "rigidity")),
+                      float(grids["dlnp"]), float(grids["dmu"]))
+        h = C.c_void_p()
+        self._check(self.lib.eprem_gpu_create(C.byref(dims), C.byref(params), C.byref(g),
+                                              C.byref(h)))
+        self.handle = h
+
+    # -- helpers ------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != abi.EPREM_GPU_OK:
+            raise EpremGpuError(rc, self.lib.eprem_gpu_last_error().decode())
+
+    @property
+    def num_cells(self) -> int:
+        d = self.dims
+        return d.num_streams * d.num_nodes * d.num_energies * d.num_mu
+
+    @property
+    def num_nodes_total(self) -> int:
+        return self.dims.num_streams * self.dims.num_nodes
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eprem_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ---------------------------------------------------------------
+    def upload_f(self, f: np.ndarray):
+        assert f.size == self.num_cells
+        self._check(self.lib.eprem_gpu_upload_f(self.handle, _dp(f)))
+
+    def download_f(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.num_cells) if out is None else out
+        self._check(self.lib.eprem_gpu_download_f(self.handle, _dp(out)))
+        return out
+
+    def upload_nodes(self, nodes: np.ndarray, mask: int = abi.NODE_MASK_ALL):
+        assert nodes.size == abi.NODE_NFIELDS * self.num_nodes_total
+        self._check(self.lib.eprem_gpu_upload_nodes(self.handle, _dp(nodes), mask))
+
+    def download_nodes(self, out: np.ndarray | None = None,
+                       mask: int = abi.NODE_MASK_ALL) -> np.ndarray:
+        out = (np.zeros((abi.NODE_NFIELDS, self.num_nodes_total)) if out is None else out)
+        self._check(self.lib.eprem_gpu_download_nodes(self.handle, _dp(out), mask))
+        return out
+
+    # -- the reference's verbs ------------------------------------------------
+    def update_energetic_particles(self, t_global: float = 0.0):
+        """updateEnergeticParticles (src/energeticParticles.c:70-203)."""
+        self._check(self.lib.eprem_gpu_update_energetic_particles(self.handle, t_global))
+
+    def update_mhd(self, t_global: float):
+        """updateMhd, analytic background (src/flow.c:36-154)."""
+        self._check(self.lib.eprem_gpu_update_mhd(self.handle, t_global))
+
+    def move_nodes(self, dt: float):
+        """moveNodes (src/simCore.c:737-785)."""
+        self._check(self.lib.eprem_gpu_move_nodes(self.handle, dt))
+
+    def read_stats(self) -> abi.EpStats:
+        st = abi.EpStats()
+        self._check(self.lib.eprem_gpu_read_stats(self.handle, C.byref(st)))
+        return st
+
+    def omni_flux(self) -> np.ndarray:
+        d = self.dims
+        out = np.empty(d.num_streams * d.num_nodes * d.num_energies)
+        self._check(self.lib.eprem_gpu_omni_flux(self.handle, _dp(out)))
+        return out
+
+    def synchronize(self):
+        self._check(self.lib.eprem_gpu_synchronize(self.handle))
+
+    def set_kernel_timing(self, enable: bool):
+        self._check(self.lib.eprem_gpu_set_kernel_timing(self.handle, int(enable)))
+
+    def read_kernel_timing(self) -> dict:
+        arr = (abi.KernelTime * len(abi.KERNEL_KINDS))()
+        self._check(self.lib.eprem_gpu_read_kernel_timing(self.handle, arr))
+        return {k: (arr[i].launches, arr[i].total_ms) for i, k in enumerate(abi.KERNEL_KINDS)}
+
+    @property
+    def stream(self) -> int:
+        return self.lib.eprem_gpu_stream(self.handle)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.eprem_gpu_kernel_launches(self.handle))

@@ -171,9 +171,28 @@ typedef struct {
   int32_t max_substeps_stream;     /* largest DiffuseStreamData nsteps         */
   int32_t pad;
   double  min_tau;                 /* min_tau (DBL_MAX when nothing computed)  */
-  double  cell_subcycles;          /* node*E*mu cells times sub-cycles done,
-                                      summed over streaming, focusing, change  */
+  double  stream_cell_subcycles;   /* sum over (stream, E) of nsteps*list*mu   */
+  double  focus_cell_subcycles;    /* sum over nodes of N_sub*E*mu (focusing)  */
+  double  change_cell_subcycles;   /* sum over nodes of N_sub*E*mu (change)    */
 } eprem_ep_stats_t;
+
+/* Kernel kinds for the optional per-launch timing below. */
+enum eprem_kernel_kind {
+  EPREM_KERNEL_GEOMETRY = 0,  /* updateStreamValues, GetStreamList, node factors */
+  EPREM_KERNEL_STREAM,        /* DiffuseStreamData (+ seed check)               */
+  EPREM_KERNEL_NODE,          /* AdiabaticFocusing + AdiabaticChange            */
+  EPREM_KERNEL_SEED_CHECK,    /* seedPopulationCheck alone                      */
+  EPREM_KERNEL_MHD,           /* updateMhd                                      */
+  EPREM_KERNEL_MOVE,          /* moveNodes                                      */
+  EPREM_KERNEL_FLUX,          /* omnidirectional flux                           */
+  EPREM_KERNEL_CONVERT,       /* f format conversion (FP32 form)                */
+  EPREM_KERNEL_NKINDS
+};
+typedef struct {
+  int32_t launches;   /* launches of this kind since the last read */
+  int32_t pad;
+  double  total_ms;   /* summed CUDA-event time of those launches  */
+} eprem_kernel_time_t;
 
 typedef struct eprem_gpu_run eprem_gpu_run;
 
@@ -236,6 +255,14 @@ int eprem_gpu_synchronize(eprem_gpu_run *run);
  * counterpart. */
 void    *eprem_gpu_stream(eprem_gpu_run *run);
 uint64_t eprem_gpu_kernel_launches(const eprem_gpu_run *run);
+
+/* Per-launch CUDA-event timing of the run's kernels on its stream (off by
+ * default).  read_kernel_timing fills out[EPREM_KERNEL_NKINDS], synchronizes
+ * and restarts the accumulation.  Measurement helpers without a reference
+ * counterpart (the reference accumulates MPI_Wtime per phase instead,
+ * src/energeticParticles.c:122-172). */
+int eprem_gpu_set_kernel_timing(eprem_gpu_run *run, int enable);
+int eprem_gpu_read_kernel_timing(eprem_gpu_run *run, eprem_kernel_time_t *out);
 
 /* Message of the last failure on this thread ("" if none). */
 const char *eprem_gpu_last_error(void);

@@ -372,7 +372,7 @@ static int orc_diffuse_stream(orc_job_t *job, orc_work_t *w, int s, int L, doubl
           f_old[(size_t)L * m + sl] = iso + (f_new[(size_t)L * m + sl] - iso) * w->emt[sl];
         }
     }
-    job->stats.cell_subcycles += (double)nsteps * L * M;
+    job->stats.stream_cell_subcycles += (double)nsteps * L * M;
     for (int m = 0; m < M; m++)
       for (int sl = 0; sl < L; sl++) f[FIDX(s, w->list[sl], e, m)] = f_old[(size_t)L * m + sl];
     for (int m = 0; m < M; m++)
@@ -689,7 +689,7 @@ static int orc_focus_node(orc_job_t *job, orc_work_t *w, int s, int k, double dt
   double dt_sub = dt / N_sub;
   orc_opctx_t ctx = {w, p->adiabatic_focus_alg, E, M, g->dmu, 0.0, 0.0, p, g, 0.0};
   orc_subcycle(p->adiabatic_focus_alg, N_sub, dt_sub, fn, w->nf1, w->ns1, E * M, orc_focus_op, &ctx);
-  job->stats.cell_subcycles += (double)N_sub * E * M;
+  job->stats.focus_cell_subcycles += (double)N_sub * E * M;
   for (int e = 0; e < E; e++)
     for (int m = 0; m < M; m++) {
       double val = fn[e * M + m];
@@ -744,7 +744,7 @@ static int orc_change_node(orc_job_t *job, orc_work_t *w, int s, int k, double d
                      log(orc_seed_function(p, g->egrid[0], rmag)),
                      log(orc_seed_function(p, g->egrid[E - 1], rmag)), p, g, rmag};
   orc_subcycle(p->adiabatic_change_alg, N_sub, dt_sub, fl, w->nf1, w->ns1, E * M, orc_change_op, &ctx);
-  job->stats.cell_subcycles += (double)N_sub * E * M;
+  job->stats.change_cell_subcycles += (double)N_sub * E * M;
   for (int e = 0; e < E; e++)
     for (int m = 0; m < M; m++) {
       double val = exp(fl[e * M + m]);
@@ -885,7 +885,9 @@ int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_para
     if (js->max_substeps_stream > stats->max_substeps_stream)
       stats->max_substeps_stream = js->max_substeps_stream;
     if (js->min_tau < stats->min_tau) stats->min_tau = js->min_tau;
-    stats->cell_subcycles += js->cell_subcycles;
+    stats->stream_cell_subcycles += js->stream_cell_subcycles;
+    stats->focus_cell_subcycles += js->focus_cell_subcycles;
+    stats->change_cell_subcycles += js->change_cell_subcycles;
     if (rc == EPREM_GPU_OK && jobs[t].status != EPREM_GPU_OK) {
       rc = jobs[t].status;
       if (errbuf) snprintf(errbuf, 256, "%s", jobs[t].err);
@@ -1045,4 +1047,47 @@ void orc_omni_flux(const eprem_dims_t *d, const eprem_grids_t *g, const double *
         iso /= M;
         out[((size_t)s * N + k) * E + e] = 2.0 * g->egrid[e] * iso;
       }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Layout of the public structs as this C compiler lays them out, so the test
+ * suite can check the Python (ctypes) mirror field by field. */
+#include <stddef.h>
+int orc_abi_layout(long *out, int cap) {
+  int n = 0;
+#define PUT(x) do { if (n < cap) out[n] = (long)(x); n++; } while (0)
+  PUT(sizeof(eprem_dims_t));
+  PUT(sizeof(eprem_params_t));
+  PUT(sizeof(eprem_grids_t));
+  PUT(sizeof(eprem_ep_stats_t));
+  PUT(EPREM_NODE_NFIELDS);
+#define OFF(T, f) PUT(offsetof(T, f))
+  OFF(eprem_dims_t, num_streams); OFF(eprem_dims_t, num_nodes); OFF(eprem_dims_t, num_species);
+  OFF(eprem_dims_t, num_energies); OFF(eprem_dims_t, num_mu); OFF(eprem_dims_t, precision);
+  OFF(eprem_params_t, r_scale); OFF(eprem_params_t, t_del); OFF(eprem_params_t, num_ep_steps);
+  OFF(eprem_params_t, use_parallel_diffusion); OFF(eprem_params_t, use_adiabatic_focus);
+  OFF(eprem_params_t, use_adiabatic_change); OFF(eprem_params_t, check_seed_population);
+  OFF(eprem_params_t, use_ep_boundary); OFF(eprem_params_t, use_boundary_function);
+  OFF(eprem_params_t, adiabatic_focus_alg); OFF(eprem_params_t, adiabatic_change_alg);
+  OFF(eprem_params_t, damp_cooling); OFF(eprem_params_t, dsh_min); OFF(eprem_params_t, mfp_type);
+  OFF(eprem_params_t, lamo); OFF(eprem_params_t, mfp_radial_power); OFF(eprem_params_t, mfp_b_power);
+  OFF(eprem_params_t, mhd_bs_au); OFF(eprem_params_t, bf_amplitude); OFF(eprem_params_t, bf_xi);
+  OFF(eprem_params_t, bf_gamma); OFF(eprem_params_t, bf_beta); OFF(eprem_params_t, bf_ecutoff);
+  OFF(eprem_params_t, bf_r0); OFF(eprem_params_t, mhd_us); OFF(eprem_params_t, mhd_ns_au);
+  OFF(eprem_params_t, omega_sun); OFF(eprem_params_t, ideal_shock);
+  OFF(eprem_params_t, ideal_shock_sharpness); OFF(eprem_params_t, ideal_shock_scale_length);
+  OFF(eprem_params_t, ideal_shock_jump); OFF(eprem_params_t, ideal_shock_falloff);
+  OFF(eprem_params_t, ideal_shock_speed); OFF(eprem_params_t, ideal_shock_init_time);
+  OFF(eprem_params_t, ideal_shock_theta); OFF(eprem_params_t, ideal_shock_phi);
+  OFF(eprem_params_t, ideal_shock_width); OFF(eprem_params_t, max_subcycles);
+  OFF(eprem_grids_t, egrid); OFF(eprem_grids_t, vgrid); OFF(eprem_grids_t, vgrid_i);
+  OFF(eprem_grids_t, mugrid); OFF(eprem_grids_t, rigidity); OFF(eprem_grids_t, dlnp);
+  OFF(eprem_grids_t, dmu);
+  OFF(eprem_ep_stats_t, max_subcycles_change); OFF(eprem_ep_stats_t, max_subcycles_focusing);
+  OFF(eprem_ep_stats_t, max_substeps_stream); OFF(eprem_ep_stats_t, pad);
+  OFF(eprem_ep_stats_t, min_tau); OFF(eprem_ep_stats_t, stream_cell_subcycles);
+  OFF(eprem_ep_stats_t, focus_cell_subcycles); OFF(eprem_ep_stats_t, change_cell_subcycles);
+#undef OFF
+#undef PUT
+  return n;
 }

@@ -1,0 +1,141 @@
+"""Parity of the CUDA path with the oracle, through the C ABI.
+
+The plain form must match the reference's C path in FP64 within 1e-12
+relative on f (the oracle is pinned bit-exact to the reference C in
+test_oracle_vs_reference.py and against committed reference outputs in
+test_oracle_golden.py).  Sub-cycle counts are integers and must be equal;
+ds and the neighbouring |B| are computed without fused multiply-adds and must
+be bit-equal.
+"""
+import numpy as np
+import pytest
+
+from eprem_gb300 import EpremRun, abi, workloads as W
+
+from helpers import oracle_update, primed_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+F_RTOL = 1e-12  # spec tolerance for the plain FP64 form
+
+
+def _cases():
+    c = {}
+    c["tiny"] = W.custom(1, 1, 48, 8, 6, num_ep_steps=2)
+    c["wind-like (thinned streams)"] = W.testsuite_like("wind", 1, 1, 30)
+    c["cone-like (ideal shock)"] = W.testsuite_like("cone", 1, 1, 40)
+    c["small-shape slab 400x20x20"] = W.custom(1, 1, 400, 20, 20, num_ep_steps=2)
+    c["multi-CTA cluster 1200 nodes x 40 mu"] = W.custom(1, 1, 1200, 4, 40, num_ep_steps=1)
+    c["mu=64 e=64 bins"] = W.custom(1, 1, 60, 64, 64, num_ep_steps=1)
+    c["odd mu (zero-crossing cell)"] = W.custom(1, 1, 50, 7, 9, num_ep_steps=2)
+    c["rk3 upwind"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2, adiabatic_focus_alg=2,
+                               adiabatic_change_alg=2)
+    c["rk3 weno3"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2, adiabatic_focus_alg=3,
+                              adiabatic_change_alg=3)
+    c["mfp by B, damped cooling"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2, mfp_type=2,
+                                             damp_cooling=0.3)
+    c["no parallel diffusion"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2,
+                                          use_parallel_diffusion=0)
+    c["no seed check, no boundary"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2,
+                                               check_seed_population=0, use_ep_boundary=0)
+    c["focus only"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2, use_parallel_diffusion=0,
+                               use_adiabatic_change=0)
+    c["change only"] = W.custom(1, 1, 40, 10, 8, num_ep_steps=2, use_parallel_diffusion=0,
+                                use_adiabatic_focus=0)
+    return c
+
+
+CASES = _cases()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp64_matches_oracle(name, oracle_lib):
+    w = CASES[name]
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    f_ref, nodes_ref, stats = oracle_update(oracle_lib, w, g, f, nodes, calls=2)
+    run = EpremRun(d, w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles(0.0)
+    st1 = run.read_stats()
+    run.update_energetic_particles(0.0)
+    st2 = run.read_stats()
+    f_gpu = run.download_f()
+    nodes_gpu = run.download_nodes()
+    run.close()
+    assert rel_err(f_gpu, f_ref) <= F_RTOL
+    for fld in ("DS", "BMAG_PLUS", "BMAG_MINUS"):
+        np.testing.assert_array_equal(nodes_gpu[abi.NODE[fld]], nodes_ref[abi.NODE[fld]])
+    for st_g, st_o in ((st1, stats[0]), (st2, stats[1])):
+        assert st_g.max_subcycles_focusing == st_o.max_subcycles_focusing
+        assert st_g.max_subcycles_change == st_o.max_subcycles_change
+        assert st_g.max_substeps_stream == st_o.max_substeps_stream
+        assert st_g.stream_cell_subcycles == st_o.stream_cell_subcycles
+        assert st_g.focus_cell_subcycles == st_o.focus_cell_subcycles
+        assert st_g.change_cell_subcycles == st_o.change_cell_subcycles
+        assert abs(st_g.min_tau - st_o.min_tau) <= 1e-13 * st_o.min_tau
+
+
+def test_many_streams_independent(oracle_lib):
+    """24 streams in one launch give the same values as the oracle stream by
+    stream (no cross-stream coupling or ordering effect)."""
+    w = W.custom(2, 2, 64, 12, 8, num_ep_steps=3)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes)
+    run = EpremRun(d, w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles(0.0)
+    assert rel_err(run.download_f(), f_ref) <= F_RTOL
+    run.close()
+
+
+def test_mhd_and_node_push_match_oracle(oracle_lib):
+    """updateMhd (analytic + ideal shock) and moveNodes against the oracle."""
+    w = W.testsuite_like("cone", 1, 1, 40)
+    d = w.dims()
+    g = W.build_grids(w)
+    nodes = W.initial_nodes(w)
+    oracle_lib.update_mhd(d, w.params, nodes, 0.0)
+    ref = nodes.copy()
+    t = 2.0 / W.DAY  # inside the shock's reach for this configuration
+    oracle_lib.move_nodes(d, w.params, ref, w.params.t_del)
+    oracle_lib.update_mhd(d, w.params, ref, t)
+    run = EpremRun(d, w.params, g)
+    run.upload_nodes(nodes)
+    run.move_nodes(w.params.t_del)
+    run.update_mhd(t)
+    out = run.download_nodes()
+    run.close()
+    for i, name in enumerate(abi.NODE_FIELDS):
+        a, b = out[i], ref[i]
+        scale = np.maximum(np.abs(b), 1e-300)
+        err = np.max(np.abs(a - b) / scale) if np.any(b != 0) else np.max(np.abs(a))
+        tol = 1e-10 if name in ("DLNB", "DLNN", "DUPAR", "DIVV") else 1e-13
+        assert err <= tol, (name, err)
+
+
+def test_omni_flux_matches_oracle(oracle_lib):
+    w = W.custom(1, 1, 30, 8, 6)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    gs, keep = W.grids_struct(g)
+    ref = oracle_lib.omni_flux(d, gs, f)
+    run = EpremRun(d, w.params, g)
+    run.upload_f(f)
+    out = run.omni_flux()
+    run.close()
+    assert rel_err(out, ref) <= 1e-14
+
+
+def test_kernel_launch_count(oracle_lib):
+    w = W.custom(1, 1, 30, 8, 6, num_ep_steps=3)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    run = EpremRun(d, w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    n0 = run.kernel_launches
+    run.update_energetic_particles(0.0)
+    run.synchronize()
+    # geometry (2) + per sub-step streaming (1) and focusing/change (1)
+    assert run.kernel_launches - n0 == 2 + 2 * 3
+    run.close()
