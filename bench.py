@@ -1,0 +1,457 @@
+"""Benchmark of the GB300 energetic-particle update.
+
+Metric: cell-updates/s, one cell-update = one (node, energy, mu) cell through
+one EP sub-step (streaming + isotropisation, focusing, adiabatic change).  A
+step is one driver step of the hot path: moveNodes + updateMhd +
+updateEnergeticParticles (numEpSteps = 30 sub-steps), src/eprem.c:620-671.
+
+Workload (default): the precision-at-scale case -- 1536 streams x 1000 nodes x
+50 energies (0.1-1000 MeV) x 40 mu, Parker wind, seed power law -- in the
+chosen form (f and stencil arithmetic in FP32, geometry / CFL in FP64).  The
+plain FP64 form is measured beside it on a 96-stream subset with identical
+per-stream work, and the FP32 omnidirectional flux is compared with it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  Under torchrun every rank runs its own
+independent copy of the workload (streams are independent; no collective on
+the data path), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "cell-updates/s (node*E*mu) plain FP64 vs chosen form at <=1e-3 rel flux err"
+UNIT = "cell-updates/s"
+FLOPS_PER_CELL_SUBCYCLE = {"stream": 8.0, "focus": 11.0, "change": 11.0}
+BYTES_PER_CELL_UPDATE = {"fp64": 32.0, "fp32": 16.0}
+
+
+# ---------------------------------------------------------------------------
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["scale", "small"], default="scale")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--fp64-faces", type=int, default=4,
+                    help="rows=cols of the plain-FP64 subset (6*n*n streams)")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return rank, ws, dist
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self._t:
+                self._t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def make_state(w, precision, run_cls, abi, W):
+    """Device run primed as the driver primes it: positions on Parker
+    spirals, updateMhd, moveNodes, updateMhd, then the seed distribution."""
+    g = W.build_grids(w)
+    d = w.dims(precision)
+    run = run_cls(d, w.params, g)
+    nodes = W.initial_nodes(w)
+    run.upload_nodes(nodes)
+    run.update_mhd(0.0)
+    run.move_nodes(w.params.t_del)
+    run.update_mhd(w.params.t_del)
+    nodes = run.download_nodes()
+    return run, g, nodes
+
+
+def host_f(w, nodes, g, W, pinned=True):
+    n = w.cells
+    if pinned:
+        import torch
+        buf = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    else:
+        buf = np.empty(n)
+    return W.fill_initial_f(w, nodes, g, buf)
+
+
+def step(run, t, w):
+    """One driver step of the hot path (src/eprem.c:620-671)."""
+    run.move_nodes(w.params.t_del)
+    run.update_mhd(t + w.params.t_del)
+    run.update_energetic_particles(t)
+    return t + w.params.t_del
+
+
+def event_pair(stream_ptr):
+    import torch
+    s = torch.cuda.ExternalStream(stream_ptr)
+    return s, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def flops_of(stats) -> dict:
+    return {"stream": FLOPS_PER_CELL_SUBCYCLE["stream"] * stats.stream_cell_subcycles,
+            "node": FLOPS_PER_CELL_SUBCYCLE["focus"] * stats.focus_cell_subcycles
+            + FLOPS_PER_CELL_SUBCYCLE["change"] * stats.change_cell_subcycles}
+
+
+def timed_steps(run, w, steps, t0):
+    """K steps on device-resident state, CUDA events on the run's stream."""
+    import torch
+    s, e0, e1 = event_pair(run.stream)
+    run.read_stats()
+    run.set_kernel_timing(True)
+    run.read_kernel_timing()
+    n0 = run.kernel_launches
+    torch.cuda.synchronize()
+    e0.record(s)
+    t = t0
+    for _ in range(steps):
+        t = step(run, t, w)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = run.kernel_launches - n0
+    kt = run.read_kernel_timing()
+    stats = run.read_stats()
+    run.set_kernel_timing(False)
+    return ms, launches, kt, stats, t
+
+
+def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
+    """Roofline of the dominant kernel: algorithmic flops per launch over the
+    kernel's mean CUDA-event duration, against the measured FMA peak."""
+    kind = max(("stream", "node"), key=lambda k: kt[k][1])
+    launches, total_ms = kt[kind]
+    fl = flops_of(stats)[kind]
+    per_launch_flops = fl / launches
+    mean_s = total_ms / launches * 1e-3
+    achieved = per_launch_flops / mean_s / 1e12
+    # algorithmic HBM bytes: one read + one write of f per operator pass
+    bytes_per_launch = cells * BYTES_PER_CELL_UPDATE[form] / 2.0
+    return {
+        "kernel": "k_stream" if kind == "stream" else "k_node",
+        "bound": "fp64" if form == "fp64" else "fp32",
+        "achieved": round(achieved, 3), "peak": round(peak_tflops, 3), "unit": "TFLOP/s",
+        "frac": round(achieved / peak_tflops, 4),
+        "peak_source": "measured FMA-chain kernel on this GPU (eprem_gpu_alu_peak)",
+        "traffic": None,
+        "launches": launches, "mean_launch_ms": round(total_ms / launches, 3),
+        "hbm_achieved_gbs": round(bytes_per_launch / mean_s / 1e9, 2),
+        "hbm_peak_gbs": hbm_peak,
+        "hbm_frac": round(bytes_per_launch / mean_s / 1e9 / hbm_peak, 5) if hbm_peak else None,
+        "share_of_step": round(total_ms / sum(v[1] for v in kt.values()), 4),
+    }
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(w, W, abi, nthreads):
+    """The oracle port on the host cores: `nthreads` streams, one EP sub-step
+    of the same dt (tDel / numEpSteps) -- a bounded sample of the workload."""
+    import ctypes as C
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as orc  # CPU baseline leg only
+    o = orc.Oracle()
+    ns = max(1, min(nthreads, w.num_streams))
+    rows = cols = 1
+    sub = W.with_faces(w, rows, cols)
+    d = sub.dims()
+    g = W.build_grids(sub)
+    nodes = W.initial_nodes(sub)
+    o.update_mhd(d, sub.params, nodes, 0.0)
+    o.move_nodes(d, sub.params, nodes, sub.params.t_del)
+    o.update_mhd(d, sub.params, nodes, sub.params.t_del)
+    # repeat the 6 streams until there are ns of them
+    reps = (ns + 5) // 6
+    S = 6 * reps
+    N = sub.num_nodes
+    big_nodes = np.tile(nodes.reshape(abi.NODE_NFIELDS, 6, N), (1, reps, 1)).reshape(
+        abi.NODE_NFIELDS, S * N)
+    f6 = W.initial_f(sub, nodes, g)
+    f = np.tile(f6.reshape(6, -1), (reps, 1)).reshape(-1)
+    p = abi.Params.from_buffer_copy(bytes(sub.params))
+    p.t_del = sub.params.t_del / sub.params.num_ep_steps
+    p.num_ep_steps = 1
+    dd = abi.Dims(S, N, 1, sub.num_energies, sub.num_mu, abi.EPREM_FP64)
+    gs, keep = W.grids_struct(g)
+    t0 = time.perf_counter()
+    rc, st, err = o.update_energetic_particles(dd, p, gs, f, big_nodes, nthreads=nthreads,
+                                               streams=(0, ns))
+    dt = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError(err)
+    cells = ns * N * sub.num_energies * sub.num_mu
+    return cells / dt, dt, ns
+
+
+def reference_arm(args, rank, ws, dist):
+    from eprem_gb300 import abi, workloads as W
+    if rank != 0:
+        return
+    w = W.scale_plain() if args.workload == "scale" else W.small_plain()
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(w, W, abi, nthreads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        v, dt, ns = cpu_sample(w, W, abi, nthreads)
+        vals.append(v)
+        secs.append(dt)
+    value = statistics.mean(vals)
+    sample = (f"{ns} streams of the {w.name} workload, one EP sub-step each "
+              f"(dt = tDel/{w.params.num_ep_steps}), one stream per thread")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": w.name, "form": "reference CPU algorithm (oracle port), FP64"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def ours(args, rank, ws, dist):
+    import torch
+    from eprem_gb300 import EpremRun, abi, workloads as W
+    from eprem_gb300.runtime import alu_peak_tflops
+
+    w = W.scale_plain() if args.workload == "scale" else W.small_plain()
+    if ws > 1:
+        w.seed += rank  # independent ensemble member per rank
+    peaks = measured_peaks()
+    fp32_peak = alu_peak_tflops(abi.EPREM_FP32)
+    fp64_peak = alu_peak_tflops(abi.EPREM_FP64)
+
+    # ---- device-resident FP32 run ---------------------------------------
+    run, g, nodes = make_state(w, abi.EPREM_FP32, EpremRun, abi, W)
+    f_host = host_f(w, nodes, g, W, pinned=True)
+    run.upload_f(f_host)
+    run.synchronize()
+    t = w.params.t_del
+    for _ in range(args.warmup):
+        t = step(run, t, w)
+    run.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms, launches, kt, stats, t = timed_steps(run, w, args.steps, t)
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms_max = reduce_max(dist, ms)
+    cell_updates = w.cells * w.params.num_ep_steps * args.steps
+    value = cell_updates * ws / (ms_max * 1e-3)
+    roof = roofline(kt, stats, args.steps, fp32_peak, peaks.get("hbm_gbs"), w.cells, "fp32")
+
+    # ---- end to end through the C ABI with host buffers ------------------
+    nodes_host = torch.empty(nodes.size, dtype=torch.float64, pin_memory=True).numpy()
+    nodes_host[:] = run.download_nodes().reshape(-1)
+    nodes_host = nodes_host.reshape(abi.NODE_NFIELDS, -1)
+    f_host[:] = run.download_f(f_host)
+    s, e0, e1 = event_pair(run.stream)
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(args.e2e_steps):
+        run.upload_f(f_host)
+        run.upload_nodes(nodes_host)
+        t = step(run, t, w)
+        run.download_f(f_host)
+        run.download_nodes(nodes_host)
+    e1.record(s)
+    e1.synchronize()
+    e2e_ms = reduce_max(dist, e0.elapsed_time(e1))
+    e2e_value = w.cells * w.params.num_ep_steps * args.e2e_steps * ws / (e2e_ms * 1e-3)
+    h2d = f_host.nbytes + nodes_host.nbytes
+    run.close()
+    del f_host
+
+    # ---- plain FP64 form and the FP32 flux error on a stream subset ------
+    plain = None
+    if not args.skip_fp64 and rank == 0:
+        sub = W.with_faces(w, args.fp64_faces, args.fp64_faces)
+        r64, g64, n64 = make_state(sub, abi.EPREM_FP64, EpremRun, abi, W)
+        r32, _, _ = make_state(sub, abi.EPREM_FP32, EpremRun, abi, W)
+        f0 = host_f(sub, n64, g64, W, pinned=False)
+        r64.upload_f(f0)
+        r32.upload_f(f0)
+        tt = sub.params.t_del
+        tt = step(r64, tt, sub)
+        step(r32, sub.params.t_del, sub)
+        r32.synchronize()
+        ms64, l64, kt64, st64, _ = timed_steps(r64, sub, 1, tt)
+        ms32, _, _, _, _ = timed_steps(r32, sub, 1, tt)
+        j64 = r64.omni_flux()
+        j32 = r32.omni_flux()
+        mask = j64 > 1e-30 * j64.max()
+        flux_err = float(np.max(np.abs(j32[mask] - j64[mask]) / j64[mask]))
+        cu = sub.cells * sub.params.num_ep_steps
+        plain = {
+            "value": cu / (ms64 * 1e-3), "unit": UNIT, "streams": sub.num_streams,
+            "ms_per_step": ms64,
+            "fp32_same_subset_value": cu / (ms32 * 1e-3),
+            "roofline": roofline(kt64, st64, 1, fp64_peak, peaks.get("hbm_gbs"), sub.cells,
+                                 "fp64"),
+            "flux_rel_err_fp32_vs_fp64": flux_err,
+            "flux_err_steps": 2,
+        }
+        r64.close()
+        r32.close()
+
+    # ---- CPU baseline ----------------------------------------------------
+    cpu = None
+    if not args.skip_cpu and rank == 0 and ws == 1:
+        nthreads = os.cpu_count() or 1
+        v, dt, ns = cpu_sample(w, W, abi, nthreads)
+        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{ns} streams x 1 EP sub-step of the same workload ({dt:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": w.name, "form": "FP32 f and stencils, FP64 positions/ds/CFL",
+                "streams": w.num_streams, "nodes": w.num_nodes, "energies": w.num_energies,
+                "mu": w.num_mu, "ep_substeps_per_step": w.params.num_ep_steps,
+                "t_del_s": w.params.t_del * W.TAU, "step": "moveNodes+updateMhd+updateEnergeticParticles",
+                "l2": "inputs larger than L2 (f = %.1f GB on the device)" % (w.cells * 4 / 1e9),
+                "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            },
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": h2d, "steps": args.e2e_steps},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "plain_fp64": plain,
+            "alu_peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak},
+            "stats_last_step": stats.as_dict(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, ws, dist = dist_setup()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, rank, ws, dist)
+        else:
+            ours(args, rank, ws, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -29,21 +29,27 @@ __global__ void k_node_prep(RunView r, double norm_radius, double neg_beta, int 
     const double rs = r.r_scale;
     const double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
                  *rz = node_field(r, EPREM_NODE_RZ), *bmag = node_field(r, EPREM_NODE_BMAG);
-    double x = rx[g] * rs, y = ry[g] * rs, z = rz[g] * rs;
+    // __dmul_rn keeps the scaled coordinates out of fused multiply-adds with
+    // the differences below (the reference scales, then subtracts).
+    double x = __dmul_rn(rx[g], rs), y = __dmul_rn(ry[g], rs), z = __dmul_rn(rz[g], rs);
     double ds, bminus, bplus;
     if (k == 0) {
-      double px = rx[g + 1] * rs, py = ry[g + 1] * rs, pz = rz[g + 1] * rs;
+      double px = __dmul_rn(rx[g + 1], rs), py = __dmul_rn(ry[g + 1], rs),
+             pz = __dmul_rn(rz[g + 1], rs);
       ds = dist3(px - x, py - y, pz - z);
       bminus = bmag[g];
       bplus = bmag[g + 1];
     } else if (k == r.N - 1) {
-      double mx = rx[g - 1] * rs, my = ry[g - 1] * rs, mz = rz[g - 1] * rs;
+      double mx = __dmul_rn(rx[g - 1], rs), my = __dmul_rn(ry[g - 1], rs),
+             mz = __dmul_rn(rz[g - 1], rs);
       ds = dist3(x - mx, y - my, z - mz);
       bminus = bmag[g - 1];
       bplus = bmag[g];
     } else {
-      double px = rx[g + 1] * rs, py = ry[g + 1] * rs, pz = rz[g + 1] * rs;
-      double mx = rx[g - 1] * rs, my = ry[g - 1] * rs, mz = rz[g - 1] * rs;
+      double px = __dmul_rn(rx[g + 1], rs), py = __dmul_rn(ry[g + 1], rs),
+             pz = __dmul_rn(rz[g + 1], rs);
+      double mx = __dmul_rn(rx[g - 1], rs), my = __dmul_rn(ry[g - 1], rs),
+             mz = __dmul_rn(rz[g - 1], rs);
       double dsp = dist3(px - x, py - y, pz - z);
       double dsm = dist3(x - mx, y - my, z - mz);
       ds = 0.5 * (dsp + dsm);
@@ -84,9 +90,9 @@ __global__ void k_stream_list(RunView r) {
   const double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
                *rz = node_field(r, EPREM_NODE_RZ);
   for (int k = lane; k < N; k += 32) {
-    xs[k] = rx[base + k] * rs;
-    ys[k] = ry[base + k] * rs;
-    zs[k] = rz[base + k] * rs;
+    xs[k] = __dmul_rn(rx[base + k], rs);
+    ys[k] = __dmul_rn(ry[base + k], rs);
+    zs[k] = __dmul_rn(rz[base + k], rs);
   }
   __syncwarp();
   if (lane == 0) {

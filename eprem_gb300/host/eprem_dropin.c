@@ -1,0 +1,261 @@
+/*
+ * eprem_dropin.c -- the GB300 path behind EPREM's own hot-path entry points.
+ *
+ * Link this file and libeprem_gpu.so into the reference build in place of the
+ * bodies of
+ *   updateEnergeticParticles()  src/energeticParticles.c:70-203
+ *   updateMhd()                 src/flow.c:36-154
+ *   moveNodes(dt)               src/simCore.c:737-785
+ * (INTEGRATION.md gives the build lines: the three originals are renamed with
+ * -D at compile time so that the driver src/eprem.c, unchanged, calls these).
+ *
+ * The reference keeps its state in globals (grid[], eParts[], config, the
+ * 1-D grids of energeticParticlesTypes.h); each call here packs what the GPU
+ * needs into the plain arrays of include/eprem_gpu.h, runs the GPU entry
+ * point and unpacks the results, so everything else in the driver -- output,
+ * shell spawning, MAS reading -- sees the same globals as before.
+ *
+ * Scope: one MPI rank holds every stream (the GPU replaces the rank
+ * decomposition), one species, analytic background (MAS coupling is refused
+ * with the reference's panic), no drift or shell diffusion.
+ */
+#include <float.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "baseTypes.h"
+#include "configuration.h"
+#include "cubeShellStruct.h"
+#include "energeticParticles.h"
+#include "energeticParticlesTypes.h"
+#include "error.h"
+#include "flow.h"
+#include "global.h"
+#include "mpiInit.h"
+#include "simCore.h"
+#include "timers.h"
+
+#include "eprem_gpu.h"
+
+static eprem_gpu_run *dropin_run = NULL;
+static double *dropin_f = NULL;     /* [S][N][E][M] host staging of eParts   */
+static double *dropin_nodes = NULL; /* [field][S*N] host staging of grid[]   */
+static size_t dropin_sn = 0, dropin_cells = 0;
+
+static void dropin_check(int rc, const char *what) {
+  if (rc != EPREM_GPU_OK) {
+    static char msg[512];
+    snprintf(msg, sizeof(msg), "%s: %s", what, eprem_gpu_last_error());
+    panic(msg);
+  }
+}
+
+/* Node_t member for each eprem_node_field (src/cubeShellStruct.h:51-93). */
+static double *dropin_member(Node_t *n, int field) {
+  switch (field) {
+    case EPREM_NODE_RX: return &n->r.x;
+    case EPREM_NODE_RY: return &n->r.y;
+    case EPREM_NODE_RZ: return &n->r.z;
+    case EPREM_NODE_RMAG: return &n->rmag;
+    case EPREM_NODE_BMAG: return &n->mhdBmag;
+    case EPREM_NODE_DLNB: return &n->mhdDlnB;
+    case EPREM_NODE_DLNN: return &n->mhdDlnN;
+    case EPREM_NODE_DUPAR: return &n->mhdDuPar;
+    case EPREM_NODE_DS: return &n->ds;
+    case EPREM_NODE_BMAG_PLUS: return &n->mhdBmagPlus;
+    case EPREM_NODE_BMAG_MINUS: return &n->mhdBmagMinus;
+    case EPREM_NODE_BR: return &n->mhdBr;
+    case EPREM_NODE_BTHETA: return &n->mhdBtheta;
+    case EPREM_NODE_BPHI: return &n->mhdBphi;
+    case EPREM_NODE_VR: return &n->mhdVr;
+    case EPREM_NODE_VTHETA: return &n->mhdVtheta;
+    case EPREM_NODE_VPHI: return &n->mhdVphi;
+    case EPREM_NODE_VMAG: return &n->mhdVmag;
+    case EPREM_NODE_DENSITY: return &n->mhdDensity;
+    case EPREM_NODE_DIVV: return &n->mhdDivV;
+    case EPREM_NODE_BVEC_X: return &n->mhdBvec.x;
+    case EPREM_NODE_BVEC_Y: return &n->mhdBvec.y;
+    case EPREM_NODE_BVEC_Z: return &n->mhdBvec.z;
+    case EPREM_NODE_VVEC_X: return &n->mhdVvec.x;
+    case EPREM_NODE_VVEC_Y: return &n->mhdVvec.y;
+    case EPREM_NODE_VVEC_Z: return &n->mhdVvec.z;
+    case EPREM_NODE_BMAG_OLD: return &n->mhdBmagOld;
+    case EPREM_NODE_DENSITY_OLD: return &n->mhdDensityOld;
+    case EPREM_NODE_VSPH_OLD_R: return &n->mhdVsphOld.r;
+    case EPREM_NODE_VSPH_OLD_THETA: return &n->mhdVsphOld.theta;
+    case EPREM_NODE_VSPH_OLD_PHI: return &n->mhdVsphOld.phi;
+    case EPREM_NODE_DS_OLD: return &n->dsOld;
+    case EPREM_NODE_ROLD_X: return &n->rOld.x;
+    case EPREM_NODE_ROLD_Y: return &n->rOld.y;
+    case EPREM_NODE_ROLD_Z: return &n->rOld.z;
+    case EPREM_NODE_ROLDER_X: return &n->rOlder.x;
+    case EPREM_NODE_ROLDER_Y: return &n->rOlder.y;
+    case EPREM_NODE_ROLDER_Z: return &n->rOlder.z;
+  }
+  return NULL;
+}
+
+/* First call: size the run from the reference globals and create it. */
+static void dropin_init(void) {
+  if (dropin_run) return;
+  if (N_PROCS != 1) panic("GPU path: run with one MPI rank (every stream lives on the GPU)");
+  if (config.masCouple > 0) panic("GPU path: MAS coupling is not supported by this build");
+  if (config.useDrift > 0 || config.useShellDiffusion > 0)
+    panic("GPU path: drift and shell diffusion are not supported by this build");
+  eprem_dims_t d;
+  d.num_streams = NUM_STREAMS;
+  d.num_nodes = TOTAL_NUM_SHELLS;
+  d.num_species = NUM_SPECIES;
+  d.num_energies = NUM_ESTEPS;
+  d.num_mu = NUM_MUSTEPS;
+  d.precision = getenv("EPREM_GPU_FP32") ? EPREM_FP32 : EPREM_FP64;
+  eprem_params_t p;
+  memset(&p, 0, sizeof(p));
+  p.r_scale = config.rScale;
+  p.t_del = config.tDel;
+  p.num_ep_steps = config.numEpSteps;
+  p.use_parallel_diffusion = config.useParallelDiffusion;
+  p.use_adiabatic_focus = config.useAdiabaticFocus;
+  p.use_adiabatic_change = config.useAdiabaticChange;
+  p.check_seed_population = config.checkSeedPopulation;
+  p.use_ep_boundary = config.useEPBoundary;
+  p.use_boundary_function = config.useBoundaryFunction;
+  p.adiabatic_focus_alg = config.adiabaticFocusAlg;
+  p.adiabatic_change_alg = config.adiabaticChangeAlg;
+  p.damp_cooling = config.dampCooling;
+  p.dsh_min = config.dsh_min;
+  p.mfp_type = config.mfpType;
+  p.lamo = config.lamo;
+  p.mfp_radial_power = config.mfpRadialPower;
+  p.mfp_b_power = config.mfpBPower;
+  p.mhd_bs_au = config.mhdBsAu;
+  p.bf_amplitude = config.boundaryFunctAmplitude;
+  p.bf_xi = config.boundaryFunctXi;
+  p.bf_gamma = config.boundaryFunctGamma;
+  p.bf_beta = config.boundaryFunctBeta;
+  p.bf_ecutoff = config.boundaryFunctEcutoff;
+  p.bf_r0 = config.boundaryFunctR0;
+  p.mhd_us = config.mhdUs;
+  p.mhd_ns_au = config.mhdNsAu;
+  p.omega_sun = config.omegaSun;
+  p.ideal_shock = config.idealShock;
+  p.ideal_shock_sharpness = config.idealShockSharpness;
+  p.ideal_shock_scale_length = config.idealShockScaleLength;
+  p.ideal_shock_jump = config.idealShockJump;
+  p.ideal_shock_falloff = config.idealShockFalloff;
+  p.ideal_shock_speed = config.idealShockSpeed;
+  p.ideal_shock_init_time = config.idealShockInitTime;
+  p.ideal_shock_theta = config.idealShockTheta;
+  p.ideal_shock_phi = config.idealShockPhi;
+  p.ideal_shock_width = config.idealShockWidth;
+  p.max_subcycles = 0;
+  eprem_grids_t g;
+  g.egrid = egrid;
+  g.vgrid = vgrid;
+  g.vgrid_i = vgrid_i;
+  g.mugrid = mugrid;
+  g.rigidity = rigidity;
+  g.dlnp = dlnp;
+  g.dmu = dmu;
+  dropin_check(eprem_gpu_create(&d, &p, &g, &dropin_run), "eprem_gpu_create");
+  dropin_sn = (size_t)d.num_streams * d.num_nodes;
+  dropin_cells = dropin_sn * d.num_energies * d.num_mu;
+  dropin_f = (double *)malloc(sizeof(double) * dropin_cells);
+  dropin_nodes = (double *)malloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
+  if (!dropin_f || !dropin_nodes) panic("GPU path: host staging allocation failed");
+}
+
+/* grid[] shells 1..N of every stream <-> nodes[field][s*N+k] (k = shell-1) */
+static void dropin_pack_nodes(uint64_t mask) {
+  const int N = TOTAL_NUM_SHELLS;
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    for (int k = 0; k < N; k++) {
+      Node_t *n = &grid[s * LOCAL_NUM_SHELLS + k + 1];
+      for (int fld = 0; fld < EPREM_NODE_NFIELDS; fld++)
+        if (mask & EPREM_NODE_MASK(fld))
+          dropin_nodes[fld * dropin_sn + s * N + k] = *dropin_member(n, fld);
+    }
+}
+
+static void dropin_unpack_nodes(uint64_t mask) {
+  const int N = TOTAL_NUM_SHELLS;
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    for (int k = 0; k < N; k++) {
+      Node_t *n = &grid[s * LOCAL_NUM_SHELLS + k + 1];
+      for (int fld = 0; fld < EPREM_NODE_NFIELDS; fld++)
+        if (mask & EPREM_NODE_MASK(fld))
+          *dropin_member(n, fld) = dropin_nodes[fld * dropin_sn + s * N + k];
+    }
+}
+
+/* eParts (with the INNER_SHELL ghost) <-> f[s][k][E][M] */
+static void dropin_pack_f(void) {
+  const size_t chunk = (size_t)TOTAL_NUM_SHELLS * SPEM;
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    memcpy(dropin_f + s * chunk, eParts + s * SSPEM + SPEM, sizeof(double) * chunk);
+}
+
+static void dropin_unpack_f(void) {
+  const size_t chunk = (size_t)TOTAL_NUM_SHELLS * SPEM;
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    memcpy(eParts + s * SSPEM + SPEM, dropin_f + s * chunk, sizeof(double) * chunk);
+}
+
+#define DROPIN_EP_IN                                                                     \
+  (EPREM_NODE_MASK(EPREM_NODE_RX) | EPREM_NODE_MASK(EPREM_NODE_RY) |                    \
+   EPREM_NODE_MASK(EPREM_NODE_RZ) | EPREM_NODE_MASK(EPREM_NODE_RMAG) |                  \
+   EPREM_NODE_MASK(EPREM_NODE_BMAG) | EPREM_NODE_MASK(EPREM_NODE_DLNB) |                \
+   EPREM_NODE_MASK(EPREM_NODE_DLNN) | EPREM_NODE_MASK(EPREM_NODE_DUPAR))
+#define DROPIN_EP_OUT                                                                    \
+  (EPREM_NODE_MASK(EPREM_NODE_DS) | EPREM_NODE_MASK(EPREM_NODE_BMAG_PLUS) |             \
+   EPREM_NODE_MASK(EPREM_NODE_BMAG_MINUS))
+
+void updateEnergeticParticles(void) {
+  dropin_init();
+  double t0 = MPI_Wtime();
+  dropin_pack_f();
+  dropin_pack_nodes(DROPIN_EP_IN);
+  dropin_check(eprem_gpu_upload_f(dropin_run, dropin_f), "upload f");
+  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, DROPIN_EP_IN), "upload nodes");
+  dropin_check(eprem_gpu_update_energetic_particles(dropin_run, t_global),
+               "updateEnergeticParticles");
+  eprem_ep_stats_t st;
+  dropin_check(eprem_gpu_read_stats(dropin_run, &st), "updateEnergeticParticles");
+  dropin_check(eprem_gpu_download_f(dropin_run, dropin_f), "download f");
+  dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, DROPIN_EP_OUT),
+               "download nodes");
+  dropin_unpack_f();
+  dropin_unpack_nodes(DROPIN_EP_OUT);
+  /* the driver's per-step report (src/eprem.c:694-716) */
+  if (st.max_subcycles_change > maxsubcycles_energychange)
+    maxsubcycles_energychange = st.max_subcycles_change;
+  if (st.max_subcycles_focusing > maxsubcycles_focusing)
+    maxsubcycles_focusing = st.max_subcycles_focusing;
+  if (st.min_tau < min_tau) min_tau = st.min_tau;
+  timer_diffusestream += MPI_Wtime() - t0;
+}
+
+void updateMhd(void) {
+  dropin_init();
+  const uint64_t all = EPREM_NODE_MASK_ALL;
+  dropin_pack_nodes(all);
+  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, all), "upload nodes");
+  dropin_check(eprem_gpu_update_mhd(dropin_run, t_global), "updateMhd");
+  dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, all), "download nodes");
+  dropin_unpack_nodes(all);
+}
+
+void moveNodes(Scalar_t dt) {
+  dropin_init();
+  const uint64_t mv = EPREM_NODE_MASK(EPREM_NODE_RX) | EPREM_NODE_MASK(EPREM_NODE_RY) |
+                      EPREM_NODE_MASK(EPREM_NODE_RZ) | EPREM_NODE_MASK(EPREM_NODE_RMAG) |
+                      EPREM_NODE_MASK(EPREM_NODE_VVEC_X) | EPREM_NODE_MASK(EPREM_NODE_VVEC_Y) |
+                      EPREM_NODE_MASK(EPREM_NODE_VVEC_Z) | EPREM_NODE_MASK(EPREM_NODE_ROLD_X) |
+                      EPREM_NODE_MASK(EPREM_NODE_ROLD_Y) | EPREM_NODE_MASK(EPREM_NODE_ROLD_Z);
+  dropin_pack_nodes(mv);
+  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, mv), "upload nodes");
+  dropin_check(eprem_gpu_move_nodes(dropin_run, dt), "moveNodes");
+  dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, mv), "download nodes");
+  dropin_unpack_nodes(mv);
+}

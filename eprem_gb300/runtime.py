@@ -41,6 +41,7 @@ EXPORTS = [
     ("eprem_gpu_kernel_launches", C.c_uint64, [C.c_void_p]),
     ("eprem_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("eprem_gpu_read_kernel_timing", C.c_int, [C.c_void_p, C.POINTER(abi.KernelTime)]),
+    ("eprem_gpu_alu_peak", C.c_int, [C.c_int, DP]),
     ("eprem_gpu_last_error", C.c_char_p, []),
 ]
 
@@ -69,6 +70,16 @@ def load_library(path: str = LIB_PATH):
     if path == LIB_PATH:
         _lib = lib
     return lib
+
+
+def alu_peak_tflops(precision: int) -> float:
+    """Measured FMA throughput (TFLOP/s) of the current GPU."""
+    lib = load_library()
+    out = C.c_double()
+    rc = lib.eprem_gpu_alu_peak(precision, C.byref(out))
+    if rc:
+        raise EpremGpuError(rc, lib.eprem_gpu_last_error().decode())
+    return out.value
 
 
 def _dp(a: np.ndarray):

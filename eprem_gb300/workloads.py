@@ -326,3 +326,26 @@ def initial_f(w: Workload, nodes: np.ndarray, grids) -> np.ndarray:
     f = seed_function(w.params, grids["egrid"][None, None, :], rmag[:, :, None])
     f = f * (1.0 + w.perturb * uniform_pm1(w.seed, S * N * E).reshape(S, N, E))
     return np.ascontiguousarray(np.broadcast_to(f[..., None], (S, N, E, M))).reshape(-1)
+
+
+def fill_initial_f(w: Workload, nodes: np.ndarray, grids, out: np.ndarray,
+                   streams_per_chunk: int = 64) -> np.ndarray:
+    """initial_f written into `out` (length S*N*E*M) stream chunk by stream
+    chunk, so that large workloads need no full-size temporaries."""
+    S, N, E, M = w.num_streams, w.num_nodes, w.num_energies, w.num_mu
+    rmag = nodes[abi.NODE["RMAG"]].reshape(S, N)
+    pert = uniform_pm1(w.seed, S * N * E).reshape(S, N, E)
+    view = out.reshape(S, N, E, M)
+    for s0 in range(0, S, streams_per_chunk):
+        s1 = min(S, s0 + streams_per_chunk)
+        f = seed_function(w.params, grids["egrid"][None, None, :], rmag[s0:s1, :, None])
+        view[s0:s1] = (f * (1.0 + w.perturb * pert[s0:s1]))[..., None]
+    return out
+
+
+
+def with_faces(w: Workload, rows: int, cols: int) -> Workload:
+    """The same per-stream workload on a 6 x rows x cols cube-sphere (fewer or
+    more streams, each with identical node, energy and mu grids)."""
+    return dataclasses.replace(w, rows=rows, cols=cols,
+                               name=f"{w.name} on {6 * rows * cols} streams")

@@ -264,6 +264,11 @@ uint64_t eprem_gpu_kernel_launches(const eprem_gpu_run *run);
 int eprem_gpu_set_kernel_timing(eprem_gpu_run *run, int enable);
 int eprem_gpu_read_kernel_timing(eprem_gpu_run *run, eprem_kernel_time_t *out);
 
+/* FMA throughput of the current GPU in TFLOP/s (EPREM_FP64 or EPREM_FP32),
+ * measured by a short kernel of independent FMA chains: the ALU roofline the
+ * kernels above are held against.  No reference counterpart. */
+int eprem_gpu_alu_peak(int precision, double *tflops);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *eprem_gpu_last_error(void);
 

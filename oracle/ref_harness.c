@@ -42,10 +42,12 @@
 #include "../include/eprem_gpu.h"
 
 /* ---- timers (defined by src/eprem.c:409-423 in the reference binary) ---- */
+#ifndef REF_HARNESS_NO_TIMERS
 double timer_diffusestream, timer_adiabaticfocus, timer_adiabaticchange,
     timer_diffuseshell, timer_driftshell, timer_eptotal, timer_mas_io,
     timer_eprem_io, timer_init, timer_other, timer_wall, timer_start,
     timer_MPIgatherscatter, timer_MPIsendrecv;
+#endif
 
 extern Index_t maxsubcycles_energychange, maxsubcycles_focusing;
 extern Scalar_t min_tau;

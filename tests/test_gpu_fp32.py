@@ -1,0 +1,54 @@
+"""The FP32 form: f and the stencil / scattering arithmetic in float, node
+geometry, dt and CFL in double.  Its omnidirectional flux must stay within
+1e-3 relative of the FP64 result (the metric's accuracy bar), counted over
+(node, energy) with J above 1e-30 of the maximum."""
+import numpy as np
+import pytest
+
+from eprem_gb300 import EpremRun, abi, workloads as W
+
+from helpers import oracle_update, primed_state
+
+pytestmark = pytest.mark.gpu
+
+FLUX_RTOL = 1e-3
+
+
+def flux_err(j, jref):
+    mask = jref > 1e-30 * jref.max()
+    return float(np.max(np.abs(j[mask] - jref[mask]) / jref[mask]))
+
+
+@pytest.mark.parametrize("calls", [1, 3])
+def test_fp32_flux_within_1e3_of_oracle(oracle_lib, calls):
+    w = W.custom(1, 1, 200, 20, 20)  # the small workload's slab shape, 30 sub-steps a call
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes, calls=calls)
+    gs, keep = W.grids_struct(g)
+    j_ref = oracle_lib.omni_flux(d, gs, f_ref)
+    run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    for _ in range(calls):
+        run.update_energetic_particles(0.0)
+    st = run.read_stats()
+    j = run.omni_flux()
+    run.close()
+    assert flux_err(j, j_ref) <= FLUX_RTOL
+    assert st.max_subcycles_focusing > 0
+
+
+def test_fp32_sub_cycle_counts_equal_fp64(oracle_lib):
+    """Sub-cycle counts come from FP64 geometry and CFL in both forms."""
+    w = W.custom(1, 1, 60, 10, 8, num_ep_steps=2)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    _, _, stats = oracle_update(oracle_lib, w, g, f, nodes)
+    run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles(0.0)
+    st = run.read_stats()
+    run.close()
+    assert st.max_substeps_stream == stats[0].max_substeps_stream
+    assert st.stream_cell_subcycles == stats[0].stream_cell_subcycles
+    assert st.max_subcycles_focusing == stats[0].max_subcycles_focusing
