@@ -82,6 +82,7 @@ class Params(C.Structure):
         ("ideal_shock_phi", C.c_double),
         ("ideal_shock_width", C.c_double),
         ("max_subcycles", C.c_int32),
+        ("stream_variant", C.c_int32),
     ]
 
 

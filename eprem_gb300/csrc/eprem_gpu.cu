@@ -196,8 +196,12 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   r->params = *params;
   r->m0 = m0;
   if (r->params.max_subcycles <= 0) r->params.max_subcycles = 1000000;
-  if (plan_stream(dims->precision, N, M, &r->splan) ||
-      plan_node(dims->precision, E, M, &r->nplan)) {
+  const bool fast32 = dims->precision == EPREM_FP32 && params->adiabatic_focus_alg == 1 &&
+                      params->adiabatic_change_alg == 1;
+  int prc = plan_stream(dims->precision, N, M, params->stream_variant, &r->splan);
+  if (!prc) prc = fast32 ? plan_node32(E, M, &r->nplan) : plan_node(dims->precision, E, M, &r->nplan);
+  r->nplan.fast32 = fast32 ? 1 : 0;
+  if (prc) {
     delete r;
     return fail(EPREM_GPU_ERR_ARG, "sizes exceed the supported kernel shapes "
                                    "(num_nodes per stream or E*M too large)");
@@ -419,8 +423,10 @@ extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_g
                  [&] { return launch_seed_check(r->v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "streaming launch");
     if (r->v.use_focus || r->v.use_change) {
-      rc = timed(r, EPREM_KERNEL_NODE,
-                 [&] { return launch_node(r->v, r->nplan, r->stream, &r->launches); });
+      rc = timed(r, EPREM_KERNEL_NODE, [&] {
+        return r->nplan.fast32 ? launch_node32(r->v, r->nplan, r->stream, &r->launches)
+                               : launch_node(r->v, r->nplan, r->stream, &r->launches);
+      });
       if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
     }
   }

@@ -17,8 +17,9 @@ struct StreamPlan {
   int mmax;      // register slots per thread (>= M)
   int threads;   // threads per CTA
   int cluster;   // CTAs per (stream, energy) slab
+  int reg_coef;  // upwind coefficients in registers (1) or shared memory (0)
 };
-int plan_stream(int precision, int N, int M, StreamPlan *plan);
+int plan_stream(int precision, int N, int M, int variant, StreamPlan *plan);
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches);
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
@@ -29,9 +30,13 @@ struct NodePlan {
   int threads;     // threads per CTA
   int nodes;       // nodes per CTA
   size_t smem;     // dynamic shared memory bytes
+  int fast32;      // FP32 form with Euler operators: node32.cu
 };
 int plan_node(int precision, int E, int M, NodePlan *plan);
 int launch_node(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_t *launches);
+// node32.cu -- FP32-form focusing + change (Euler operators)
+int plan_node32(int E, int M, NodePlan *plan);
+int launch_node32(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_t *launches);
 
 // mhd.cu -- updateMhd (analytic), moveNodes, omnidirectional flux, f conversion
 struct MhdParams {

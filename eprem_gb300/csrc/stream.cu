@@ -1,17 +1,24 @@
 // stream.cu -- streaming along each stream with isotropisation (K1).
 //
 // Restates DiffuseStreamData (src/energeticParticles.c:2240-2490) for one
-// (stream, energy) slab per thread-block cluster:
-//   * thread i of the cluster owns list node i (GetStreamList order) and keeps
-//     all of that node's mu cells in registers for every sub-cycle;
+// (stream, energy) slab per CTA or thread-block cluster:
+//   * thread i owns list node i (GetStreamList order) and keeps that node's mu
+//     cells in registers for all of the slab's sub-cycles;
 //   * the upwind neighbour (list node i-1 for mu >= 0, i+1 for mu < 0) comes
-//     from a warp shuffle; at warp edges from a small shared-memory edge
-//     buffer, and at CTA edges from the neighbouring CTA's edge buffer through
-//     distributed shared memory -- one cluster barrier per sub-cycle;
+//     from a warp shuffle; lanes at warp edges read a halo slot in their own
+//     CTA's shared memory, which the neighbouring warp -- or, across a CTA
+//     edge, the neighbouring CTA of the cluster, by a distributed-shared-memory
+//     store -- fills before the sub-cycle's barrier.  The inner loop therefore
+//     only ever loads from local shared memory;
 //   * the isotropisation mean over mu is a register sum in the owning thread.
+// The upwind coefficients mult*del_fac are fixed for the slab: the FP32 form
+// keeps them in registers, the FP64 form (bound by the FP64 pipe, next to
+// which shared-memory loads cost nothing) in shared memory.  A second FP32
+// shape keeps them in shared memory so that 1024 threads -- a whole 1000-node
+// stream -- fit one CTA without a cluster.
 // seedPopulationCheck (src/energeticParticlesBoundary.c:28-59) is applied as
-// the slab is loaded; the thinned-out nodes receive their reference node's
-// values on write-back, as the reference's shellRef copy does (:2448-2455).
+// the slab is loaded; thinned-out nodes receive their reference node's values
+// on write-back, as the reference's shellRef copy does (:2448-2455).
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -21,33 +28,60 @@ namespace cg = cooperative_groups;
 
 namespace eprem {
 
-template <typename Real, int MMAX> struct StreamShape;
-// Threads per CTA so that MMAX register slots per thread fit the SM's 64 K
-// registers with one CTA per SM.
-#define EPREM_STREAM_SHAPE(R, MM, TT) \
-  template <> struct StreamShape<R, MM> { static constexpr int T = TT; };
-EPREM_STREAM_SHAPE(double, 8, 1024)
-EPREM_STREAM_SHAPE(double, 16, 768)
-EPREM_STREAM_SHAPE(double, 24, 640)
-EPREM_STREAM_SHAPE(double, 32, 512)
-EPREM_STREAM_SHAPE(double, 40, 512)
-EPREM_STREAM_SHAPE(double, 48, 384)
-EPREM_STREAM_SHAPE(double, 64, 256)
-EPREM_STREAM_SHAPE(float, 8, 1024)
-EPREM_STREAM_SHAPE(float, 16, 1024)
-EPREM_STREAM_SHAPE(float, 24, 1024)
-EPREM_STREAM_SHAPE(float, 32, 768)
-EPREM_STREAM_SHAPE(float, 40, 768)
-EPREM_STREAM_SHAPE(float, 48, 640)
-EPREM_STREAM_SHAPE(float, 64, 512)
+// Threads per CTA (multiples of 128, the register-allocation granule) for
+// register-held coefficients (FP32) and shared-memory coefficients.
+template <typename Real, int MMAX, bool RegCoef> struct StreamShape;
+#define EPREM_STREAM_SHAPE(R, MM, RC, TT) \
+  template <> struct StreamShape<R, MM, RC> { static constexpr int T = TT; };
+EPREM_STREAM_SHAPE(double, 8, false, 1024)
+EPREM_STREAM_SHAPE(double, 16, false, 768)
+EPREM_STREAM_SHAPE(double, 24, false, 512)
+EPREM_STREAM_SHAPE(double, 32, false, 512)
+EPREM_STREAM_SHAPE(double, 40, false, 512)
+EPREM_STREAM_SHAPE(double, 48, false, 384)
+EPREM_STREAM_SHAPE(double, 64, false, 384)
+EPREM_STREAM_SHAPE(float, 8, true, 1024)
+EPREM_STREAM_SHAPE(float, 16, true, 768)
+EPREM_STREAM_SHAPE(float, 24, true, 512)
+EPREM_STREAM_SHAPE(float, 32, true, 512)
+EPREM_STREAM_SHAPE(float, 40, true, 512)
+EPREM_STREAM_SHAPE(float, 48, true, 384)
+EPREM_STREAM_SHAPE(float, 64, true, 384)
+EPREM_STREAM_SHAPE(float, 8, false, 1024)
+EPREM_STREAM_SHAPE(float, 16, false, 1024)
+EPREM_STREAM_SHAPE(float, 24, false, 1024)
+EPREM_STREAM_SHAPE(float, 32, false, 1024)
+EPREM_STREAM_SHAPE(float, 40, false, 1024)
+EPREM_STREAM_SHAPE(float, 48, false, 768)
+EPREM_STREAM_SHAPE(float, 64, false, 512)
 #undef EPREM_STREAM_SHAPE
 
-template <typename Real, int MMAX, int T>
-__global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
+// Shared memory of one CTA: coefficient table (shared-coefficient shapes) and
+// the halo slots.
+template <typename Real, int MMAX, bool RegCoef>
+constexpr size_t stream_smem_bytes() {
+  constexpr int T = StreamShape<Real, MMAX, RegCoef>::T;
+  constexpr int W = T / 32;
+  return (RegCoef ? 0 : sizeof(Real) * MMAX * T) + sizeof(Real) * 2 * 2 * (W + 1) * MMAX;
+}
+
+template <typename Real, int MMAX, bool RegCoef>
+__global__ void __launch_bounds__((StreamShape<Real, MMAX, RegCoef>::T), 1)
+    k_stream(RunView r, int m0) {
+  constexpr int T = StreamShape<Real, MMAX, RegCoef>::T;
   constexpr int W = T / 32;
   constexpr unsigned FULL = 0xffffffffu;
-  __shared__ Real edge[2 * 2 * W * MMAX];  // [parity][hi=lane31 / lo=lane0][warp][mu]
-  __shared__ Real del_s[MMAX];
+  // halo slots, double-buffered by sub-cycle parity p:
+  //   hi[p][w][mu], w = 0..W : slot w+1 holds lane 31 of warp w; slot 0 the
+  //                            previous CTA's last lane (written remotely);
+  //   lo[p][w][mu], w = 0..W : slot w holds lane 0 of warp w; slot W the next
+  //                            CTA's first lane (written remotely).
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  Real *coef = reinterpret_cast<Real *>(sm_raw);  // [mu][T], shared-coefficient shapes
+  Real *halo = coef + (RegCoef ? 0 : MMAX * T);
+  auto hi = [&](int p, int w) { return halo + ((p * 2 + 0) * (W + 1) + w) * MMAX; };
+  auto lo = [&](int p, int w) { return halo + ((p * 2 + 1) * (W + 1) + w) * MMAX; };
+
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int crank = (int)cluster.block_rank();
@@ -72,16 +106,20 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
     atomicMax(&r.status->max_stream, nsteps);
     atomicAdd(&r.status->stream_cs, (unsigned long long)nsteps * L * M);
   }
-  for (int mu = tid; mu < M; mu += T) del_s[mu] = (Real)(ec.vgrid * dtProp * r.mugrid[mu]);
+  // zero the halo slots: the ones no neighbour writes stay zero (finite)
+  for (int j = tid; j < 2 * 2 * (W + 1) * MMAX; j += T) halo[j] = (Real)0;
 
   const int i = crank * T + tid;
   const bool active = i < L;
-  const bool first = (i == 0), last = (i == L - 1);
   const size_t sN = (size_t)s * N;
-  Real fr[MMAX];
+  Real fr[MMAX], cf[RegCoef ? MMAX : 1];
 #pragma unroll
-  for (int mu = 0; mu < MMAX; ++mu) fr[mu] = (Real)0;
-  double mult = 0.0, emt = 0.0;
+  for (int mu = 0; mu < MMAX; ++mu) {
+    fr[mu] = (Real)0;
+    if (RegCoef) cf[mu] = (Real)0;
+    else if (mu < M) coef[mu * T + tid] = (Real)0;
+  }
+  double emt = 0.0;
   Real bcv = (Real)0;
   bool bc_node = false;
   int k = 0;
@@ -90,7 +128,7 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
     const size_t gidx = sN + k;
     const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
     const double dsi = r.ds_i[sN + i];
-    mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
+    const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
     emt = exp(-dtProp / tau);
     const double seedv = seed_value(r, ec, r.seed_radial[gidx]);
     const Real *fp = reinterpret_cast<const Real *>(r.f) + (gidx * r.E + e) * M;
@@ -100,6 +138,16 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
         Real v = fp[mu];
         if (r.check_seed && (double)v < seedv) v = to_real<Real>(seedv);
         fr[mu] = v;
+        // upwind coefficient mult * del_fac (src/energeticParticles.c:2346, :2386);
+        // zero where the reference copies the cell unchanged (the first list
+        // node for mu >= 0, the last for mu < 0, :2381 and :2393)
+        const bool edge_cell = (mu >= m0) ? (i == 0) : (i == L - 1);
+        const double del_fac = ec.vgrid * dtProp * r.mugrid[mu];
+        const Real c = edge_cell ? (Real)0 : (Real)(mult * del_fac);
+        if (RegCoef)
+          cf[mu] = c;
+        else
+          coef[mu * T + tid] = c;
       }
     }
     if (r.use_bc && i < 3) {
@@ -107,59 +155,65 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
       bcv = to_real<Real>(seedv);
     }
   }
-  const Real c_mult = (Real)mult;
   const Real c_emt = (Real)emt;
   const Real c_omemt = (Real)(1.0 - emt);
   const Real inv_m = (Real)(1.0 / M);
-  const Real *prev_edge = crank > 0 ? cluster.map_shared_rank(edge, crank - 1) : nullptr;
-  const Real *next_edge = crank < C - 1 ? cluster.map_shared_rank(edge, crank + 1) : nullptr;
-  __syncthreads();
+  // remote halo slots this CTA fills in its neighbours
+  Real *next_hi0 = (C > 1 && crank < C - 1) ? cluster.map_shared_rank(halo, crank + 1) : nullptr;
+  Real *prev_loW = (C > 1 && crank > 0) ? cluster.map_shared_rank(halo, crank - 1) : nullptr;
+  if (C > 1)
+    cluster.sync();  // halo zeroing above is complete before any remote store lands
+  else
+    __syncthreads();
 
   for (int step = 0; step < nsteps; ++step) {
     const int p = step & 1;
-    Real *ep = edge + p * 2 * W * MMAX;
     if (bc_node) {
 #pragma unroll
       for (int mu = 0; mu < MMAX; ++mu) fr[mu] = bcv;
     }
     if (lane == 31) {
+      Real *dst = hi(p, warp + 1);
+      Real *rdst = (warp == W - 1 && next_hi0)
+                       ? next_hi0 + ((p * 2 + 0) * (W + 1) + 0) * MMAX : nullptr;
 #pragma unroll
       for (int mu = 0; mu < MMAX; ++mu)
-        if (mu < M) ep[warp * MMAX + mu] = fr[mu];
+        if (mu < M) {
+          dst[mu] = fr[mu];
+          if (rdst) rdst[mu] = fr[mu];
+        }
     }
     if (lane == 0) {
+      Real *dst = lo(p, warp);
+      Real *rdst = (warp == 0 && prev_loW)
+                       ? prev_loW + ((p * 2 + 1) * (W + 1) + W) * MMAX : nullptr;
 #pragma unroll
       for (int mu = 0; mu < MMAX; ++mu)
-        if (mu < M) ep[(W + warp) * MMAX + mu] = fr[mu];
+        if (mu < M) {
+          dst[mu] = fr[mu];
+          if (rdst) rdst[mu] = fr[mu];
+        }
     }
     if (C > 1)
       cluster.sync();
     else
       __syncthreads();
+    const Real *my_hi = hi(p, warp);      // lane 31 of warp-1 / previous CTA
+    const Real *my_lo = lo(p, warp + 1);  // lane 0 of warp+1 / next CTA
     Real acc = (Real)0;
 #pragma unroll
     for (int mu = 0; mu < MMAX; ++mu) {
       if (mu < M) {
-        const Real c = c_mult * del_s[mu];
+        const Real c = RegCoef ? cf[mu] : coef[mu * T + tid];
         Real fn;
         if (mu >= m0) {  // mugrid[mu] >= 0: upwind from list node i-1
           Real nb = __shfl_up_sync(FULL, fr[mu], 1);
-          if (lane == 0) {
-            if (warp > 0)
-              nb = ep[(warp - 1) * MMAX + mu];
-            else if (prev_edge)
-              nb = prev_edge[p * 2 * W * MMAX + (W - 1) * MMAX + mu];
-          }
-          fn = first ? fr[mu] : fr[mu] + c * (nb - fr[mu]);
+          if (lane == 0) nb = my_hi[mu];
+          fn = fr[mu] + c * (nb - fr[mu]);
         } else {  // mu < 0: upwind from list node i+1
           Real nb = __shfl_down_sync(FULL, fr[mu], 1);
-          if (lane == 31) {
-            if (warp < W - 1)
-              nb = ep[(W + warp + 1) * MMAX + mu];
-            else if (next_edge)
-              nb = next_edge[p * 2 * W * MMAX + W * MMAX + mu];
-          }
-          fn = last ? fr[mu] : fr[mu] + c * (fr[mu] - nb);
+          if (lane == 31) nb = my_lo[mu];
+          fn = fr[mu] + c * (fr[mu] - nb);
         }
         fr[mu] = fn;
         acc += fn;
@@ -184,7 +238,7 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
       }
     }
     // node k and the thinned nodes that reference it (previous list node + 1 .. k)
-    const int kfirst = first ? 0 : r.list[sN + i - 1] + 1;
+    const int kfirst = (i == 0) ? 0 : r.list[sN + i - 1] + 1;
     for (int kk = kfirst; kk <= k; ++kk) {
       Real *op = reinterpret_cast<Real *>(r.f) + ((sN + kk) * r.E + e) * M;
 #pragma unroll
@@ -192,7 +246,7 @@ __global__ void __launch_bounds__(T, 1) k_stream(RunView r, int m0) {
         if (mu < M) op[mu] = fr[mu];
     }
   }
-  if (C > 1) cluster.sync();  // neighbours may still read this CTA's edge buffer
+  if (C > 1) cluster.sync();  // no CTA leaves while a neighbour may still store into it
 }
 
 // seedPopulationCheck alone, for runs without parallel diffusion.
@@ -212,48 +266,60 @@ __global__ void k_seed_check(RunView r) {
 
 static const int kStreamBins[] = {8, 16, 24, 32, 40, 48, 64};
 
-static int stream_threads(int precision, int mmax) {
-  if (precision == EPREM_FP64) {
-    switch (mmax) {
-      case 8: return StreamShape<double, 8>::T;
-      case 16: return StreamShape<double, 16>::T;
-      case 24: return StreamShape<double, 24>::T;
-      case 32: return StreamShape<double, 32>::T;
-      case 40: return StreamShape<double, 40>::T;
-      case 48: return StreamShape<double, 48>::T;
-      default: return StreamShape<double, 64>::T;
-    }
-  }
+template <typename Real, bool RC>
+static int threads_for(int mmax) {
   switch (mmax) {
-    case 8: return StreamShape<float, 8>::T;
-    case 16: return StreamShape<float, 16>::T;
-    case 24: return StreamShape<float, 24>::T;
-    case 32: return StreamShape<float, 32>::T;
-    case 40: return StreamShape<float, 40>::T;
-    case 48: return StreamShape<float, 48>::T;
-    default: return StreamShape<float, 64>::T;
+    case 8: return StreamShape<Real, 8, RC>::T;
+    case 16: return StreamShape<Real, 16, RC>::T;
+    case 24: return StreamShape<Real, 24, RC>::T;
+    case 32: return StreamShape<Real, 32, RC>::T;
+    case 40: return StreamShape<Real, 40, RC>::T;
+    case 48: return StreamShape<Real, 48, RC>::T;
+    default: return StreamShape<Real, 64, RC>::T;
   }
 }
 
-int plan_stream(int precision, int N, int M, StreamPlan *plan) {
+// variant: 0 automatic, 1 coefficients in registers, 2 in shared memory.
+// The FP64 form always keeps them in shared memory.  Automatic FP32 choice:
+// one CTA per slab when the shared-coefficient shape holds the whole stream,
+// else registers and a cluster.
+int plan_stream(int precision, int N, int M, int variant, StreamPlan *plan) {
   int mmax = 0;
   for (int b : kStreamBins)
     if (M <= b) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
   plan->mmax = mmax;
-  plan->threads = stream_threads(precision, mmax);
+  bool reg;
+  if (precision == EPREM_FP64) {
+    reg = false;
+  } else if (variant == 1) {
+    reg = true;
+  } else if (variant == 2) {
+    reg = false;
+  } else {
+    reg = N > threads_for<float, false>(mmax);
+  }
+  plan->reg_coef = reg ? 1 : 0;
+  plan->threads = precision == EPREM_FP64 ? threads_for<double, false>(mmax)
+                  : reg                   ? threads_for<float, true>(mmax)
+                                          : threads_for<float, false>(mmax);
   plan->cluster = (N + plan->threads - 1) / plan->threads;
   if (plan->cluster > 8) return EPREM_GPU_ERR_ARG;  // portable cluster limit
   return 0;
 }
 
-template <typename Real, int MMAX>
+template <typename Real, int MMAX, bool RC>
 static cudaError_t launch_stream_t(const RunView &r, int cluster, int m0, cudaStream_t st) {
-  constexpr int T = StreamShape<Real, MMAX>::T;
+  constexpr int T = StreamShape<Real, MMAX, RC>::T;
+  constexpr size_t dyn = stream_smem_bytes<Real, MMAX, RC>();
+  auto kern = k_stream<Real, MMAX, RC>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = dyn;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -262,27 +328,32 @@ static cudaError_t launch_stream_t(const RunView &r, int cluster, int m0, cudaSt
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_stream<Real, MMAX, T>, r, m0);
+  return cudaLaunchKernelEx(&cfg, kern, r, m0);
 }
 
-template <typename Real>
-static cudaError_t dispatch_stream(const RunView &r, const StreamPlan &pl, int m0,
-                                   cudaStream_t st) {
+template <typename Real, bool RC>
+static cudaError_t dispatch_mmax(const RunView &r, const StreamPlan &pl, int m0,
+                                 cudaStream_t st) {
   switch (pl.mmax) {
-    case 8: return launch_stream_t<Real, 8>(r, pl.cluster, m0, st);
-    case 16: return launch_stream_t<Real, 16>(r, pl.cluster, m0, st);
-    case 24: return launch_stream_t<Real, 24>(r, pl.cluster, m0, st);
-    case 32: return launch_stream_t<Real, 32>(r, pl.cluster, m0, st);
-    case 40: return launch_stream_t<Real, 40>(r, pl.cluster, m0, st);
-    case 48: return launch_stream_t<Real, 48>(r, pl.cluster, m0, st);
-    default: return launch_stream_t<Real, 64>(r, pl.cluster, m0, st);
+    case 8: return launch_stream_t<Real, 8, RC>(r, pl.cluster, m0, st);
+    case 16: return launch_stream_t<Real, 16, RC>(r, pl.cluster, m0, st);
+    case 24: return launch_stream_t<Real, 24, RC>(r, pl.cluster, m0, st);
+    case 32: return launch_stream_t<Real, 32, RC>(r, pl.cluster, m0, st);
+    case 40: return launch_stream_t<Real, 40, RC>(r, pl.cluster, m0, st);
+    case 48: return launch_stream_t<Real, 48, RC>(r, pl.cluster, m0, st);
+    default: return launch_stream_t<Real, 64, RC>(r, pl.cluster, m0, st);
   }
 }
 
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches) {
-  cudaError_t err = r.precision == EPREM_FP64 ? dispatch_stream<double>(r, plan, m0, st)
-                                              : dispatch_stream<float>(r, plan, m0, st);
+  cudaError_t err;
+  if (r.precision == EPREM_FP64)
+    err = dispatch_mmax<double, false>(r, plan, m0, st);
+  else if (plan.reg_coef)
+    err = dispatch_mmax<float, true>(r, plan, m0, st);
+  else
+    err = dispatch_mmax<float, false>(r, plan, m0, st);
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

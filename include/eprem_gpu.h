@@ -121,6 +121,11 @@ typedef struct {
   int32_t max_subcycles;            /* cap on any sub-cycle count; above it the
                                        update stops with ERR_SUBCYCLES (0 means
                                        1,000,000).  The reference has no cap. */
+  int32_t stream_variant;           /* streaming-kernel shape (tuning, no effect
+                                       on results): 0 automatic, 1 upwind
+                                       coefficients in registers (thread-block
+                                       clusters for long streams), 2 coefficients
+                                       in shared memory (one CTA per slab)     */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids

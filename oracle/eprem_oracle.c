@@ -1080,6 +1080,7 @@ int orc_abi_layout(long *out, int cap) {
   OFF(eprem_params_t, ideal_shock_speed); OFF(eprem_params_t, ideal_shock_init_time);
   OFF(eprem_params_t, ideal_shock_theta); OFF(eprem_params_t, ideal_shock_phi);
   OFF(eprem_params_t, ideal_shock_width); OFF(eprem_params_t, max_subcycles);
+  OFF(eprem_params_t, stream_variant);
   OFF(eprem_grids_t, egrid); OFF(eprem_grids_t, vgrid); OFF(eprem_grids_t, vgrid_i);
   OFF(eprem_grids_t, mugrid); OFF(eprem_grids_t, rigidity); OFF(eprem_grids_t, dlnp);
   OFF(eprem_grids_t, dmu);

@@ -25,7 +25,9 @@ def test_nan_in_distribution_is_reported(oracle_lib):
     w = W.custom(1, 1, 30, 8, 6, num_ep_steps=2)
     run, d, g, f, nodes = _run(w, oracle_lib)
     bad = f.copy()
-    bad[len(bad) // 2] = np.nan
+    # stream 1, node 15, energy 3, mu 2: an interior node (the first three
+    # list nodes are reset to the seed every sub-cycle, which would erase it)
+    bad[((1 * 30 + 15) * 8 + 3) * 6 + 2] = np.nan
     run.upload_f(bad)
     run.update_energetic_particles(0.0)
     with pytest.raises(EpremGpuError) as ei:
