@@ -152,3 +152,27 @@ def node_mask(*names):
 # The node fields the energetic-particle update reads and writes.
 EP_INPUT_MASK = node_mask("RX", "RY", "RZ", "RMAG", "BMAG", "DLNB", "DLNN", "DUPAR")
 EP_OUTPUT_MASK = node_mask("DS", "BMAG_PLUS", "BMAG_MINUS")
+
+
+# MAS coupling (include/eprem_gpu.h): Bp, Bt, Br, Vp, Vt, Vr, rho
+MAS_NFIELDS = 7
+MAS_FIELDS = ["Bp", "Bt", "Br", "Vp", "Vt", "Vr", "rho"]
+
+
+class MasSlice(C.Structure):
+    _fields_ = [
+        ("dims", (C.c_int32 * 3) * MAS_NFIELDS),
+        ("mesh", (C.POINTER(C.c_float) * 3) * MAS_NFIELDS),
+        ("data", C.POINTER(C.c_float) * MAS_NFIELDS),
+    ]
+
+
+class MasParams(C.Structure):
+    _fields_ = [
+        ("radial_max", C.c_double),
+        ("v_min", C.c_double),
+        ("cor_rotate_fake", C.c_int32),
+        ("rotate_solution", C.c_int32),
+        ("max_slices", C.c_int32),
+        ("pad", C.c_int32),
+    ]

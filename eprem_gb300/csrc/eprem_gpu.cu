@@ -67,6 +67,12 @@ struct eprem_gpu_run {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, int>> ev_pending;  // (kind, index of start event)
   size_t ev_used = 0;
+  // MAS background: device copies of the loaded time slices
+  bool mas_on = false, mas_selected = false;
+  std::vector<std::vector<void *>> mas_allocs;
+  std::vector<MasSlotDev> mas_slots;
+  std::vector<char> mas_loaded;
+  MasView mv{};
   size_t cells() const {
     return (size_t)dims.num_streams * dims.num_nodes * dims.num_energies * dims.num_mu;
   }
@@ -198,7 +204,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   if (r->params.max_subcycles <= 0) r->params.max_subcycles = 1000000;
   const bool fast32 = dims->precision == EPREM_FP32 && params->adiabatic_focus_alg == 1 &&
                       params->adiabatic_change_alg == 1;
-  int prc = plan_stream(dims->precision, N, M, params->stream_variant, &r->splan);
+  int prc = plan_stream(dims->precision, N, M, m0, params->stream_variant, &r->splan);
   if (!prc) prc = fast32 ? plan_node32(E, M, &r->nplan) : plan_node(dims->precision, E, M, &r->nplan);
   r->nplan.fast32 = fast32 ? 1 : 0;
   if (prc) {
@@ -323,6 +329,8 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_stage);
   cudaFree(r->d_flux);
   for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
+  for (auto &slot : r->mas_allocs)
+    for (void *p : slot) cudaFree(p);
   if (r->h_status) cudaFreeHost(r->h_status);
   if (r->stream) cudaStreamDestroy(r->stream);
   delete r;
@@ -440,9 +448,96 @@ extern "C" int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *stats) {
 
 extern "C" int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (r->mas_on) {
+    if (!r->mas_selected)
+      return fail(EPREM_GPU_ERR_STATE, "MAS background: no time slices selected");
+    if (timed(r, EPREM_KERNEL_MHD, [&] {
+          return launch_mas_update_mhd(r->v, r->mv, r->params.t_del, r->stream, &r->launches);
+        }))
+      return cuda_fail(cudaGetLastError(), "updateMhd (MAS) launch");
+    return EPREM_GPU_OK;
+  }
   if (timed(r, EPREM_KERNEL_MHD,
             [&] { return launch_update_mhd(r->v, r->mhd, t_global, r->stream, &r->launches); }))
     return cuda_fail(cudaGetLastError(), "updateMhd launch");
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp) {
+  if (!r || !mp) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  if (mp->max_slices < 2 || mp->max_slices > 4096)
+    return fail(EPREM_GPU_ERR_ARG, "max_slices must be 2..4096");
+  r->mas_on = true;
+  r->mas_selected = false;
+  r->mas_allocs.assign(mp->max_slices, {});
+  r->mas_slots.assign(mp->max_slices, MasSlotDev{});
+  r->mas_loaded.assign(mp->max_slices, 0);
+  r->mv.radial_max = mp->radial_max;
+  r->mv.v_min = mp->v_min;
+  r->mv.cor_rotate_fake = mp->cor_rotate_fake;
+  r->mv.rotate_solution = mp->rotate_solution;
+  r->mv.r_scale = r->params.r_scale;
+  r->mv.omega_sun = r->params.omega_sun;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_mas_load_slice(eprem_gpu_run *r, int slot, const eprem_mas_slice_t *s) {
+  if (!r || !s) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  if (!r->mas_on) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
+  if (slot < 0 || slot >= (int)r->mas_slots.size()) return fail(EPREM_GPU_ERR_ARG, "slot out of range");
+  CK(cudaStreamSynchronize(r->stream));
+  for (void *p : r->mas_allocs[slot]) cudaFree(p);
+  r->mas_allocs[slot].clear();
+  r->mas_loaded[slot] = 0;
+  MasSlotDev dev{};
+  for (int f = 0; f < EPREM_MAS_NFIELDS; f++) {
+    size_t n = 1;
+    for (int a = 0; a < 3; a++) {
+      const int d = s->dims[f][a];
+      if (d < 2 || !s->mesh[f][a]) return fail(EPREM_GPU_ERR_ARG, "MAS meshes need >= 2 points");
+      n *= (size_t)d;
+      float *m = nullptr;
+      CK(cudaMalloc(&m, d * sizeof(float)));
+      r->mas_allocs[slot].push_back(m);
+      CK(cudaMemcpy(m, s->mesh[f][a], d * sizeof(float), cudaMemcpyHostToDevice));
+      dev.mesh[f][a] = m;
+      dev.dims[f][a] = d;
+    }
+    if (!s->data[f]) return fail(EPREM_GPU_ERR_ARG, "null MAS field");
+    float *v = nullptr;
+    CK(cudaMalloc(&v, n * sizeof(float)));
+    r->mas_allocs[slot].push_back(v);
+    CK(cudaMemcpy(v, s->data[f], n * sizeof(float), cudaMemcpyHostToDevice));
+    dev.data[f] = v;
+  }
+  r->mas_slots[slot] = dev;
+  r->mas_loaded[slot] = 1;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_mas_select(eprem_gpu_run *r, int slot0, int slot1, double s_cor,
+                                    double phi_offset) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (!r->mas_on) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
+  const int n = (int)r->mas_slots.size();
+  if (slot0 < 0 || slot0 >= n || slot1 < 0 || slot1 >= n || !r->mas_loaded[slot0] ||
+      !r->mas_loaded[slot1])
+    return fail(EPREM_GPU_ERR_ARG, "MAS slot not loaded");
+  r->mv.s0 = r->mas_slots[slot0];
+  r->mv.s1 = r->mas_slots[slot1];
+  r->mv.s_cor = s_cor;
+  r->mv.phi_offset = phi_offset;
+  r->mas_selected = true;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_mas_move_nodes(eprem_gpu_run *r, double dt) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (!r->mas_on || !r->mas_selected)
+    return fail(EPREM_GPU_ERR_STATE, "MAS background not initialised or no slices selected");
+  if (timed(r, EPREM_KERNEL_MOVE,
+            [&] { return launch_mas_move_nodes(r->v, r->mv, dt, r->stream, &r->launches); }))
+    return cuda_fail(cudaGetLastError(), "masMoveNodes launch");
   return EPREM_GPU_OK;
 }
 

@@ -17,12 +17,16 @@ struct StreamPlan {
   int mmax;      // register slots per thread (>= M)
   int threads;   // threads per CTA
   int cluster;   // CTAs per (stream, energy) slab
-  int reg_coef;  // upwind coefficients in registers (1) or shared memory (0)
+  int reg_coef;  // coefficients in registers (1), shared memory (0); 2: stream2.cu
 };
-int plan_stream(int precision, int N, int M, int variant, StreamPlan *plan);
+int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan);
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches);
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
+// stream2.cu -- FP32 streaming, two list nodes per thread (plan.reg_coef == 2)
+int plan_stream2(int N, int M, int m0, StreamPlan *plan);
+int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
+                   uint64_t *launches);
 
 // node.cu -- AdiabaticFocusing + AdiabaticChange
 struct NodePlan {
@@ -50,5 +54,21 @@ int launch_move_nodes(const RunView &r, double dt, cudaStream_t st, uint64_t *la
 int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *launches);
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
                      size_t count, cudaStream_t st, uint64_t *launches);
+
+// mas.cu -- MAS background (updateMhd MHD_MAS branch, masMoveNodes)
+struct MasSlotDev {
+  const float *data[EPREM_MAS_NFIELDS];
+  const float *mesh[EPREM_MAS_NFIELDS][3];
+  int dims[EPREM_MAS_NFIELDS][3];
+};
+struct MasView {
+  MasSlotDev s0, s1;
+  double s_cor, phi_offset, radial_max, v_min, r_scale, omega_sun;
+  int cor_rotate_fake, rotate_solution;
+};
+int launch_mas_update_mhd(const RunView &r, const MasView &mv, double t_del, cudaStream_t st,
+                          uint64_t *launches);
+int launch_mas_move_nodes(const RunView &r, const MasView &mv, double dt, cudaStream_t st,
+                          uint64_t *launches);
 
 }  // namespace eprem

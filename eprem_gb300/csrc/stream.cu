@@ -279,11 +279,12 @@ static int threads_for(int mmax) {
   }
 }
 
-// variant: 0 automatic, 1 coefficients in registers, 2 in shared memory.
-// The FP64 form always keeps them in shared memory.  Automatic FP32 choice:
-// one CTA per slab when the shared-coefficient shape holds the whole stream,
-// else registers and a cluster.
-int plan_stream(int precision, int N, int M, int variant, StreamPlan *plan) {
+// variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
+// 3 two list nodes per thread (stream2.cu).  The FP64 form always keeps the
+// coefficients in shared memory; the automatic FP32 choice is variant 3.
+int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
+  if (precision == EPREM_FP32 && (variant == 0 || variant == 3) && plan_stream2(N, M, m0, plan) == 0)
+    return 0;
   int mmax = 0;
   for (int b : kStreamBins)
     if (M <= b) { mmax = b; break; }
@@ -297,7 +298,7 @@ int plan_stream(int precision, int N, int M, int variant, StreamPlan *plan) {
   } else if (variant == 2) {
     reg = false;
   } else {
-    reg = N > threads_for<float, false>(mmax);
+    reg = N > threads_for<float, false>(mmax);  // unreachable: variant 0 goes to stream2
   }
   plan->reg_coef = reg ? 1 : 0;
   plan->threads = precision == EPREM_FP64 ? threads_for<double, false>(mmax)
@@ -347,6 +348,7 @@ static cudaError_t dispatch_mmax(const RunView &r, const StreamPlan &pl, int m0,
 
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches) {
+  if (plan.reg_coef == 2) return launch_stream2(r, plan, m0, st, launches);
   cudaError_t err;
   if (r.precision == EPREM_FP64)
     err = dispatch_mmax<double, false>(r, plan, m0, st);

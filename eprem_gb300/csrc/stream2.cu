@@ -1,0 +1,317 @@
+// stream2.cu -- streaming in the FP32 form with several list nodes per thread.
+//
+// DiffuseStreamData (src/energeticParticles.c:2240-2490) as in stream.cu, but
+// shaped for the FP32 pipe, where the per-cell cost of shuffles and shared-
+// memory loads, not arithmetic, limited the one-node-per-thread kernel:
+//   * thread i owns NPT consecutive list nodes; inside the thread a node's
+//     upwind neighbour is the next register array, across threads one shuffle
+//     serves NPT cells;
+//   * the upwind coefficient mult*del_fac is formed per cell from the node's
+//     mult (register) and del_fac(mu) = v dtProp mugrid(mu), evaluated from
+//     the uniform mu grid (mugrid = -1 + (mu + 1/2) dmu) -- no per-cell load;
+//   * a thread keeps each node's cells in two register halves, mu < 0 and
+//     mu >= 0 (the mu grid is increasing, so the split is one index m0); each
+//     half has its own loop, so the upwind direction is never a branch;
+//   * warp-edge lanes publish only the half their neighbour needs (lane 31's
+//     last node for mu >= 0, lane 0's first node for mu < 0).
+// A CTA of T threads holds NPT*T >= 1024 nodes for mu bins up to 48, so a
+// 1000-node stream fits one CTA.
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace eprem {
+
+// Threads per CTA and list nodes per thread for each mu bin: NPT * T >= 1024
+// where registers allow (a 1000-node stream in one CTA), the f halves of all
+// NPT nodes plus ~45 scalars inside the register cap of T threads.
+template <int MMAX> struct Stream2Shape;
+template <> struct Stream2Shape<8> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<16> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<24> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<32> { static constexpr int T = 256, NPT = 4; };
+template <> struct Stream2Shape<40> { static constexpr int T = 256, NPT = 4; };
+template <> struct Stream2Shape<48> { static constexpr int T = 256, NPT = 3; };
+template <> struct Stream2Shape<64> { static constexpr int T = 256, NPT = 2; };
+
+template <int MMAX>
+constexpr size_t stream2_smem_bytes() {
+  return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
+}
+
+template <int MMAX>
+__global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
+  constexpr int T = Stream2Shape<MMAX>::T;
+  constexpr int NPT = Stream2Shape<MMAX>::NPT;
+  constexpr int W = T / 32;
+  constexpr int H = MMAX / 2;  // register slots per direction (mu < 0, mu >= 0)
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) float halo[];  // [p][hi/lo][W+1][H]
+  auto hi = [&](int p, int w) { return halo + ((p * 2 + 0) * (W + 1) + w) * H; };
+  auto lo = [&](int p, int w) { return halo + ((p * 2 + 1) * (W + 1) + w) * H; };
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int crank = (int)cluster.block_rank();
+  const int s = blockIdx.y;
+  const int e = r.E - 1 - (int)blockIdx.z;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int M = r.M, N = r.N;
+  const int nL = m0, nR = M - m0;  // cells moving toward the inner / outer end
+  const int L = r.list_size[s];
+  if (L < 3) return;
+
+  const EnergyConsts ec = r.ec[e];
+  const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
+  const double nst = floor(r.dt / dtMin + 1.0);
+  if (!(nst <= (double)r.max_subcycles)) {
+    if (crank == 0 && tid == 0) set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    return;
+  }
+  const int nsteps = (int)nst;
+  const double dtProp = r.dt / (1.0 * nsteps);
+  const double dtProp_i = 1.0 / dtProp;
+  if (crank == 0 && tid == 0) {
+    atomicMax(&r.status->max_stream, nsteps);
+    atomicAdd(&r.status->stream_cs, (unsigned long long)nsteps * L * M);
+  }
+  for (int j = tid; j < 2 * 2 * (W + 1) * H; j += T) halo[j] = 0.f;
+
+  const int i0 = NPT * (crank * T + tid);  // list index of this thread's first node
+  const size_t sN = (size_t)s * N;
+  // Lf[q] holds node q's mu = j cells (mu < 0), Rf[q] its mu = m0 + j cells
+  float Lf[NPT][H], Rf[NPT][H];
+  // per node: mult for each upwind direction (zero where the reference leaves
+  // the cell unchanged: first list node for mu >= 0, last for mu < 0),
+  // relaxation factor exp(-dtProp/tau) and 1 - it, boundary seed
+  float mhi[NPT], mlo[NPT], em[NPT], om[NPT], bcv[NPT];
+  bool bc[NPT];
+  const double vdt = ec.vgrid * dtProp;
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    mhi[q] = mlo[q] = em[q] = om[q] = bcv[q] = 0.f;
+    bc[q] = false;
+#pragma unroll
+    for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = 0.f;
+    const int il = i0 + q;
+    if (il < L) {
+      const int k = r.list[sN + il];
+      const size_t gidx = sN + k;
+      const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
+      const double dsi = r.ds_i[sN + il];
+      const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
+      const double emt = exp(-dtProp / tau);
+      const double seedv = seed_value(r, ec, r.seed_radial[gidx]);
+      const float seedf = to_real<float>(seedv);
+      const float *fp = reinterpret_cast<const float *>(r.f) + (gidx * r.E + e) * M;
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        if (j < nL) {
+          float v = fp[j];
+          if (r.check_seed && (double)v < seedv) v = seedf;
+          Lf[q][j] = v;
+        }
+        if (j < nR) {
+          float v = fp[m0 + j];
+          if (r.check_seed && (double)v < seedv) v = seedf;
+          Rf[q][j] = v;
+        }
+      }
+      mhi[q] = (il == 0) ? 0.f : (float)mult;
+      mlo[q] = (il == L - 1) ? 0.f : (float)mult;
+      em[q] = (float)emt;
+      om[q] = (float)(1.0 - emt);
+      bc[q] = r.use_bc && il < 3;
+      bcv[q] = seedf;
+    }
+  }
+  // del_fac(mu) = v dtProp mugrid(mu), mugrid(mu) = -1 + (mu + 1/2) dmu
+  const float dl0 = (float)(vdt * r.mugrid[0]);
+  const float dr0 = (float)(vdt * r.mugrid[m0 < M ? m0 : M - 1]);
+  const float ddel = (float)(vdt * r.dmu);
+  const float inv_m = (float)(1.0 / M);
+  float *next_hi0 = (C > 1 && crank < C - 1) ? cluster.map_shared_rank(halo, crank + 1) : nullptr;
+  float *prev_loW = (C > 1 && crank > 0) ? cluster.map_shared_rank(halo, crank - 1) : nullptr;
+  if (C > 1)
+    cluster.sync();
+  else
+    __syncthreads();
+
+  for (int step = 0; step < nsteps; ++step) {
+    const int p = step & 1;
+#pragma unroll
+    for (int q = 0; q < NPT; ++q)
+      if (bc[q]) {
+#pragma unroll
+        for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = bcv[q];
+      }
+    if (lane == 31) {  // last node's outward half for the next warp's first node
+      float *dst = hi(p, warp + 1);
+      float *rdst = (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H : nullptr;
+#pragma unroll
+      for (int j = 0; j < H; ++j)
+        if (j < nR) {
+          dst[j] = Rf[NPT - 1][j];
+          if (rdst) rdst[j] = Rf[NPT - 1][j];
+        }
+    }
+    if (lane == 0) {  // first node's inward half for the previous warp's last node
+      float *dst = lo(p, warp);
+      float *rdst = (warp == 0 && prev_loW) ? prev_loW + ((p * 2 + 1) * (W + 1) + W) * H : nullptr;
+#pragma unroll
+      for (int j = 0; j < H; ++j)
+        if (j < nL) {
+          dst[j] = Lf[0][j];
+          if (rdst) rdst[j] = Lf[0][j];
+        }
+    }
+    if (C > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+    const float *my_hi = hi(p, warp);
+    const float *my_lo = lo(p, warp + 1);
+    float acc[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) acc[q] = 0.f;
+    // mu < 0: upwind from the outer neighbour (list node + 1), old values
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      if (j < nL) {
+        float del = dl0 + (float)j * ddel;
+        // opaque to loop-invariant code motion: otherwise the compiler hoists
+        // every mult*del product out of the sub-cycle loop into registers
+        asm volatile("" : "+f"(del));
+        float nb = __shfl_down_sync(FULL, Lf[0][j], 1);
+        if (lane == 31) nb = my_lo[j];
+#pragma unroll
+        for (int q = 0; q < NPT; ++q) {
+          const float right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][j] : nb;
+          Lf[q][j] = Lf[q][j] + (mlo[q] * del) * (Lf[q][j] - right);
+          acc[q] += Lf[q][j];
+        }
+      }
+    }
+    // mu >= 0: upwind from the inner neighbour (list node - 1), old values
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      if (j < nR) {
+        float del = dr0 + (float)j * ddel;
+        asm volatile("" : "+f"(del));
+        float nb = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
+        if (lane == 0) nb = my_hi[j];
+#pragma unroll
+        for (int q = NPT - 1; q >= 0; --q) {
+          const float left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][j] : nb;
+          Rf[q][j] = Rf[q][j] + (mhi[q] * del) * (left - Rf[q][j]);
+          acc[q] += Rf[q][j];
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const float iso = (inv_m * acc[q]) * om[q];
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        Lf[q][j] = Lf[q][j] * em[q] + iso;
+        Rf[q][j] = Rf[q][j] * em[q] + iso;
+      }
+    }
+  }
+
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il < L) {
+      const int k = r.list[sN + il];
+      int code = 0;
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        if (j < nL) {
+          const float v = Lf[q][j];
+          if (bad_value(v, &code)) set_error(r.status, code, 1, s, k, e, j);
+          Lf[q][j] = v < FLT_MIN ? FLT_MIN : v;
+        }
+        if (j < nR) {
+          const float v = Rf[q][j];
+          if (bad_value(v, &code)) set_error(r.status, code, 1, s, k, e, m0 + j);
+          Rf[q][j] = v < FLT_MIN ? FLT_MIN : v;
+        }
+      }
+      // node k and the thinned nodes that reference it (previous list node + 1 .. k)
+      const int kfirst = (il == 0) ? 0 : r.list[sN + il - 1] + 1;
+      for (int kk = kfirst; kk <= k; ++kk) {
+        float *op = reinterpret_cast<float *>(r.f) + ((sN + kk) * r.E + e) * M;
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+          if (j < nL) op[j] = Lf[q][j];
+          if (j < nR) op[m0 + j] = Rf[q][j];
+        }
+      }
+    }
+  }
+  if (C > 1) cluster.sync();
+}
+
+int plan_stream2(int N, int M, int m0, StreamPlan *plan) {
+  int mmax = 0;
+  for (int b : {8, 16, 24, 32, 40, 48, 64})
+    if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
+  if (!mmax) return EPREM_GPU_ERR_ARG;
+  int T, npt;
+  switch (mmax) {
+    case 8: T = Stream2Shape<8>::T; npt = Stream2Shape<8>::NPT; break;
+    case 16: T = Stream2Shape<16>::T; npt = Stream2Shape<16>::NPT; break;
+    case 24: T = Stream2Shape<24>::T; npt = Stream2Shape<24>::NPT; break;
+    case 32: T = Stream2Shape<32>::T; npt = Stream2Shape<32>::NPT; break;
+    case 40: T = Stream2Shape<40>::T; npt = Stream2Shape<40>::NPT; break;
+    case 48: T = Stream2Shape<48>::T; npt = Stream2Shape<48>::NPT; break;
+    default: T = Stream2Shape<64>::T; npt = Stream2Shape<64>::NPT; break;
+  }
+  plan->mmax = mmax;
+  plan->threads = T;
+  plan->reg_coef = 2;  // marks the several-nodes-per-thread kernel
+  plan->cluster = (N + npt * T - 1) / (npt * T);
+  return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
+}
+
+template <int MMAX>
+static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, cudaStream_t st) {
+  constexpr int T = Stream2Shape<MMAX>::T;
+  constexpr size_t dyn = stream2_smem_bytes<MMAX>();
+  auto kern = k_stream2<MMAX>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cluster, r.S, r.E);
+  cfg.blockDim = dim3(T, 1, 1);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, r, m0);
+}
+
+int launch_stream2(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st,
+                   uint64_t *launches) {
+  cudaError_t err;
+  switch (pl.mmax) {
+    case 8: err = launch_stream2_t<8>(r, pl.cluster, m0, st); break;
+    case 16: err = launch_stream2_t<16>(r, pl.cluster, m0, st); break;
+    case 24: err = launch_stream2_t<24>(r, pl.cluster, m0, st); break;
+    case 32: err = launch_stream2_t<32>(r, pl.cluster, m0, st); break;
+    case 40: err = launch_stream2_t<40>(r, pl.cluster, m0, st); break;
+    case 48: err = launch_stream2_t<48>(r, pl.cluster, m0, st); break;
+    default: err = launch_stream2_t<64>(r, pl.cluster, m0, st); break;
+  }
+  *launches += 1;
+  return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+}  // namespace eprem

@@ -42,6 +42,10 @@ EXPORTS = [
     ("eprem_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("eprem_gpu_read_kernel_timing", C.c_int, [C.c_void_p, C.POINTER(abi.KernelTime)]),
     ("eprem_gpu_alu_peak", C.c_int, [C.c_int, DP]),
+    ("eprem_gpu_mas_init", C.c_int, [C.c_void_p, C.POINTER(abi.MasParams)]),
+    ("eprem_gpu_mas_load_slice", C.c_int, [C.c_void_p, C.c_int, C.POINTER(abi.MasSlice)]),
+    ("eprem_gpu_mas_select", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]),
+    ("eprem_gpu_mas_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_last_error", C.c_char_p, []),
 ]
 
@@ -162,6 +166,21 @@ class EpremRun:
     def move_nodes(self, dt: float):
         """moveNodes (src/simCore.c:737-785)."""
         self._check(self.lib.eprem_gpu_move_nodes(self.handle, dt))
+
+    # -- MAS background ------------------------------------------------------
+    def mas_init(self, mas_params: abi.MasParams):
+        """Switch updateMhd to the MAS background (masGetNode)."""
+        self._check(self.lib.eprem_gpu_mas_init(self.handle, C.byref(mas_params)))
+
+    def mas_load_slice(self, slot: int, slice_struct: abi.MasSlice):
+        self._check(self.lib.eprem_gpu_mas_load_slice(self.handle, slot, C.byref(slice_struct)))
+
+    def mas_select(self, slot0: int, slot1: int, s_cor: float, phi_offset: float = 0.0):
+        self._check(self.lib.eprem_gpu_mas_select(self.handle, slot0, slot1, s_cor, phi_offset))
+
+    def mas_move_nodes(self, dt: float):
+        """masMoveNodes (src/masInterp.c:1344-1393)."""
+        self._check(self.lib.eprem_gpu_mas_move_nodes(self.handle, dt))
 
     def read_stats(self) -> abi.EpStats:
         st = abi.EpStats()

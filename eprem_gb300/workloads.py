@@ -349,3 +349,132 @@ def with_faces(w: Workload, rows: int, cols: int) -> Workload:
     more streams, each with identical node, energy and mu grids)."""
     return dataclasses.replace(w, rows=rows, cols=cols,
                                name=f"{w.name} on {6 * rows * cols} streams")
+
+
+# ---------------------------------------------------------------------------
+# Synthetic MAS-like background (the MHD-coupled workload).  MAS output is a
+# set of HDF5 slices per field on staggered spherical meshes in MAS units
+# (src/readMAS.c, src/baseTypes.h:104-115).  This builds the same structure
+# from an analytic Parker wind plus a Gaussian-shell CME pulse: the CME doubles
+# the density and adds a radial speed increment inside a shell launched at
+# 2 Rs that moves outward at the CME speed, within a cone of given half-width.
+MAS_LENGTH_NORM = 6.96e10
+MAS_RHO_NORM = 1.6726e-16
+RSUN = 6.96e10
+RSAU = RSUN / AU
+MAS_B_CONVERT = math.sqrt(4.0 * PI * MAS_RHO_NORM) * MAS_LENGTH_NORM / MAS_TIME_NORM / MHD_B_NORM
+MAS_V_CONVERT = (MAS_LENGTH_NORM / MAS_TIME_NORM) / C_LIGHT
+MAS_RHO_CONVERT = (MAS_RHO_NORM / MP) / MHD_DENSITY_NORM
+
+
+@dataclasses.dataclass
+class MasGrid:
+    nr: int
+    nt: int
+    np_: int
+    r_min_rs: float
+    r_max_rs: float
+    times: np.ndarray               # slice times (AU/c)
+    params: "abi.MasParams"
+    wind: abi.Params
+    cme_speed_kms: float = 1500.0
+    cme_dv_kms: float = 1200.0
+    cme_density_factor: float = 2.0
+    cme_half_width_deg: float = 30.0
+    cme_launch_rs: float = 2.0
+    cme_theta: float = PI / 2
+    cme_phi: float = 0.0
+
+    def meshes(self):
+        """Cell-centre meshes and the half-shifted ones of the staggered
+        components: r (solar radii, geometric stretch), theta, phi."""
+        rf = self.r_min_rs * (self.r_max_rs / self.r_min_rs) ** (np.arange(self.nr) / (self.nr - 1))
+        rh = np.sqrt(rf * np.concatenate([rf[1:], [rf[-1] * rf[-1] / rf[-2]]]))
+        dt_ = PI / self.nt
+        tc = (np.arange(self.nt) + 0.5) * dt_
+        th = np.arange(self.nt) * dt_ + dt_  # half-shifted
+        th[-1] = min(th[-1], PI)
+        dp = 2 * PI / self.np_
+        pc = (np.arange(self.np_) + 0.5) * dp
+        ph = np.arange(self.np_) * dp + dp
+        return {"r": rf, "rh": rh, "t": tc, "th": th, "p": pc, "ph": ph}
+
+    def field_meshes(self):
+        m = self.meshes()
+        # staggered by half a cell along each vector component's own direction
+        return {"Bp": (m["r"], m["t"], m["ph"]), "Bt": (m["r"], m["th"], m["p"]),
+                "Br": (m["rh"], m["t"], m["p"]), "Vp": (m["r"], m["t"], m["ph"]),
+                "Vt": (m["r"], m["th"], m["p"]), "Vr": (m["rh"], m["t"], m["p"]),
+                "rho": (m["r"], m["t"], m["p"])}
+
+    def slice_fields(self, t: float) -> dict:
+        """All seven fields at time t (AU/c), MAS units, float32 [phi][theta][r]."""
+        w = self.wind
+        out = {}
+        shell_r = self.cme_launch_rs + self.cme_speed_kms * 1e5 * (t * TAU) / RSUN
+        ct0, st0 = math.cos(self.cme_theta), math.sin(self.cme_theta)
+        for name, (mr, mt, mp) in self.field_meshes().items():
+            P, Tt, R = np.meshgrid(mp, mt, mr, indexing="ij")
+            r_au = R * RSAU
+            cos_ang = np.cos(Tt) * ct0 + np.sin(Tt) * st0 * np.cos(P - self.cme_phi)
+            ang = np.arccos(np.clip(cos_ang, -1.0, 1.0))
+            hw = math.radians(self.cme_half_width_deg)
+            g = np.exp(-((R - shell_r) / 1.0) ** 2) * np.exp(-(ang / hw) ** 2)
+            vr = w.mhd_us * (1.0 + 0.0 * R) + self.cme_dv_kms * 1e5 / C_LIGHT * g
+            br = w.mhd_bs_au / (r_au * r_au)
+            if name == "Br":
+                val = br / MAS_B_CONVERT
+            elif name == "Bt":  # weak latitudinal field so every component is exercised
+                val = (0.05 * br * np.sin(P)) / MAS_B_CONVERT
+            elif name == "Bp":
+                val = (-1.0 * r_au * br * (w.omega_sun / vr) * np.sin(Tt)) / MAS_B_CONVERT
+            elif name == "Vr":
+                val = vr / MAS_V_CONVERT
+            elif name == "Vt":
+                val = (5.0e5 / C_LIGHT) * np.sin(P) / MAS_V_CONVERT
+            elif name == "Vp":
+                val = (10.0e5 / C_LIGHT) * np.cos(Tt) / MAS_V_CONVERT
+            else:
+                val = (w.mhd_ns_au / (r_au * r_au)) * (1.0 + (self.cme_density_factor - 1.0) * g)
+                val = val / MAS_RHO_CONVERT
+            out[name] = np.ascontiguousarray(val, dtype=np.float32)
+        return out
+
+
+def mas_grid(nr=300, nt=180, np_=360, r_min_rs=1.0, r_max_rs=30.0, n_slices=16,
+             slice_dt_hours=1.0, wind: abi.Params | None = None, **kw) -> MasGrid:
+    p = abi.MasParams()
+    p.radial_max = r_max_rs
+    p.v_min = 50.0e5
+    p.cor_rotate_fake = 0
+    p.rotate_solution = 1
+    p.max_slices = n_slices
+    times = np.arange(n_slices) * slice_dt_hours * 3600.0 / TAU
+    return MasGrid(nr, nt, np_, r_min_rs, r_max_rs, times, p, wind or _plain_wind_params(), **kw)
+
+
+def mas_slice_struct(grid: MasGrid, fields: dict):
+    """abi.MasSlice over `fields` (keep the returned list alive)."""
+    keep = []
+    s = abi.MasSlice()
+    fm = grid.field_meshes()
+    for i, name in enumerate(abi.MAS_FIELDS):
+        meshes = [np.ascontiguousarray(m, dtype=np.float32) for m in fm[name]]
+        data = fields[name]
+        keep.extend(meshes)
+        keep.append(data)
+        for ax in range(3):
+            s.dims[i][ax] = len(meshes[ax])
+            s.mesh[i][ax] = meshes[ax].ctypes.data_as(abi.C.POINTER(abi.C.c_float))
+        s.data[i] = data.ctypes.data_as(abi.C.POINTER(abi.C.c_float))
+    return s, keep
+
+
+def mas_workload(streams_rows=2, streams_cols=2, nodes=60, energies=12, mu=8, r_min_au=0.006,
+                 r_max_au=1.0, name=None) -> Workload:
+    """Nodes from inside the MAS domain out past its edge (masWind takes over
+    beyond masRadialMax)."""
+    p = _plain_wind_params()
+    return Workload(name or f"mas {6 * streams_rows * streams_cols}x{nodes}x{energies}x{mu}",
+                    streams_rows, streams_cols, nodes, energies, mu, 0.1, 100.0, r_min_au,
+                    r_max_au, p)

@@ -121,11 +121,12 @@ typedef struct {
   int32_t max_subcycles;            /* cap on any sub-cycle count; above it the
                                        update stops with ERR_SUBCYCLES (0 means
                                        1,000,000).  The reference has no cap. */
-  int32_t stream_variant;           /* streaming-kernel shape (tuning, no effect
-                                       on results): 0 automatic, 1 upwind
-                                       coefficients in registers (thread-block
-                                       clusters for long streams), 2 coefficients
-                                       in shared memory (one CTA per slab)     */
+  int32_t stream_variant;           /* streaming-kernel shape in the FP32 form
+                                       (tuning; results agree to rounding): 0
+                                       automatic (= 3), 1 one node per thread
+                                       with coefficients in registers, 2 one
+                                       node per thread with coefficients in
+                                       shared memory, 3 two nodes per thread  */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids
@@ -260,6 +261,45 @@ int eprem_gpu_synchronize(eprem_gpu_run *run);
  * counterpart. */
 void    *eprem_gpu_stream(eprem_gpu_run *run);
 uint64_t eprem_gpu_kernel_launches(const eprem_gpu_run *run);
+
+/* ---- MAS coupling (src/masInterp.c, src/readMAS.c) ----------------------
+ * The reference reads MAS HDF5 slices into float arrays, one per field and
+ * time slot (masBp_0 ... masD_1, src/readMAS.h), each on its own staggered
+ * (r, theta, phi) mesh, and interpolates them onto the nodes in updateMhd and
+ * masMoveNodes.  File reading stays in the reference; these calls take the
+ * arrays it read.  Field order is the reference's: */
+#define EPREM_MAS_NFIELDS 7  /* Bp, Bt, Br, Vp, Vt, Vr, rho (src/masInterp.c:593-720) */
+typedef struct {
+  int32_t dims[EPREM_MAS_NFIELDS][3];       /* points along r, theta, phi per field */
+  const float *mesh[EPREM_MAS_NFIELDS][3];  /* r (solar radii), theta, phi (rad)     */
+  const float *data[EPREM_MAS_NFIELDS];     /* [phi][theta][r], r fastest, MAS units */
+} eprem_mas_slice_t;
+
+typedef struct {
+  double  radial_max;       /* config.masRadialMax (solar radii)                  */
+  double  v_min;            /* config.masVmin (cm/s)                              */
+  int32_t cor_rotate_fake;  /* config.masCorRotateFake                            */
+  int32_t rotate_solution;  /* config.masRotateSolution                           */
+  int32_t max_slices;       /* device slots for time slices (the reference holds
+                               two, state0/state1; HBM holds many)                */
+  int32_t pad;
+} eprem_mas_params_t;
+
+/* Switch the run to the MAS background: updateMhd takes its MHD_MAS branch
+ * (masGetNode, src/masInterp.c:31-68, with masTriLinear :539-740 and the
+ * Parker extrapolation masWind :1007-1065 outside masRadialMax) and
+ * eprem_gpu_mas_move_nodes becomes available (masMoveNodes). */
+int eprem_gpu_mas_init(eprem_gpu_run *run, const eprem_mas_params_t *mp);
+/* Copy one time slice (all seven fields with their meshes) into device slot
+ * `slot`; the replacement of masReadData's H2D side (src/readMAS.c:705-830). */
+int eprem_gpu_mas_load_slice(eprem_gpu_run *run, int slot, const eprem_mas_slice_t *slice);
+/* Interpolate between slots slot0 and slot1 with the time factor s_cor
+ * (masGetInterpData, src/readMAS.c:645-998) and the phi offset phiOffset. */
+int eprem_gpu_mas_select(eprem_gpu_run *run, int slot0, int slot1, double s_cor,
+                         double phi_offset);
+/* masMoveNodes(dt): RK4 push of every node but the innermost of each stream
+ * through the interpolated MAS velocity (src/masInterp.c:1281-1393). */
+int eprem_gpu_mas_move_nodes(eprem_gpu_run *run, double dt);
 
 /* Per-launch CUDA-event timing of the run's kernels on its stream (off by
  * default).  read_kernel_timing fills out[EPREM_KERNEL_NKINDS], synchronizes

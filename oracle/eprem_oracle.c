@@ -1092,3 +1092,271 @@ int orc_abi_layout(long *out, int cap) {
 #undef PUT
   return n;
 }
+
+/* ======================================================================== */
+/* MAS coupling.  Unit conversions of src/baseTypes.h:104-115; note that
+ * MAS_B_CONVERT expands without parentheses where the reference multiplies by
+ * it, so the product is ((((x*sqrt(4 pi rho_n))*L_n)/T_n)/B_norm). */
+#define ORC_RSUN 6.96e10
+#define ORC_RSAU (ORC_RSUN / ORC_AU)
+#define ORC_MAS_LENGTH_NORM 6.96e10
+#define ORC_MAS_RHO_NORM 1.6726e-16
+
+typedef struct {
+  double br, bt, bp, vr, vt, vp, d;
+} orc_masnode_t;
+
+/* masTriLinearBinarySearch, src/masInterp.c:118-171 */
+static double orc_mas_search(const float *A, double key, int *imin, int *imax, int lower,
+                             int upper) {
+  while (upper != (lower + 1)) {
+    int imid = (lower + upper) / 2;
+    if (A[imid] < key)
+      lower = imid;
+    else
+      upper = imid;
+  }
+  *imin = lower;
+  *imax = upper;
+  if (A[*imin] > key) return 0.0;
+  if (A[*imax] < key) return 1.0;
+  return ((key - A[lower]) / (A[upper] - A[lower]));
+}
+
+/* masInterpolate, src/masInterp.c:178-200 */
+static double orc_mas_interp(const float *V, int r0, int r1, int t0, int t1, int p0, int p1,
+                             double rd, double td, double pd, int rDim, int tDim) {
+#define VIX(r, t, p) ((size_t)(r) + (size_t)rDim * (t) + (size_t)rDim * tDim * (p))
+  double c00 = V[VIX(r0, t0, p0)] * (1.0 - rd) + V[VIX(r1, t0, p0)] * rd;
+  double c10 = V[VIX(r0, t0, p1)] * (1.0 - rd) + V[VIX(r1, t0, p1)] * rd;
+  double c01 = V[VIX(r0, t1, p0)] * (1.0 - rd) + V[VIX(r1, t1, p0)] * rd;
+  double c11 = V[VIX(r0, t1, p1)] * (1.0 - rd) + V[VIX(r1, t1, p1)] * rd;
+#undef VIX
+  double c0 = c00 * (1.0 - pd) + c10 * pd;
+  double c1 = c01 * (1.0 - pd) + c11 * pd;
+  return (c0 * (1.0 - td) + c1 * td);
+}
+
+/* One field of masTriLinear: search both slots' meshes and blend in time. */
+static double orc_mas_field(const orc_mas_t *mas, int f, double rr, double th, double ph) {
+  double val[2];
+  for (int sl = 0; sl < 2; sl++) {
+    const eprem_mas_slice_t *S = sl ? mas->slot1 : mas->slot0;
+    int r0, r1, t0, t1, p0, p1;
+    double rd = orc_mas_search(S->mesh[f][0], rr, &r0, &r1, 0, S->dims[f][0] - 1);
+    double td = orc_mas_search(S->mesh[f][1], th, &t0, &t1, 0, S->dims[f][1] - 1);
+    double pd = orc_mas_search(S->mesh[f][2], ph, &p0, &p1, 0, S->dims[f][2] - 1);
+    val[sl] = orc_mas_interp(S->data[f], r0, r1, t0, t1, p0, p1, rd, td, pd, S->dims[f][0],
+                             S->dims[f][1]);
+  }
+  return ((1.0 - mas->s_cor) * val[0] + mas->s_cor * val[1]);
+}
+
+/* masTriLinear, src/masInterp.c:539-740 (position: r in AU, theta, phi). */
+static void orc_mas_trilinear(const orc_mas_t *mas, double pr, double pth, double pph,
+                              orc_masnode_t *out) {
+  double rr = pr / ORC_RSAU;
+  double th = pth;
+  double ph = pph - mas->phi_offset;
+  if (ph < 0.0)
+    while (ph < 0.0) ph += (2.0 * ORC_PI);
+  if (ph > (2.0 * ORC_PI))
+    while (ph > (2.0 * ORC_PI)) ph -= (2.0 * ORC_PI);
+  double b;
+  b = orc_mas_field(mas, 0, rr, th, ph);
+  out->bp = b * sqrt(4.0 * ORC_PI * ORC_MAS_RHO_NORM) * ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM / ORC_MHD_B_NORM;
+  b = orc_mas_field(mas, 1, rr, th, ph);
+  out->bt = b * sqrt(4.0 * ORC_PI * ORC_MAS_RHO_NORM) * ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM / ORC_MHD_B_NORM;
+  b = orc_mas_field(mas, 2, rr, th, ph);
+  out->br = b * sqrt(4.0 * ORC_PI * ORC_MAS_RHO_NORM) * ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM / ORC_MHD_B_NORM;
+  b = orc_mas_field(mas, 3, rr, th, ph);
+  out->vp = b * (ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM) / ORC_C;
+  b = orc_mas_field(mas, 4, rr, th, ph);
+  out->vt = b * (ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM) / ORC_C;
+  b = orc_mas_field(mas, 5, rr, th, ph);
+  out->vr = b * (ORC_MAS_LENGTH_NORM / ORC_MAS_TIME_NORM) / ORC_C;
+  if (out->vr < (mas->p.v_min / ORC_C)) out->vr = (mas->p.v_min / ORC_C);
+  b = orc_mas_field(mas, 6, rr, th, ph);
+  out->d = b * (ORC_MAS_RHO_NORM / ORC_MP) / ORC_MHD_DENSITY_NORM;
+}
+
+/* masWind, src/masInterp.c:1007-1065: Parker extrapolation from the node's
+ * previous values. */
+static void orc_mas_wind(const orc_mas_t *mas, const eprem_params_t *p, const double *nodes,
+                         size_t SN, size_t g, orc_masnode_t *out) {
+  const double *F = nodes;
+#define NF(field) F[(size_t)(field) * SN + g]
+  double ox = NF(EPREM_NODE_ROLD_X), oy = NF(EPREM_NODE_ROLD_Y), oz = NF(EPREM_NODE_ROLD_Z);
+  double br = NF(EPREM_NODE_BR), bt = NF(EPREM_NODE_BTHETA), bp = NF(EPREM_NODE_BPHI);
+  double vr = NF(EPREM_NODE_VR), vt = NF(EPREM_NODE_VTHETA), vp = NF(EPREM_NODE_VPHI);
+  double rho = NF(EPREM_NODE_DENSITY);
+  double rOldmag = sqrt(ox * ox + oy * oy + oz * oz);
+  double rmag = NF(EPREM_NODE_RMAG);
+  double oneOverR = rOldmag / rmag;
+  out->br = br * oneOverR * oneOverR;
+  out->bt = bt * oneOverR;
+  out->bp = bp * oneOverR;
+  if ((mas->p.cor_rotate_fake > 0) && (mas->p.rotate_solution > 0)) {
+    double theta = acos(NF(EPREM_NODE_RZ) / rmag);
+    double thetaOld = acos(oz / rOldmag);
+    out->bp += ((p->r_scale * p->omega_sun / vr) *
+                (rOldmag * br * sin(thetaOld) - rmag * out->br * sin(theta)));
+  }
+  out->vr = vr;
+  out->vt = vt * oneOverR;
+  out->vp = vp * oneOverR;
+  out->d = rho * oneOverR * oneOverR;
+#undef NF
+}
+
+/* cartToSphPosAu, src/geometry.c:131-157 */
+static void orc_sph_au(const eprem_params_t *p, double x, double y, double z, double *r,
+                       double *th, double *ph) {
+  double ax = x * p->r_scale, ay = y * p->r_scale, az = z * p->r_scale;
+  *r = sqrt(ax * ax + ay * ay + az * az);
+  *th = acos(az / *r);
+  *ph = atan2(ay, ax);
+  while (*ph < 0.0) *ph += (2.0 * ORC_PI);
+  if (*ph < 0.0)
+    while (*ph < 0.0) *ph += 2 * ORC_PI;
+  if (*ph > 2 * ORC_PI)
+    while (*ph > 2 * ORC_PI) *ph -= 2 * ORC_PI;
+}
+
+/* masGetNode, src/masInterp.c:31-68 (no heliospheric domain). */
+static void orc_mas_get_node(const orc_mas_t *mas, const eprem_params_t *p, const double *nodes,
+                             size_t SN, size_t g, double pr, double pth, double pph,
+                             orc_masnode_t *out) {
+  if (pr <= (mas->p.radial_max * ORC_RSAU))
+    orc_mas_trilinear(mas, pr, pth, pph, out);
+  else
+    orc_mas_wind(mas, p, nodes, SN, g, out);
+}
+
+int orc_mas_update_mhd(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                       const orc_mas_t *mas, double t_global) {
+  (void)t_global;
+  const int N = d->num_nodes;
+  const size_t SN = (size_t)d->num_streams * N;
+  for (int s = 0; s < d->num_streams; s++)
+    for (int k = 0; k < N; k++) {
+      const size_t g = (size_t)s * N + k;
+      NODE(EPREM_NODE_BMAG_OLD, s, k) = NODE(EPREM_NODE_BMAG, s, k);
+      NODE(EPREM_NODE_DENSITY_OLD, s, k) = NODE(EPREM_NODE_DENSITY, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_R, s, k) = NODE(EPREM_NODE_VR, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_THETA, s, k) = NODE(EPREM_NODE_VTHETA, s, k);
+      NODE(EPREM_NODE_VSPH_OLD_PHI, s, k) = NODE(EPREM_NODE_VPHI, s, k);
+      NODE(EPREM_NODE_DS_OLD, s, k) = NODE(EPREM_NODE_DS, s, k);
+      NODE(EPREM_NODE_ROLDER_X, s, k) = NODE(EPREM_NODE_RX, s, k);
+      NODE(EPREM_NODE_ROLDER_Y, s, k) = NODE(EPREM_NODE_RY, s, k);
+      NODE(EPREM_NODE_ROLDER_Z, s, k) = NODE(EPREM_NODE_RZ, s, k);
+      double x = NODE(EPREM_NODE_RX, s, k), y = NODE(EPREM_NODE_RY, s, k),
+             z = NODE(EPREM_NODE_RZ, s, k), rmag = NODE(EPREM_NODE_RMAG, s, k);
+      double pr, pth, pph;
+      orc_sph_au(p, x, y, z, &pr, &pth, &pph);
+      orc_masnode_t mn;
+      orc_mas_get_node(mas, p, nodes, SN, g, pr, pth, pph, &mn);
+      double dens = mn.d;
+      NODE(EPREM_NODE_DENSITY, s, k) = dens;
+      if (dens <= 0.0)
+        NODE(EPREM_NODE_DIVV, s, k) = 0.0;
+      else
+        NODE(EPREM_NODE_DIVV, s, k) = -1.0 * log(dens / NODE(EPREM_NODE_DENSITY_OLD, s, k)) / p->t_del;
+      double theta = acos(z / rmag);
+      double phi = atan2(y, x);
+      double Vr = mn.vr, Vt = mn.vt, Vp = mn.vp;
+      NODE(EPREM_NODE_VR, s, k) = Vr;
+      NODE(EPREM_NODE_VTHETA, s, k) = Vt;
+      NODE(EPREM_NODE_VPHI, s, k) = Vp;
+      NODE(EPREM_NODE_VMAG, s, k) = sqrt(Vr * Vr + Vt * Vt + Vp * Vp);
+      NODE(EPREM_NODE_VVEC_X, s, k) = Vr * sin(theta) * cos(phi) + Vt * cos(theta) * cos(phi) - Vp * sin(phi);
+      NODE(EPREM_NODE_VVEC_Y, s, k) = Vr * sin(theta) * sin(phi) + Vt * cos(theta) * sin(phi) + Vp * cos(phi);
+      NODE(EPREM_NODE_VVEC_Z, s, k) = Vr * cos(theta) - Vt * sin(theta);
+      double Br = mn.br, Bt = mn.bt, Bp = mn.bp;
+      NODE(EPREM_NODE_BR, s, k) = Br;
+      NODE(EPREM_NODE_BTHETA, s, k) = Bt;
+      NODE(EPREM_NODE_BPHI, s, k) = Bp;
+      double Bmag = sqrt(Br * Br + Bt * Bt + Bp * Bp);
+      NODE(EPREM_NODE_BMAG, s, k) = Bmag;
+      NODE(EPREM_NODE_BVEC_X, s, k) = Br * sin(theta) * cos(phi) + Bt * cos(theta) * cos(phi) - Bp * sin(phi);
+      NODE(EPREM_NODE_BVEC_Y, s, k) = Br * sin(theta) * sin(phi) + Bt * cos(theta) * sin(phi) + Bp * cos(phi);
+      NODE(EPREM_NODE_BVEC_Z, s, k) = Br * cos(theta) - Bt * sin(theta);
+      if (k == 0) {
+        NODE(EPREM_NODE_DUPAR, s, k) = 0.0;
+        NODE(EPREM_NODE_DLNB, s, k) = 0.0;
+        NODE(EPREM_NODE_DLNN, s, k) = 0.0;
+      } else {
+        double dupar = (Vr - NODE(EPREM_NODE_VSPH_OLD_R, s, k)) * Br +
+                       (Vt - NODE(EPREM_NODE_VSPH_OLD_THETA, s, k)) * Bt +
+                       (Vp - NODE(EPREM_NODE_VSPH_OLD_PHI, s, k)) * Bp;
+        dupar /= Bmag;
+        NODE(EPREM_NODE_DUPAR, s, k) = dupar;
+        NODE(EPREM_NODE_DLNB, s, k) = log(Bmag / NODE(EPREM_NODE_BMAG_OLD, s, k));
+        NODE(EPREM_NODE_DLNN, s, k) = log(dens / NODE(EPREM_NODE_DENSITY_OLD, s, k));
+      }
+    }
+  return EPREM_GPU_OK;
+}
+
+/* sphToCartVector, src/geometry.c:89-121 */
+static void orc_sph_to_cart_vec(double vr, double vt, double vp, double x, double y, double z,
+                                double *ox, double *oy, double *oz) {
+  double rmag = sqrt(x * x + y * y + z * z);
+  if ((rmag - fabs(z)) < ORC_VERYSMALL) {
+    *ox = 0.0;
+    *oy = 0.0;
+  } else {
+    *ox = x / rmag * vr + x * z / (rmag * sqrt(rmag * rmag - z * z)) * vt -
+          y / sqrt(rmag * rmag - z * z) * vp;
+    *oy = y / rmag * vr + y * z / (rmag * sqrt(rmag * rmag - z * z)) * vt +
+          x / sqrt(rmag * rmag - z * z) * vp;
+  }
+  *oz = z / rmag * vr - sqrt(rmag * rmag - z * z) / rmag * vt;
+}
+
+/* vMas, src/masInterp.c:1281-1296: velocity at position (x,y,z) for node g
+ * (whose stored fields feed masWind beyond the MAS domain). */
+static void orc_vmas(const orc_mas_t *mas, const eprem_params_t *p, const double *nodes,
+                     size_t SN, size_t g, double x, double y, double z, double *vx, double *vy,
+                     double *vz) {
+  double pr, pth, pph;
+  orc_sph_au(p, x, y, z, &pr, &pth, &pph);
+  orc_masnode_t mn;
+  orc_mas_get_node(mas, p, nodes, SN, g, pr, pth, pph, &mn);
+  orc_sph_to_cart_vec(mn.vr, mn.vt, mn.vp, x, y, z, vx, vy, vz);
+}
+
+int orc_mas_move_nodes(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                       const orc_mas_t *mas, double dt) {
+  const int N = d->num_nodes;
+  const size_t SN = (size_t)d->num_streams * N;
+  const double sixth = 1.0 / 6.0, two = 2.0, half = 0.5;
+  for (int s = 0; s < d->num_streams; s++)
+    for (int k = 1; k < N; k++) {
+      const size_t g = (size_t)s * N + k;
+      double x0 = NODE(EPREM_NODE_RX, s, k), y0 = NODE(EPREM_NODE_RY, s, k),
+             z0 = NODE(EPREM_NODE_RZ, s, k);
+      /* rungeKuttaFlow (src/masInterp.c:1306-1334) reads the node as it was
+       * before this call set rOld, so rOld is written after the push. */
+      double vx, vy, vz, k1x, k1y, k1z, k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z;
+      orc_vmas(mas, p, nodes, SN, g, x0, y0, z0, &vx, &vy, &vz);
+      k1x = vx * (dt / p->r_scale); k1y = vy * (dt / p->r_scale); k1z = vz * (dt / p->r_scale);
+      orc_vmas(mas, p, nodes, SN, g, x0 + k1x * half, y0 + k1y * half, z0 + k1z * half, &vx, &vy, &vz);
+      k2x = vx * (dt / p->r_scale); k2y = vy * (dt / p->r_scale); k2z = vz * (dt / p->r_scale);
+      orc_vmas(mas, p, nodes, SN, g, x0 + k2x * half, y0 + k2y * half, z0 + k2z * half, &vx, &vy, &vz);
+      k3x = vx * (dt / p->r_scale); k3y = vy * (dt / p->r_scale); k3z = vz * (dt / p->r_scale);
+      orc_vmas(mas, p, nodes, SN, g, x0 + k3x, y0 + k3y, z0 + k3z, &vx, &vy, &vz);
+      k4x = vx * (dt / p->r_scale); k4y = vy * (dt / p->r_scale); k4z = vz * (dt / p->r_scale);
+      double x1 = x0 + sixth * (k1x + two * k2x + two * k3x + k4x);
+      double y1 = y0 + sixth * (k1y + two * k2y + two * k3y + k4y);
+      double z1 = z0 + sixth * (k1z + two * k2z + two * k3z + k4z);
+      NODE(EPREM_NODE_ROLD_X, s, k) = x0;
+      NODE(EPREM_NODE_ROLD_Y, s, k) = y0;
+      NODE(EPREM_NODE_ROLD_Z, s, k) = z0;
+      NODE(EPREM_NODE_RX, s, k) = x1;
+      NODE(EPREM_NODE_RY, s, k) = y1;
+      NODE(EPREM_NODE_RZ, s, k) = z1;
+      NODE(EPREM_NODE_RMAG, s, k) = sqrt((x1 * x1) + (y1 * y1) + (z1 * z1));
+    }
+  return EPREM_GPU_OK;
+}

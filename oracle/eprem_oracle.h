@@ -70,6 +70,21 @@ int orc_move_nodes(const eprem_dims_t *d, const eprem_params_t *p,
 void orc_omni_flux(const eprem_dims_t *d, const eprem_grids_t *g,
                    const double *f, double *out);
 
+/* MAS background: two time slots, the time factor s_cor and the phi offset,
+ * as the reference's readMAS globals hold them. */
+typedef struct {
+  const eprem_mas_slice_t *slot0, *slot1;
+  double s_cor, phi_offset;
+  eprem_mas_params_t p;
+} orc_mas_t;
+
+/* updateMhd with mhdGridStatus == MHD_MAS (src/flow.c:36-154 with
+ * masGetNode src/masInterp.c:31-68). */
+int orc_mas_update_mhd(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                       const orc_mas_t *mas, double t_global);
+/* masMoveNodes (src/masInterp.c:1344-1393). */
+int orc_mas_move_nodes(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                       const orc_mas_t *mas, double dt);
 #ifdef __cplusplus
 }
 #endif

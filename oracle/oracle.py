@@ -54,7 +54,16 @@ class Oracle:
         lib.orc_build_grids.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                         C.c_double, C.c_double, DP, DP, DP, DP, DP, DP, DP, DP]
         lib.orc_build_grids.restype = None
+        _mas_bind(lib)
         self.lib = lib
+
+    def mas_update_mhd(self, dims, params, nodes, mas: MasState, t_global=0.0):
+        return self.lib.orc_mas_update_mhd(C.byref(dims), C.byref(params), _dp(nodes),
+                                           C.byref(mas), t_global)
+
+    def mas_move_nodes(self, dims, params, nodes, mas: MasState, dt):
+        return self.lib.orc_mas_move_nodes(C.byref(dims), C.byref(params), _dp(nodes),
+                                           C.byref(mas), dt)
 
     def grids(self, E, M, e_min, e_max, mass=1.0, charge=1.0, rigidity_power=1.0 / 3.0):
         out = {k: np.zeros(E) for k in ("egrid", "vgrid", "vgrid_i", "pgrid", "rigidity")}
@@ -93,6 +102,19 @@ class Oracle:
         return self.lib.orc_seed_function(C.byref(params), energy, r)
 
 
+class MasState(C.Structure):
+    """orc_mas_t of eprem_oracle.h."""
+    _fields_ = [("slot0", C.POINTER(abi.MasSlice)), ("slot1", C.POINTER(abi.MasSlice)),
+                ("s_cor", C.c_double), ("phi_offset", C.c_double), ("p", abi.MasParams)]
+
+
+def _mas_bind(lib):
+    lib.orc_mas_update_mhd.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP,
+                                       C.POINTER(MasState), C.c_double]
+    lib.orc_mas_move_nodes.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP,
+                                       C.POINTER(MasState), C.c_double]
+
+
 class Reference:
     """The reference's own updateEnergeticParticles / updateMhd / moveNodes.
     The reference allocates its globals once per process, so one process can
@@ -108,7 +130,17 @@ class Reference:
         lib.ref_update_energetic_particles.argtypes = [C.c_double, C.POINTER(abi.EpStats)]
         lib.ref_update_mhd.argtypes = [C.c_double]
         lib.ref_move_nodes.argtypes = [C.c_double]
+        lib.ref_mas_setup.argtypes = [C.POINTER(abi.MasParams), C.POINTER(abi.MasSlice),
+                                      C.POINTER(abi.MasSlice), C.c_double, C.c_double]
+        lib.ref_mas_move_nodes.argtypes = [C.c_double]
         self.lib = lib
+
+    def mas_setup(self, mp, s0, s1, s_cor, phi_offset):
+        self._mas_keep = (mp, s0, s1)
+        return self.lib.ref_mas_setup(C.byref(mp), C.byref(s0), C.byref(s1), s_cor, phi_offset)
+
+    def mas_move_nodes(self, dt):
+        self.lib.ref_mas_move_nodes(dt)
 
     def setup(self, w, precision=abi.EPREM_FP64):
         d = w.dims(precision)

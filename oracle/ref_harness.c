@@ -38,6 +38,8 @@
 #include "mpiInit.h"
 #include "simCore.h"
 #include "unifiedOutput.h"
+#include "readMAS.h"
+#include "masInterp.h"
 
 #include "../include/eprem_gpu.h"
 
@@ -456,3 +458,41 @@ int ref_move_nodes(double dt) {
 
 int ref_node_t_size(void) { return (int)sizeof(Node_t); }
 int ref_node_T_extent(void) { return (int)tsize(Node_T); }
+
+/* ---- MAS background ------------------------------------------------------ */
+/* Point the reference's MAS globals (src/readMAS.h) at caller arrays, as
+ * masGetInterpData leaves them after reading two slices, and switch updateMhd
+ * to its MHD_MAS branch. */
+int ref_mas_setup(const eprem_mas_params_t *mp, const eprem_mas_slice_t *a,
+                  const eprem_mas_slice_t *b, double scor, double phioff) {
+  config.masCouple = 1;
+  config.masHelCouple = 0;
+  config.masRadialMax = mp->radial_max;
+  config.masVmin = mp->v_min;
+  config.masCorRotateFake = mp->cor_rotate_fake;
+  config.masRotateSolution = mp->rotate_solution;
+  mhdGridStatus = MHD_MAS;
+  s_cor = scor;
+  phiOffset = phioff;
+#define SETF(F, i, S, sl)                                      \
+  mas##F##_##sl = (float *)S->data[i];                         \
+  mas##F##rDim_##sl = (float *)S->mesh[i][0];                  \
+  mas##F##tDim_##sl = (float *)S->mesh[i][1];                  \
+  mas##F##pDim_##sl = (float *)S->mesh[i][2];                  \
+  mas##F##rDimMax_##sl[0] = S->dims[i][0];                     \
+  mas##F##tDimMax_##sl[0] = S->dims[i][1];                     \
+  mas##F##pDimMax_##sl[0] = S->dims[i][2];
+  SETF(Bp, 0, a, 0) SETF(Bt, 1, a, 0) SETF(Br, 2, a, 0) SETF(Vp, 3, a, 0) SETF(Vt, 4, a, 0)
+  SETF(Vr, 5, a, 0) SETF(D, 6, a, 0)
+  SETF(Bp, 0, b, 1) SETF(Bt, 1, b, 1) SETF(Br, 2, b, 1) SETF(Vp, 3, b, 1) SETF(Vt, 4, b, 1)
+  SETF(Vr, 5, b, 1) SETF(D, 6, b, 1)
+#undef SETF
+  masDimMin_0[0] = 0;
+  masDimMin_1[0] = 0;
+  return 0;
+}
+
+int ref_mas_move_nodes(double dt) {
+  masMoveNodes(dt);
+  return 0;
+}

@@ -52,3 +52,28 @@ def test_fp32_sub_cycle_counts_equal_fp64(oracle_lib):
     assert st.max_substeps_stream == stats[0].max_substeps_stream
     assert st.stream_cell_subcycles == stats[0].stream_cell_subcycles
     assert st.max_subcycles_focusing == stats[0].max_subcycles_focusing
+
+
+@pytest.mark.parametrize("nodes", [400, 1100])
+def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
+    """The three FP32 streaming shapes (one node per thread with register or
+    shared-memory coefficients, several nodes per thread) compute the same
+    update up to float rounding; 1100 nodes needs a two-CTA cluster in the
+    several-nodes shape."""
+    w = W.custom(1, 1, nodes, 3, 40, num_ep_steps=2, use_adiabatic_focus=0,
+                 use_adiabatic_change=0)
+    d, g, f, nodes_arr = primed_state(w, oracle_lib)
+    f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes_arr)
+    outs = []
+    for variant in (1, 2, 3):
+        w.params.stream_variant = variant
+        run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+        run.upload_f(f)
+        run.upload_nodes(nodes_arr)
+        run.update_energetic_particles(0.0)
+        outs.append(run.download_f())
+        run.close()
+    w.params.stream_variant = 0
+    for o in outs:
+        assert np.max(np.abs(o - f_ref) / f_ref) <= 1e-4
+    assert np.max(np.abs(outs[0] - outs[2]) / outs[2]) <= 1e-5
