@@ -44,6 +44,17 @@ struct EnergyConsts {
   double rig_lamo;       // rigidity[E] * lamo              (src/meanFreePath.c:15)
   double seed_power;     // pow(E/normE1, -gamma)           (src/energeticParticlesBoundary.c:101)
   double seed_exp;       // exp(-(E/normE0))                (:102)
+  float v32, vi32;       // vgrid, vgrid_i rounded to float (FP32 stencils)
+};
+
+// Per-node coefficients of the FP32 focusing / change kernels, fixed for one
+// updateEnergeticParticles call (a node's MHD fields, ds and |B+-| do not
+// change during it).  ok = 0 for the spawn node, which is not updated.
+struct NodeCoef32 {
+  int ok, ns_f, ns_c, pad0;
+  float dlnbds, dupar, b, scale_f;  // focusing: a_E = -v dlnbds - (2/v) dupar
+  float cool, dlnb, dlnn, scale_c;  // change (rates per unit time)
+  float bc0, bc1, pad1, pad2;       // ln seed at the first and last energy
 };
 
 struct RunView {
@@ -53,6 +64,7 @@ struct RunView {
   double *nodes;           // [NF][S*N]
   const double *mugrid;    // [M]
   const EnergyConsts *ec;  // [E]
+  const float *mugrid32;   // [M]     mugrid rounded to float
   // per-call scratch
   int *list;               // [S][N]  stream list (GetStreamList shellList)
   int *list_size;          // [S]
@@ -60,6 +72,7 @@ struct RunView {
   double *ds_min;          // [S]
   double *seed_radial;     // [S*N]   pow(r/normRadius, -beta)
   double *mfp_node;        // [S*N]   pow(r*rScale, a) or pow(BsAu/B, b)
+  NodeCoef32 *coef32;      // [S*N]   FP32 form only
   DevStatus *status;
   // parameters
   double r_scale, dt, dt_full, dmu, dlnp;

@@ -54,6 +54,8 @@ struct eprem_gpu_run {
   double norm_radius = 0, neg_beta = 0;
   void *d_f = nullptr;
   double *d_nodes = nullptr, *d_mugrid = nullptr;
+  float *d_mugrid32 = nullptr;
+  NodeCoef32 *d_coef32 = nullptr;
   EnergyConsts *d_ec = nullptr;
   int *d_list = nullptr, *d_list_size = nullptr;
   double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;
@@ -219,6 +221,8 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   if (e == cudaSuccess) e = cudaMalloc(&r->d_f, cells * fbytes + 16);
   if (e == cudaSuccess) e = dalloc(&r->d_nodes, (size_t)EPREM_NODE_NFIELDS * SN);
   if (e == cudaSuccess) e = dalloc(&r->d_mugrid, (size_t)M);
+  if (e == cudaSuccess) e = dalloc(&r->d_mugrid32, (size_t)M);
+  if (e == cudaSuccess && fast32) e = dalloc(&r->d_coef32, SN);
   if (e == cudaSuccess) e = dalloc(&r->d_ec, (size_t)E);
   if (e == cudaSuccess) e = dalloc(&r->d_list, SN);
   if (e == cudaSuccess) e = dalloc(&r->d_list_size, (size_t)S);
@@ -247,10 +251,16 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
     ec[i].rig_lamo = grids->rigidity[i] * p.lamo;
     ec[i].seed_power = pow((grids->egrid[i] / normE1), -p.bf_gamma);
     ec[i].seed_exp = exp(-(grids->egrid[i] / normE0));
+    ec[i].v32 = (float)grids->vgrid[i];
+    ec[i].vi32 = (float)grids->vgrid_i[i];
   }
+  std::vector<float> mu32(M);
+  for (int m = 0; m < M; m++) mu32[m] = (float)grids->mugrid[m];
   e = cudaMemcpyAsync(r->d_ec, ec.data(), E * sizeof(EnergyConsts), cudaMemcpyHostToDevice, r->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(r->d_mugrid, grids->mugrid, M * sizeof(double), cudaMemcpyHostToDevice, r->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(r->d_mugrid32, mu32.data(), M * sizeof(float), cudaMemcpyHostToDevice, r->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
   if (e != cudaSuccess) {
     eprem_gpu_destroy(r);
@@ -269,6 +279,8 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.f = r->d_f;
   v.nodes = r->d_nodes;
   v.mugrid = r->d_mugrid;
+  v.mugrid32 = r->d_mugrid32;
+  v.coef32 = r->d_coef32;
   v.ec = r->d_ec;
   v.list = r->d_list;
   v.list_size = r->d_list_size;
@@ -318,6 +330,8 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_f);
   cudaFree(r->d_nodes);
   cudaFree(r->d_mugrid);
+  cudaFree(r->d_mugrid32);
+  cudaFree(r->d_coef32);
   cudaFree(r->d_ec);
   cudaFree(r->d_list);
   cudaFree(r->d_list_size);
@@ -422,6 +436,11 @@ extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_g
                            &r->launches);
   });
   if (rc) return cuda_fail(cudaGetLastError(), "geometry launch");
+  if (r->nplan.fast32 && (r->v.use_focus || r->v.use_change)) {
+    rc = timed(r, EPREM_KERNEL_NODE,
+               [&] { return launch_node32_setup(r->v, r->stream, &r->launches); });
+    if (rc) return cuda_fail(cudaGetLastError(), "focusing/change set-up launch");
+  }
   for (int step = 0; step < p.num_ep_steps; step++) {
     if (r->v.use_stream)
       rc = timed(r, EPREM_KERNEL_STREAM,

@@ -27,10 +27,15 @@ int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 int plan_stream2(int N, int M, int m0, StreamPlan *plan);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                    uint64_t *launches);
+// stream3.cu -- FP32 streaming, mu halves on two lanes (plan.reg_coef == 3, 4)
+int plan_stream3(int N, int M, int m0, int alt, StreamPlan *plan);
+int launch_stream3(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
+                   uint64_t *launches);
 
 // node.cu -- AdiabaticFocusing + AdiabaticChange
 struct NodePlan {
-  int pmax;        // register slots per thread (>= max(E, M))
+  int pmax;        // register slots per thread (>= max(E, M); FP32 form: >= M)
+  int pcol;        // FP32 form: register slots of a change column (>= E)
   int threads;     // threads per CTA
   int nodes;       // nodes per CTA
   size_t smem;     // dynamic shared memory bytes
@@ -41,6 +46,8 @@ int launch_node(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_
 // node32.cu -- FP32-form focusing + change (Euler operators)
 int plan_node32(int E, int M, NodePlan *plan);
 int launch_node32(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_t *launches);
+// once per updateEnergeticParticles call, before the first launch_node32
+int launch_node32_setup(const RunView &r, cudaStream_t st, uint64_t *launches);
 
 // mhd.cu -- updateMhd (analytic), moveNodes, omnidirectional flux, f conversion
 struct MhdParams {

@@ -142,12 +142,14 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
 
   for (int step = 0; step < nsteps; ++step) {
     const int p = step & 1;
+    if (crank == 0 && warp == 0) {  // the boundary nodes (list 0..2) live in warp 0
 #pragma unroll
-    for (int q = 0; q < NPT; ++q)
-      if (bc[q]) {
+      for (int q = 0; q < NPT; ++q)
+        if (bc[q]) {
 #pragma unroll
-        for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = bcv[q];
-      }
+          for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = bcv[q];
+        }
+    }
     if (lane == 31) {  // last node's outward half for the next warp's first node
       float *dst = hi(p, warp + 1);
       float *rdst = (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H : nullptr;

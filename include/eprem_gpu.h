@@ -126,7 +126,9 @@ typedef struct {
                                        automatic (= 3), 1 one node per thread
                                        with coefficients in registers, 2 one
                                        node per thread with coefficients in
-                                       shared memory, 3 two nodes per thread  */
+                                       shared memory, 3 several nodes per
+                                       thread, 4 / 5 the mu halves of a node
+                                       on two lanes (two thread shapes)       */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids
