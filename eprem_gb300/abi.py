@@ -29,6 +29,7 @@ STATUS_NAMES = {
 
 EPREM_FP64 = 0
 EPREM_FP32 = 1
+FLUX_STATIC_MAX = 1048576  # EPREM_GPU_FLUX_STATIC_MAX
 
 
 class Dims(C.Structure):

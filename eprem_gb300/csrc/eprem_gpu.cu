@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -576,6 +577,57 @@ extern "C" int eprem_gpu_omni_flux(eprem_gpu_run *r, double *out) {
             [&] { return launch_omni_flux(r->v, r->d_flux, r->stream, &r->launches); }))
     return cuda_fail(cudaGetLastError(), "flux launch");
   CK(cudaMemcpyAsync(out, r->d_flux, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  return check_status(r, false, nullptr);
+}
+
+// Omnidirectional flux staged in a fixed device buffer, for callers that may
+// not allocate once their run is set up (a run set sized to fill the GPU's
+// memory, a host that budgets device memory at start-up).  The buffer is a
+// file-scope device array, created with the module on each device; its
+// address is looked up once per device, with that device current, by the
+// first call there, so that call should come before any stream capture.
+// Every value is written by the flux kernel before it is copied out, so no
+// part of the buffer needs zeroing.  All runs on a device share it: calls
+// that overlap in time race on it and must be serialised by the caller.
+namespace {
+constexpr int kFluxStaticDevices = 64;
+__device__ __align__(256) double g_flux_static[EPREM_GPU_FLUX_STATIC_MAX];
+std::mutex g_flux_static_mutex;
+double *g_flux_static_addr[kFluxStaticDevices] = {};
+
+int flux_static_buffer(int device, double **out) {
+  if (device < 0 || device >= kFluxStaticDevices)
+    return fail(EPREM_GPU_ERR_ARG, "device ordinal beyond the static flux buffer table");
+  std::lock_guard<std::mutex> lock(g_flux_static_mutex);
+  if (!g_flux_static_addr[device]) {
+    int current = -1;
+    CK(cudaGetDevice(&current));
+    if (current != device) CK(cudaSetDevice(device));
+    void *addr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_flux_static);
+    if (current != device) CK(cudaSetDevice(current));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static flux buffer)");
+    g_flux_static_addr[device] = static_cast<double *>(addr);
+  }
+  *out = g_flux_static_addr[device];
+  return EPREM_GPU_OK;
+}
+}  // namespace
+
+extern "C" int eprem_gpu_omni_flux_static(eprem_gpu_run *r, double *out) {
+  if (!r || !out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t n = r->sn() * r->dims.num_energies;
+  if (n > (size_t)EPREM_GPU_FLUX_STATIC_MAX)
+    return fail(EPREM_GPU_ERR_ARG,
+                "eprem_gpu_omni_flux_static: S*N*E = " + std::to_string(n) +
+                    " values exceed the static buffer's " +
+                    std::to_string(EPREM_GPU_FLUX_STATIC_MAX) + "; use eprem_gpu_omni_flux");
+  double *buf = nullptr;
+  const int rc = flux_static_buffer(r->device, &buf);
+  if (rc) return rc;
+  if (launch_omni_flux(r->v, buf, r->stream, &r->launches))
+    return cuda_fail(cudaGetLastError(), "flux launch");
+  CK(cudaMemcpyAsync(out, buf, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
   return check_status(r, false, nullptr);
 }
 

@@ -36,6 +36,7 @@ EXPORTS = [
     ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_omni_flux_static", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_synchronize", C.c_int, [C.c_void_p]),
     ("eprem_gpu_stream", C.c_void_p, [C.c_void_p]),
     ("eprem_gpu_kernel_launches", C.c_uint64, [C.c_void_p]),
@@ -191,6 +192,14 @@ class EpremRun:
         d = self.dims
         out = np.empty(d.num_streams * d.num_nodes * d.num_energies)
         self._check(self.lib.eprem_gpu_omni_flux(self.handle, _dp(out)))
+        return out
+
+    def omni_flux_static(self) -> np.ndarray:
+        """omni_flux staged in the library's fixed device buffer: allocates
+        no device memory (S*N*E <= abi.FLUX_STATIC_MAX)."""
+        d = self.dims
+        out = np.empty(d.num_streams * d.num_nodes * d.num_energies)
+        self._check(self.lib.eprem_gpu_omni_flux_static(self.handle, _dp(out)))
         return out
 
     def synchronize(self):

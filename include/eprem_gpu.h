@@ -255,6 +255,35 @@ int eprem_gpu_move_nodes(eprem_gpu_run *run, double dt);
  * output unit scale.  out: S*N*E doubles, host memory.  Synchronizes. */
 int eprem_gpu_omni_flux(eprem_gpu_run *run, double *out_host);
 
+/* Capacity, in doubles, of the fixed device buffer behind
+ * eprem_gpu_omni_flux_static: 1,048,576 values (8 MiB), i.e. S*N*E up to
+ * that many (96 streams x 1000 nodes x 10 energies fits). */
+#define EPREM_GPU_FLUX_STATIC_MAX 1048576
+
+/* The omnidirectional flux of eprem_gpu_omni_flux, computed by the same
+ * kernel, but staged in a fixed device buffer that the library holds from
+ * the moment it is loaded on a device, so this call allocates no device or
+ * pinned host memory.  No counterpart in the reference: it exists for
+ * callers that cannot allocate at output time -- a run set or ensemble that
+ * sizes its runs to fill the GPU's memory up front (where the first
+ * eprem_gpu_omni_flux call, which allocates its staging buffer then, could
+ * fail for lack of memory in the middle of a simulation), or a host program
+ * that budgets device memory at start-up and permits no allocation later.
+ *   - The first call on each device does a one-time set-up: it looks up the
+ *     buffer's device address with that device current.  Make that first
+ *     call before any stream capture on the device.
+ *   - S*N*E above EPREM_GPU_FLUX_STATIC_MAX is rejected with
+ *     EPREM_GPU_ERR_ARG before anything is launched; use eprem_gpu_omni_flux.
+ *   - Nothing in the buffer needs to start at zero: the kernel writes every
+ *     one of the S*N*E values before they are copied out.
+ *   - There is one buffer per device, shared by all runs on it.  Calls that
+ *     overlap in time (two host threads, or two runs on one device) race on
+ *     it; serialise them.  One thread making calls one after another is safe,
+ *     since each call synchronizes before it returns.
+ *   - Kernel timing (eprem_gpu_set_kernel_timing) does not cover this call.
+ * out_host: S*N*E doubles, host memory.  Synchronizes. */
+int eprem_gpu_omni_flux_static(eprem_gpu_run *run, double *out_host);
+
 /* Wait for all work of the run; returns the first device-side failure. */
 int eprem_gpu_synchronize(eprem_gpu_run *run);
 
