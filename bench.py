@@ -52,6 +52,11 @@ def parse():
                     help="rows=cols of the plain-FP64 subset (6*n*n streams)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-mas", action="store_true")
+    ap.add_argument("--mas-steps", type=int, default=2)
+    ap.add_argument("--profile-step", choices=["fp32", "fp64"], default=None,
+                    help="run one EP sub-step of the 96-stream subset and exit "
+                         "(the case the ncu captures use)")
     return ap.parse_args()
 
 
@@ -226,7 +231,8 @@ def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
     # algorithmic HBM bytes: one read + one write of f per operator pass
     bytes_per_launch = cells * BYTES_PER_CELL_UPDATE[form] / 2.0
     return {
-        "kernel": "k_stream" if kind == "stream" else "k_node",
+        "kernel": ({"fp32": "k_stream2", "fp64": "k_stream"}[form] if kind == "stream"
+                   else {"fp32": "k_focus32+k_change32", "fp64": "k_node"}[form]),
         "bound": "fp64" if form == "fp64" else "fp32",
         "achieved": round(achieved, 3), "peak": round(peak_tflops, 3), "unit": "TFLOP/s",
         "frac": round(achieved / peak_tflops, 4),
@@ -413,6 +419,11 @@ def ours(args, rank, ws, dist):
         r64.close()
         r32.close()
 
+    # ---- MHD-coupled (MAS) workload ----------------------------------------
+    mas = None
+    if not args.skip_mas and rank == 0:
+        mas = mas_case(args, EpremRun, abi, W, fp32_peak, peaks.get("hbm_gbs"))
+
     # ---- CPU baseline ----------------------------------------------------
     cpu = None
     if not args.skip_cpu and rank == 0 and ws == 1:
@@ -443,14 +454,151 @@ def ours(args, rank, ws, dist):
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "plain_fp64": plain,
+            "mhd_coupled": mas,
             "alu_peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak},
             "stats_last_step": stats.as_dict(),
         }
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+class MasSlices:
+    """masGetInterpData's role for the bench (src/readMAS.c:645-998): the two
+    slices bounding a time are on the device (slot = slice index mod 3, so
+    the next slice can be loaded while the current pair stays selected), and
+    s_cor interpolates between them."""
+
+    def __init__(self, run, grid, W, t_end):
+        self.run, self.grid, self.W = run, grid, W
+        self.slot_of = {}
+        self.keep = {}
+        self.h2d_bytes = 0
+        # the synthetic slices are made on the host before any timing, as the
+        # reference reads its slice files outside its hot path
+        last = int(np.searchsorted(grid.times, t_end, side="right"))
+        self.fields = {k: grid.slice_fields(grid.times[k])
+                       for k in range(min(last + 1, len(grid.times)))}
+
+    def _load(self, k):
+        if k in self.slot_of:
+            return self.slot_of[k]
+        slot = k % 3
+        for kk in [kk for kk, sl in self.slot_of.items() if sl == slot]:
+            del self.slot_of[kk]
+            self.keep.pop(kk, None)
+        fields = self.fields[k]
+        st, keep = self.W.mas_slice_struct(self.grid, fields)
+        self.run.mas_load_slice(slot, st)
+        self.h2d_bytes += sum(a.nbytes for a in fields.values())
+        self.keep[k] = (st, keep, fields)
+        self.slot_of[k] = slot
+        return slot
+
+    def select(self, t):
+        times = self.grid.times
+        k0 = int(np.searchsorted(times, t, side="right") - 1)
+        k0 = min(max(k0, 0), len(times) - 2)
+        s_cor = (t - times[k0]) / (times[k0 + 1] - times[k0])
+        a, b = self._load(k0), self._load(k0 + 1)
+        self.run.mas_select(a, b, float(min(max(s_cor, 0.0), 1.0)), 0.0)
+
+
+def mas_case(args, EpremRun, abi, W, fp32_peak, hbm_peak):
+    """The MHD-coupled workload: 1536 streams x 1500 nodes x 40 E x 40 mu in
+    the FP32 form on a synthetic 300 x 180 x 360 staggered MAS grid (1-30 Rs)
+    with a CME pulse, 16 slices an hour apart; a step is masMoveNodes (RK4
+    through the interpolated V) + masGetInterpData + updateMhd (trilinear
+    interpolation of B, V, rho at every node) + updateEnergeticParticles."""
+    import torch
+    w = W.mas_workload(16, 16, 1500, 40, 40, r_min_au=0.006, r_max_au=1.0,
+                       name="mhd-coupled 1536x1500x40x40 on a 300x180x360 MAS grid")
+    grid = W.mas_grid(nr=300, nt=180, np_=360, r_min_rs=1.0, r_max_rs=30.0, n_slices=16)
+    g = W.build_grids(w)
+    run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+    nodes = W.initial_nodes(w)
+    run.upload_nodes(nodes)
+    mp = abi.MasParams.from_buffer_copy(bytes(grid.params))
+    mp.max_slices = 3
+    run.mas_init(mp)
+    td = w.params.t_del
+    sl = MasSlices(run, grid, W, td * (args.mas_steps + 4))
+    sl.select(0.0)
+    run.update_mhd(0.0)
+    run.mas_move_nodes(td)
+    sl.select(td)
+    run.update_mhd(td)
+    nodes = run.download_nodes()
+    f = W.fill_initial_f(w, nodes, g, np.empty(w.cells))
+    run.upload_f(f)
+    del f
+    run.synchronize()
+
+    def mas_step(t):
+        run.mas_move_nodes(td)           # src/eprem.c:621, interpolation data of time t
+        sl.select(t + td)                # masGetInterpData(tDel), :638
+        run.update_mhd(t + td)           # :639
+        run.update_energetic_particles(t)
+        return t + td
+
+    t = td
+    t = mas_step(t)
+    run.synchronize()
+    s, e0, e1 = event_pair(run.stream)
+    run.read_stats()
+    run.set_kernel_timing(True)
+    run.read_kernel_timing()
+    n0 = run.kernel_launches
+    torch.cuda.synchronize()
+    h0 = sl.h2d_bytes
+    e0.record(s)
+    for _ in range(args.mas_steps):
+        t = mas_step(t)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    kt = run.read_kernel_timing()
+    stats = run.read_stats()
+    launches = run.kernel_launches - n0
+    run.set_kernel_timing(False)
+    out = {
+        "value": w.cells * w.params.num_ep_steps * args.mas_steps / (ms * 1e-3),
+        "unit": UNIT, "workload": w.name, "steps": args.mas_steps, "warmup": 1,
+        "ms_per_step": ms / args.mas_steps, "dtype": "f32",
+        "step": "masMoveNodes(RK4)+masGetInterpData+updateMhd(MAS)+updateEnergeticParticles",
+        "mas_grid": {"nr": grid.nr, "nt": grid.nt, "np": grid.np_, "slices": len(grid.times),
+                     "slice_h2d_bytes_in_timed_steps": sl.h2d_bytes - h0},
+        "kernel_ms_per_step": {k: v[1] / args.mas_steps for k, v in kt.items() if v[0]},
+        "gpu_launches": launches,
+        "roofline": roofline(kt, stats, args.mas_steps, fp32_peak, hbm_peak, w.cells, "fp32"),
+    }
+    run.close()
+    return out
+
+
+def profile_step(args):
+    """One EP sub-step of the 96-stream subset of the precision-at-scale
+    workload (f = 0.77 GB in FP32, above L2): the small case of the ncu
+    captures."""
+    from eprem_gb300 import EpremRun, abi, workloads as W
+    w = W.scale_plain()
+    sub = W.with_faces(w, 4, 4)
+    sub.params.t_del = w.params.t_del / w.params.num_ep_steps
+    sub.params.num_ep_steps = 1
+    prec = abi.EPREM_FP32 if args.profile_step == "fp32" else abi.EPREM_FP64
+    run, g, nodes = make_state(sub, prec, EpremRun, abi, W)
+    run.upload_f(W.fill_initial_f(sub, nodes, g, np.empty(sub.cells)))
+    run.update_energetic_particles(0.0)
+    run.synchronize()
+    print(json.dumps({"profile_step": args.profile_step, "workload": sub.name,
+                      "stats": run.read_stats().as_dict()}))
+    run.close()
+
+
 def main():
     args = parse()
+    if args.profile_step:
+        profile_step(args)
+        return
     rank, ws, dist = dist_setup()
     try:
         if args.impl == "reference":

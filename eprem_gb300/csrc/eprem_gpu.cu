@@ -71,7 +71,8 @@ struct eprem_gpu_run {
   std::vector<std::pair<int, int>> ev_pending;  // (kind, index of start event)
   size_t ev_used = 0;
   // MAS background: device copies of the loaded time slices
-  bool mas_on = false, mas_selected = false;
+  bool mas_ready = false;  // eprem_gpu_mas_init done
+  bool mas_on = false, mas_selected = false;  // updateMhd uses MAS; slots chosen
   std::vector<std::vector<void *>> mas_allocs;
   std::vector<MasSlotDev> mas_slots;
   std::vector<char> mas_loaded;
@@ -487,6 +488,7 @@ extern "C" int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp
   if (!r || !mp) return fail(EPREM_GPU_ERR_ARG, "null argument");
   if (mp->max_slices < 2 || mp->max_slices > 4096)
     return fail(EPREM_GPU_ERR_ARG, "max_slices must be 2..4096");
+  r->mas_ready = true;
   r->mas_on = true;
   r->mas_selected = false;
   r->mas_allocs.assign(mp->max_slices, {});
@@ -503,7 +505,7 @@ extern "C" int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp
 
 extern "C" int eprem_gpu_mas_load_slice(eprem_gpu_run *r, int slot, const eprem_mas_slice_t *s) {
   if (!r || !s) return fail(EPREM_GPU_ERR_ARG, "null argument");
-  if (!r->mas_on) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
+  if (!r->mas_ready) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
   if (slot < 0 || slot >= (int)r->mas_slots.size()) return fail(EPREM_GPU_ERR_ARG, "slot out of range");
   CK(cudaStreamSynchronize(r->stream));
   for (void *p : r->mas_allocs[slot]) cudaFree(p);
@@ -538,7 +540,7 @@ extern "C" int eprem_gpu_mas_load_slice(eprem_gpu_run *r, int slot, const eprem_
 extern "C" int eprem_gpu_mas_select(eprem_gpu_run *r, int slot0, int slot1, double s_cor,
                                     double phi_offset) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
-  if (!r->mas_on) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
+  if (!r->mas_ready) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
   const int n = (int)r->mas_slots.size();
   if (slot0 < 0 || slot0 >= n || slot1 < 0 || slot1 >= n || !r->mas_loaded[slot0] ||
       !r->mas_loaded[slot1])
@@ -551,9 +553,16 @@ extern "C" int eprem_gpu_mas_select(eprem_gpu_run *r, int slot0, int slot1, doub
   return EPREM_GPU_OK;
 }
 
+extern "C" int eprem_gpu_mas_use(eprem_gpu_run *r, int use_mas) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (!r->mas_ready) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
+  r->mas_on = use_mas != 0;
+  return EPREM_GPU_OK;
+}
+
 extern "C" int eprem_gpu_mas_move_nodes(eprem_gpu_run *r, double dt) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
-  if (!r->mas_on || !r->mas_selected)
+  if (!r->mas_ready || !r->mas_selected)
     return fail(EPREM_GPU_ERR_STATE, "MAS background not initialised or no slices selected");
   if (timed(r, EPREM_KERNEL_MOVE,
             [&] { return launch_mas_move_nodes(r->v, r->mv, dt, r->stream, &r->launches); }))

@@ -27,10 +27,6 @@ int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 int plan_stream2(int N, int M, int m0, StreamPlan *plan);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                    uint64_t *launches);
-// stream3.cu -- FP32 streaming, mu halves on two lanes (plan.reg_coef == 3, 4)
-int plan_stream3(int N, int M, int m0, int alt, StreamPlan *plan);
-int launch_stream3(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
-                   uint64_t *launches);
 
 // node.cu -- AdiabaticFocusing + AdiabaticChange
 struct NodePlan {

@@ -280,13 +280,9 @@ static int threads_for(int mmax) {
 }
 
 // variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
-// 3 several list nodes per thread (stream2.cu), 4 / 5 mu halves on two lanes
-// in its two shapes (stream3.cu).  The FP64 form always keeps the
+// 3 several list nodes per thread (stream2.cu).  The FP64 form always keeps the
 // coefficients in shared memory; the automatic FP32 choice is variant 3.
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
-  if (precision == EPREM_FP32 && (variant == 4 || variant == 5) &&
-      plan_stream3(N, M, m0, variant == 5, plan) == 0)
-    return 0;
   if (precision == EPREM_FP32 && (variant == 0 || variant == 3) && plan_stream2(N, M, m0, plan) == 0)
     return 0;
   int mmax = 0;
@@ -353,7 +349,6 @@ static cudaError_t dispatch_mmax(const RunView &r, const StreamPlan &pl, int m0,
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches) {
   if (plan.reg_coef == 2) return launch_stream2(r, plan, m0, st, launches);
-  if (plan.reg_coef >= 3) return launch_stream3(r, plan, m0, st, launches);
   cudaError_t err;
   if (r.precision == EPREM_FP64)
     err = dispatch_mmax<double, false>(r, plan, m0, st);

@@ -6,8 +6,9 @@
  *   updateEnergeticParticles()  src/energeticParticles.c:70-203
  *   updateMhd()                 src/flow.c:36-154
  *   moveNodes(dt)               src/simCore.c:737-785
- * (INTEGRATION.md gives the build lines: the three originals are renamed with
- * -D at compile time so that the driver src/eprem.c, unchanged, calls these).
+ *   masMoveNodes(dt)            src/masInterp.c:1344-1393
+ * (the originals are renamed with -D at compile time so that the driver
+ * src/eprem.c, unchanged, calls these).
  *
  * The reference keeps its state in globals (grid[], eParts[], config, the
  * 1-D grids of energeticParticlesTypes.h); each call here packs what the GPU
@@ -15,9 +16,15 @@
  * point and unpacks the results, so everything else in the driver -- output,
  * shell spawning, MAS reading -- sees the same globals as before.
  *
+ * MAS runs: masGetInterpData (src/readMAS.c:645-998) still reads the slice
+ * files into the reference's _0 / _1 globals; a slot is copied to the device
+ * when its file index (masFileIndex0 / masFileIndex1) changes, and s_cor and
+ * phiOffset are passed on every call.
+ *
  * Scope: one MPI rank holds every stream (the GPU replaces the rank
- * decomposition), one species, analytic background (MAS coupling is refused
- * with the reference's panic), no drift or shell diffusion.
+ * decomposition), one species, analytic or MAS coronal background (the
+ * heliospheric MAS coupling is refused with the reference's panic), no drift
+ * or shell diffusion.
  */
 #include <float.h>
 #include <stdio.h>
@@ -32,7 +39,9 @@
 #include "error.h"
 #include "flow.h"
 #include "global.h"
+#include "masInterp.h"
 #include "mpiInit.h"
+#include "readMAS.h"
 #include "simCore.h"
 #include "timers.h"
 
@@ -100,7 +109,8 @@ static double *dropin_member(Node_t *n, int field) {
 static void dropin_init(void) {
   if (dropin_run) return;
   if (N_PROCS != 1) panic("GPU path: run with one MPI rank (every stream lives on the GPU)");
-  if (config.masCouple > 0) panic("GPU path: MAS coupling is not supported by this build");
+  if (config.masHelCouple > 0)
+    panic("GPU path: heliospheric MAS coupling is not supported by this build");
   if (config.useDrift > 0 || config.useShellDiffusion > 0)
     panic("GPU path: drift and shell diffusion are not supported by this build");
   eprem_dims_t d;
@@ -236,9 +246,67 @@ void updateEnergeticParticles(void) {
   timer_diffusestream += MPI_Wtime() - t0;
 }
 
+/* ---- MAS background --------------------------------------------------- */
+static int dropin_mas_ready = 0;
+static Index_t dropin_mas_file[2] = {-1, -1};
+
+/* The reference's slot globals (src/readMAS.h) as an ABI slice. */
+#define DROPIN_MAS_FIELD(S, i, F, SL)                                  \
+  do {                                                                 \
+    (S)->data[i] = mas##F##_##SL;                                      \
+    (S)->mesh[i][0] = mas##F##rDim_##SL;                               \
+    (S)->mesh[i][1] = mas##F##tDim_##SL;                               \
+    (S)->mesh[i][2] = mas##F##pDim_##SL;                               \
+    (S)->dims[i][0] = mas##F##rDimMax_##SL[0];                         \
+    (S)->dims[i][1] = mas##F##tDimMax_##SL[0];                         \
+    (S)->dims[i][2] = mas##F##pDimMax_##SL[0];                         \
+  } while (0)
+
+static void dropin_mas_slot(int slot, eprem_mas_slice_t *sl) {
+  if (slot == 0) {
+    DROPIN_MAS_FIELD(sl, 0, Bp, 0); DROPIN_MAS_FIELD(sl, 1, Bt, 0); DROPIN_MAS_FIELD(sl, 2, Br, 0);
+    DROPIN_MAS_FIELD(sl, 3, Vp, 0); DROPIN_MAS_FIELD(sl, 4, Vt, 0); DROPIN_MAS_FIELD(sl, 5, Vr, 0);
+    DROPIN_MAS_FIELD(sl, 6, D, 0);
+  } else {
+    DROPIN_MAS_FIELD(sl, 0, Bp, 1); DROPIN_MAS_FIELD(sl, 1, Bt, 1); DROPIN_MAS_FIELD(sl, 2, Br, 1);
+    DROPIN_MAS_FIELD(sl, 3, Vp, 1); DROPIN_MAS_FIELD(sl, 4, Vt, 1); DROPIN_MAS_FIELD(sl, 5, Vr, 1);
+    DROPIN_MAS_FIELD(sl, 6, D, 1);
+  }
+}
+
+/* Bring the device slots up to the slices masGetInterpData has loaded. */
+static void dropin_mas_sync(void) {
+  if (!dropin_mas_ready) {
+    eprem_mas_params_t mp;
+    memset(&mp, 0, sizeof(mp));
+    mp.radial_max = config.masRadialMax;
+    mp.v_min = config.masVmin;
+    mp.cor_rotate_fake = config.masCorRotateFake;
+    mp.rotate_solution = config.masRotateSolution;
+    mp.max_slices = 2;
+    dropin_check(eprem_gpu_mas_init(dropin_run, &mp), "MAS set-up");
+    dropin_mas_ready = 1;
+  }
+  const Index_t idx[2] = {masFileIndex0, masFileIndex1};
+  for (int slot = 0; slot < 2; slot++)
+    if (idx[slot] != dropin_mas_file[slot]) {
+      eprem_mas_slice_t sl;
+      dropin_mas_slot(slot, &sl);
+      dropin_check(eprem_gpu_mas_load_slice(dropin_run, slot, &sl), "MAS slice upload");
+      dropin_mas_file[slot] = idx[slot];
+    }
+  dropin_check(eprem_gpu_mas_select(dropin_run, 0, 1, s_cor, phiOffset), "MAS slices");
+}
+
 void updateMhd(void) {
   dropin_init();
   const uint64_t all = EPREM_NODE_MASK_ALL;
+  if (mhdGridStatus == MHD_MAS) {
+    dropin_mas_sync();
+    dropin_check(eprem_gpu_mas_use(dropin_run, 1), "updateMhd");
+  } else if (dropin_mas_ready) {
+    dropin_check(eprem_gpu_mas_use(dropin_run, 0), "updateMhd");
+  }
   dropin_pack_nodes(all);
   dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, all), "upload nodes");
   dropin_check(eprem_gpu_update_mhd(dropin_run, t_global), "updateMhd");
@@ -258,4 +326,15 @@ void moveNodes(Scalar_t dt) {
   dropin_check(eprem_gpu_move_nodes(dropin_run, dt), "moveNodes");
   dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, mv), "download nodes");
   dropin_unpack_nodes(mv);
+}
+
+void masMoveNodes(Scalar_t dt) {
+  dropin_init();
+  dropin_mas_sync();
+  const uint64_t all = EPREM_NODE_MASK_ALL;
+  dropin_pack_nodes(all);
+  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, all), "upload nodes");
+  dropin_check(eprem_gpu_mas_move_nodes(dropin_run, dt), "masMoveNodes");
+  dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, all), "download nodes");
+  dropin_unpack_nodes(all);
 }

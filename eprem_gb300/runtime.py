@@ -47,6 +47,7 @@ EXPORTS = [
     ("eprem_gpu_mas_load_slice", C.c_int, [C.c_void_p, C.c_int, C.POINTER(abi.MasSlice)]),
     ("eprem_gpu_mas_select", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]),
     ("eprem_gpu_mas_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_mas_use", C.c_int, [C.c_void_p, C.c_int]),
     ("eprem_gpu_last_error", C.c_char_p, []),
 ]
 
@@ -178,6 +179,10 @@ class EpremRun:
 
     def mas_select(self, slot0: int, slot1: int, s_cor: float, phi_offset: float = 0.0):
         self._check(self.lib.eprem_gpu_mas_select(self.handle, slot0, slot1, s_cor, phi_offset))
+
+    def mas_use(self, use_mas: bool):
+        """updateMhd's background after mas_init: MAS (True) or analytic."""
+        self._check(self.lib.eprem_gpu_mas_use(self.handle, int(bool(use_mas))))
 
     def mas_move_nodes(self, dt: float):
         """masMoveNodes (src/masInterp.c:1344-1393)."""

@@ -413,8 +413,11 @@ class MasGrid:
         out = {}
         shell_r = self.cme_launch_rs + self.cme_speed_kms * 1e5 * (t * TAU) / RSUN
         ct0, st0 = math.cos(self.cme_theta), math.sin(self.cme_theta)
+        shape = (len(self.field_meshes()["rho"][2]), len(self.field_meshes()["rho"][1]),
+                 len(self.field_meshes()["rho"][0]))
         for name, (mr, mt, mp) in self.field_meshes().items():
-            P, Tt, R = np.meshgrid(mp, mt, mr, indexing="ij")
+            # broadcast views [phi][theta][r] (the values a full meshgrid holds)
+            P, Tt, R = mp[:, None, None], mt[None, :, None], mr[None, None, :]
             r_au = R * RSAU
             cos_ang = np.cos(Tt) * ct0 + np.sin(Tt) * st0 * np.cos(P - self.cme_phi)
             ang = np.arccos(np.clip(cos_ang, -1.0, 1.0))
@@ -437,7 +440,7 @@ class MasGrid:
             else:
                 val = (w.mhd_ns_au / (r_au * r_au)) * (1.0 + (self.cme_density_factor - 1.0) * g)
                 val = val / MAS_RHO_CONVERT
-            out[name] = np.ascontiguousarray(val, dtype=np.float32)
+            out[name] = np.ascontiguousarray(np.broadcast_to(val, shape), dtype=np.float32)
         return out
 
 

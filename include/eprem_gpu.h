@@ -127,8 +127,7 @@ typedef struct {
                                        with coefficients in registers, 2 one
                                        node per thread with coefficients in
                                        shared memory, 3 several nodes per
-                                       thread, 4 / 5 the mu halves of a node
-                                       on two lanes (two thread shapes)       */
+                                       thread                                 */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids
@@ -331,6 +330,13 @@ int eprem_gpu_mas_select(eprem_gpu_run *run, int slot0, int slot1, double s_cor,
 /* masMoveNodes(dt): RK4 push of every node but the innermost of each stream
  * through the interpolated MAS velocity (src/masInterp.c:1281-1393). */
 int eprem_gpu_mas_move_nodes(eprem_gpu_run *run, double dt);
+/* Which background eprem_gpu_update_mhd uses after eprem_gpu_mas_init: the
+ * MAS interpolation (use_mas = 1, mhdGridStatus == MHD_MAS) or the analytic
+ * wind (0, MHD_DEFAULT: masGetInterpData keeps the analytic background
+ * before the first MAS time, src/readMAS.c:667-674).  The slots stay loaded
+ * and eprem_gpu_mas_move_nodes keeps using them either way, as
+ * masMoveNodes does. */
+int eprem_gpu_mas_use(eprem_gpu_run *run, int use_mas);
 
 /* Per-launch CUDA-event timing of the run's kernels on its stream (off by
  * default).  read_kernel_timing fills out[EPREM_KERNEL_NKINDS], synchronizes

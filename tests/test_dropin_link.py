@@ -24,11 +24,14 @@ def test_driver_links_against_dropin():
     exe = os.path.join(ROOT, "eprem_gb300", "host", "_link", "eprem_gb300")
     syms = subprocess.check_output(["nm", exe], text=True)
     defined = {ln.split()[-1] for ln in syms.splitlines() if " T " in ln}
-    for name in ("updateEnergeticParticles", "updateMhd", "moveNodes", "main"):
+    for name in ("updateEnergeticParticles", "updateMhd", "moveNodes", "masMoveNodes", "main"):
         assert name in defined
     # the reference bodies are kept under other names; the driver calls the shim
-    for name in ("updateEnergeticParticles_cpu", "updateMhd_cpu", "moveNodes_cpu"):
+    for name in ("updateEnergeticParticles_cpu", "updateMhd_cpu", "moveNodes_cpu",
+                 "masMoveNodes_cpu"):
         assert name in defined
     undefined = {ln.split()[-1] for ln in syms.splitlines() if " U " in ln}
     assert {"eprem_gpu_create", "eprem_gpu_update_energetic_particles",
-            "eprem_gpu_update_mhd", "eprem_gpu_move_nodes"} <= undefined
+            "eprem_gpu_update_mhd", "eprem_gpu_move_nodes", "eprem_gpu_mas_init",
+            "eprem_gpu_mas_load_slice", "eprem_gpu_mas_select", "eprem_gpu_mas_move_nodes",
+            "eprem_gpu_mas_use"} <= undefined

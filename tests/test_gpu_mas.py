@@ -27,8 +27,12 @@ def _case(rows=1, cols=1, nodes=40):
 def _assert_nodes_close(a, b, what):
     for name in FIELDS_CHECKED:
         i = abi.NODE[name]
-        scale = max(np.max(np.abs(b[i])), 1e-300)
-        err = np.max(np.abs(a[i] - b[i])) / scale
+        same = a[i] == b[i]  # includes the infinite ln(B/Bold) of a first update
+        assert np.array_equal(np.isfinite(a[i]), np.isfinite(b[i])), f"{what}: field {name}"
+        fin = np.isfinite(b[i])
+        scale = max(np.max(np.abs(b[i][fin]), initial=0.0), 1e-300)
+        diff = np.where(same, 0.0, np.abs(a[i] - b[i]))
+        err = np.max(diff) / scale
         assert err <= 1e-10, f"{what}: field {name} differs by {err:.3e} of its scale"
 
 
@@ -76,4 +80,23 @@ def test_mas_requires_selection():
         run.mas_select(0, 1, 0.5)  # slot 1 never loaded
     with pytest.raises(Exception):
         run.mas_load_slice(5, s0)  # beyond max_slices
+    run.close()
+
+
+def test_mas_use_switches_back_to_the_analytic_wind(oracle_lib):
+    """mhdGridStatus == MHD_DEFAULT before the first MAS time: updateMhd takes
+    the analytic background although the slots stay loaded."""
+    w, grid, f0, f1 = _case()
+    s0, k0 = W.mas_slice_struct(grid, f0)
+    d = w.dims()
+    nodes = W.initial_nodes(w)
+    run = EpremRun(d, w.params, W.build_grids(w))
+    run.upload_nodes(nodes)
+    run.mas_init(grid.params)
+    run.mas_load_slice(0, s0)
+    run.mas_select(0, 0, 0.0)
+    run.mas_use(False)
+    run.update_mhd(0.0)
+    oracle_lib.update_mhd(d, w.params, nodes, 0.0)
+    _assert_nodes_close(run.download_nodes(), nodes, "analytic after mas_use(False)")
     run.close()
