@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mas", action="store_true")
+    ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--ensemble-runs", type=int, default=8,
+                    help="members of the 64-run batched ensemble to step (first n)")
+    ap.add_argument("--ensemble-steps", type=int, default=2)
     ap.add_argument("--mas-steps", type=int, default=2)
     ap.add_argument("--profile-step", choices=["fp32", "fp64"], default=None,
                     help="run one EP sub-step of the 96-stream subset and exit "
@@ -424,6 +428,12 @@ def ours(args, rank, ws, dist):
     if not args.skip_mas and rank == 0:
         mas = mas_case(args, EpremRun, abi, W, fp32_peak, peaks.get("hbm_gbs"))
 
+    # ---- batched ensemble --------------------------------------------------
+    ensemble = None
+    if not args.skip_ensemble and rank == 0:
+        from eprem_gb300 import Ensemble
+        ensemble = ensemble_case(args, EpremRun, Ensemble, abi, W)
+
     # ---- CPU baseline ----------------------------------------------------
     cpu = None
     if not args.skip_cpu and rank == 0 and ws == 1:
@@ -455,6 +465,7 @@ def ours(args, rank, ws, dist):
             "clocks": clk.summary(),
             "plain_fp64": plain,
             "mhd_coupled": mas,
+            "ensemble": ensemble,
             "alu_peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak},
             "stats_last_step": stats.as_dict(),
         }
@@ -572,6 +583,68 @@ def mas_case(args, EpremRun, abi, W, fp32_peak, hbm_peak):
         "roofline": roofline(kt, stats, args.mas_steps, fp32_peak, hbm_peak, w.cells, "fp32"),
     }
     run.close()
+    return out
+
+
+def ensemble_case(args, EpremRun, Ensemble, abi, W):
+    """The batched-ensemble workload: the first n of 64 runs with uneven
+    sizes and parameters (24-1536 streams, 400-2000 nodes, 20-50 E, 20-40 mu,
+    seed index, mean free path and shock speed drawn from a fixed seed) in
+    the FP32 form, streaming shapes autotuned per size class, one CUDA-graph
+    launch per step for all runs; beside it the same runs stepped one after
+    another through the per-run entry points."""
+    import torch
+    members = W.ensemble_members(64)[: args.ensemble_runs]
+    runs = []
+    for w in members:
+        run = EpremRun(w.dims(abi.EPREM_FP32), w.params, W.build_grids(w))
+        run.upload_nodes(W.initial_nodes(w))
+        run.update_mhd(0.0)
+        run.move_nodes(w.params.t_del)
+        run.update_mhd(w.params.t_del)
+        run.init_seed_population(w.seed, w.perturb)
+        runs.append(run)
+    cells = sum(w.cells * w.params.num_ep_steps for w in members)
+    t_tune = time.perf_counter()
+    ens = Ensemble(runs)
+    chosen = ens.autotune()
+    t_tune = time.perf_counter() - t_tune
+    # one after another, per-run entry points (host-timed around device syncs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for run, w in zip(runs, members):
+        t = w.params.t_del
+        run.move_nodes(w.params.t_del)
+        run.update_mhd(t + w.params.t_del)
+        run.update_energetic_particles(t)
+        run.synchronize()
+    seq_s = time.perf_counter() - t0
+    ens.set_time([2 * w.params.t_del for w in members])
+    ens.step()  # capture + first replay
+    ens.synchronize()
+    s, e0, e1 = event_pair(ens.stream)
+    n0 = sum(r.kernel_launches for r in runs)
+    e0.record(s)
+    for _ in range(args.ensemble_steps):
+        ens.step()
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    ens.synchronize()
+    launches = sum(r.kernel_launches for r in runs) - n0
+    out = {
+        "value": cells * args.ensemble_steps / (ms * 1e-3), "unit": UNIT,
+        "runs": len(members), "of_runs": 64, "total_cells": sum(w.cells for w in members),
+        "sizes": [w.name.split(": ")[1] for w in members],
+        "steps": args.ensemble_steps, "warmup": 1, "ms_per_step": ms / args.ensemble_steps,
+        "graph_launches_per_step": 1, "kernel_launches_per_step": launches // args.ensemble_steps,
+        "one_by_one_value": cells / seq_s,
+        "speedup_vs_one_by_one": (cells * args.ensemble_steps / (ms * 1e-3)) / (cells / seq_s),
+        "autotuned_stream_variants": chosen, "autotune_s": round(t_tune, 3), "dtype": "f32",
+    }
+    ens.close()
+    for r in runs:
+        r.close()
     return out
 
 

@@ -51,8 +51,12 @@ struct MhdParams {
   int ideal_shock;
   double sharp, scale_len, jump, falloff, speed, init_time, theta, phi, width;
 };
+// tg_dev: the run's time on the device (t = *tg_dev + t_global), or null
 int launch_update_mhd(const RunView &r, const MhdParams &p, double t_global, cudaStream_t st,
-                      uint64_t *launches);
+                      uint64_t *launches, const double *tg_dev = nullptr);
+int launch_advance_time(double *t_dev, double dt, cudaStream_t st, uint64_t *launches);
+int launch_seed_population(const RunView &r, unsigned long long seed, double perturb,
+                           cudaStream_t st, uint64_t *launches);
 int launch_move_nodes(const RunView &r, double dt, cudaStream_t st, uint64_t *launches);
 int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *launches);
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
@@ -73,5 +77,10 @@ int launch_mas_update_mhd(const RunView &r, const MasView &mv, double t_del, cud
                           uint64_t *launches);
 int launch_mas_move_nodes(const RunView &r, const MasView &mv, double dt, cudaStream_t st,
                           uint64_t *launches);
+
+// mlp.cu -- tcgen05 BF16 GEMM C = A * Bt^T (+ bias) of the learned surrogate;
+// err: device int set to 1 when a wait on the tensor cores timed out
+int launch_gemm_bf16(const void *A, int lda, const void *Bt, int ldb, const float *bias,
+                     float *C, int ldc, int M, int N, int K, int *err, cudaStream_t st);
 
 }  // namespace eprem

@@ -29,7 +29,10 @@ __device__ double shock_factor(const MhdParams &p, double r, double tg) {
   return 1 + (factor - 1) * falloff;
 }
 
-__global__ void k_update_mhd(RunView r, MhdParams p, double tg) {
+// tg_dev, when given, holds the run's time on the device (graph replays of an
+// ensemble step); tg is then the offset added to it.
+__global__ void k_update_mhd(RunView r, MhdParams p, double tg, const double *tg_dev) {
+  if (tg_dev) tg = *tg_dev + tg;
   const size_t SN = (size_t)r.S * r.N;
   for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < SN;
        g += (size_t)gridDim.x * blockDim.x) {
@@ -162,8 +165,18 @@ static int grid_for(size_t n) {
 }
 
 int launch_update_mhd(const RunView &r, const MhdParams &p, double tg, cudaStream_t st,
-                      uint64_t *launches) {
-  k_update_mhd<<<grid_for((size_t)r.S * r.N), 256, 0, st>>>(r, p, tg);
+                      uint64_t *launches, const double *tg_dev) {
+  k_update_mhd<<<grid_for((size_t)r.S * r.N), 256, 0, st>>>(r, p, tg, tg_dev);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+__global__ void k_advance_time(double *t, double dt) {
+  if (threadIdx.x == 0) *t += dt;
+}
+
+int launch_advance_time(double *t_dev, double dt, cudaStream_t st, uint64_t *launches) {
+  k_advance_time<<<1, 32, 0, st>>>(t_dev, dt);
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
@@ -193,6 +206,41 @@ int launch_convert_f(const RunView &r, const double *src64, double *dst64, int t
   else
     k_f32_to_f64<<<grid_for(count), 256, 0, st>>>(reinterpret_cast<const float *>(src64), dst64,
                                                   count);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+// Synthetic seed population: f = sepSeedFunction(E, r) (1 + perturb U) per
+// (stream, node, energy), isotropic in mu, with U in (-1, 1) from the top 53
+// bits of splitmix64(seed) at index (stream * N + node) * E + energy + 1 --
+// the same draw as the workload generator on the host.  Needs seed_radial
+// (geometry) of the current positions.
+__global__ void k_seed_population(RunView r, unsigned long long seed, double perturb) {
+  const size_t SNE = (size_t)r.S * r.N * r.E;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < SNE;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t g = i / r.E;
+    const int e = (int)(i - g * r.E);
+    unsigned long long z = seed + (unsigned long long)(i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    const double u = 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+    const double v = seed_value(r, r.ec[e], r.seed_radial[g]) * (1.0 + perturb * u);
+    if (r.precision == EPREM_FP64) {
+      double *row = reinterpret_cast<double *>(r.f) + i * r.M;
+      for (int m = 0; m < r.M; m++) row[m] = v;
+    } else {
+      float *row = reinterpret_cast<float *>(r.f) + i * r.M;
+      const float vf = to_real<float>(v);
+      for (int m = 0; m < r.M; m++) row[m] = vf;
+    }
+  }
+}
+
+int launch_seed_population(const RunView &r, unsigned long long seed, double perturb,
+                           cudaStream_t st, uint64_t *launches) {
+  k_seed_population<<<grid_for((size_t)r.S * r.N * r.E), 256, 0, st>>>(r, seed, perturb);
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

@@ -48,6 +48,21 @@ EXPORTS = [
     ("eprem_gpu_mas_select", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]),
     ("eprem_gpu_mas_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_mas_use", C.c_int, [C.c_void_p, C.c_int]),
+    ("eprem_gpu_init_seed_population", C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
+    ("eprem_gpu_autotune", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("eprem_gpu_set_stream_variant", C.c_int, [C.c_void_p, C.c_int]),
+    ("eprem_gpu_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int,
+                                            C.POINTER(C.c_void_p)]),
+    ("eprem_gpu_ensemble_destroy", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_ensemble_set_time", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_ensemble_get_time", C.c_int, [C.c_void_p, DP]),
+    ("eprem_gpu_ensemble_autotune", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("eprem_gpu_ensemble_step", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_ensemble_synchronize", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_ensemble_stream", C.c_void_p, [C.c_void_p]),
+    ("eprem_gpu_gemm_bf16", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_void_p]),
     ("eprem_gpu_last_error", C.c_char_p, []),
 ]
 
@@ -225,3 +240,72 @@ class EpremRun:
     @property
     def kernel_launches(self) -> int:
         return int(self.lib.eprem_gpu_kernel_launches(self.handle))
+
+    # -- synthetic state and tuning (no reference counterpart) ----------------
+    def init_seed_population(self, seed: int, perturbation: float):
+        """f = seed function x (1 + perturbation U(-1,1)) built on the device."""
+        self._check(self.lib.eprem_gpu_init_seed_population(self.handle, int(seed),
+                                                             float(perturbation)))
+
+    def autotune(self) -> int:
+        """Time the streaming shapes on a scratch copy and keep the fastest."""
+        v = C.c_int()
+        self._check(self.lib.eprem_gpu_autotune(self.handle, C.byref(v)))
+        return v.value
+
+    def set_stream_variant(self, variant: int):
+        self._check(self.lib.eprem_gpu_set_stream_variant(self.handle, int(variant)))
+
+
+class Ensemble:
+    """Independent runs stepped together: one CUDA-graph launch per step
+    (moveNodes, updateMhd at t + tDel, updateEnergeticParticles for every
+    run).  The runs stay usable on their own after synchronize()."""
+
+    def __init__(self, runs: list[EpremRun]):
+        self.lib = load_library()
+        self.runs = list(runs)
+        arr = (C.c_void_p * len(runs))(*[r.handle.value for r in runs])
+        h = C.c_void_p()
+        self._check(self.lib.eprem_gpu_ensemble_create(arr, len(runs), C.byref(h)))
+        self.handle = h
+
+    def _check(self, rc: int):
+        if rc != abi.EPREM_GPU_OK:
+            raise EpremGpuError(rc, self.lib.eprem_gpu_last_error().decode())
+
+    def set_time(self, t):
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64),
+                                                 (len(self.runs),)))
+        self._check(self.lib.eprem_gpu_ensemble_set_time(self.handle, _dp(t)))
+
+    def get_time(self) -> np.ndarray:
+        out = np.empty(len(self.runs))
+        self._check(self.lib.eprem_gpu_ensemble_get_time(self.handle, _dp(out)))
+        return out
+
+    def autotune(self) -> list[int]:
+        out = (C.c_int * len(self.runs))()
+        self._check(self.lib.eprem_gpu_ensemble_autotune(self.handle, out))
+        return list(out)
+
+    def step(self):
+        self._check(self.lib.eprem_gpu_ensemble_step(self.handle))
+
+    def synchronize(self):
+        self._check(self.lib.eprem_gpu_ensemble_synchronize(self.handle))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.eprem_gpu_ensemble_stream(self.handle)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eprem_gpu_ensemble_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

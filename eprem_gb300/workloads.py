@@ -481,3 +481,33 @@ def mas_workload(streams_rows=2, streams_cols=2, nodes=60, energies=12, mu=8, r_
     return Workload(name or f"mas {6 * streams_rows * streams_cols}x{nodes}x{energies}x{mu}",
                     streams_rows, streams_cols, nodes, energies, mu, 0.1, 100.0, r_min_au,
                     r_max_au, p)
+
+
+def ensemble_members(n: int = 64, seed: int = 20240607) -> list[Workload]:
+    """The batched-ensemble workload: n independent runs with uneven sizes and
+    parameters drawn from splitmix64(seed) -- streams 6 r^2 with r log-uniform
+    in [2, 16] (24-1536 streams), 400-2000 nodes, 20-50 energies, 20-40 mu
+    cells, seed-spectrum index -[2.5, 4], lambda_parallel 0.05-1 AU at 1 GV,
+    and an ideal shock (a CME-driven front in the analytic wind, 30-degree
+    half-width) at 800-2500 km/s."""
+    u = 0.5 * (uniform_pm1(seed, 8 * n).reshape(n, 8) + 1.0)  # U(0, 1)
+    out = []
+    for i in range(n):
+        r = int(round(2.0 * 8.0 ** u[i, 0]))
+        nodes = 400 + int(u[i, 1] * 1600.999)
+        E = 20 + int(u[i, 2] * 30.999)
+        M = 20 + int(u[i, 3] * 20.999)
+        p = _plain_wind_params()
+        p.bf_gamma = 2.5 + 1.5 * u[i, 4]
+        p.lamo = 0.05 + 0.95 * u[i, 5]
+        p.ideal_shock = 1
+        p.ideal_shock_speed = (800.0 + 1700.0 * u[i, 6]) * 1e5
+        p.ideal_shock_jump = 2.9
+        p.ideal_shock_init_time = 0.0
+        p.ideal_shock_theta = PI / 2
+        p.ideal_shock_phi = 2.0 * PI * u[i, 7]
+        p.ideal_shock_width = 2.0 * math.radians(30.0)
+        w = Workload(f"member {i}: {6 * r * r}x{nodes}x{E}x{M}", r, r, nodes, E, M, 0.1,
+                     1000.0, 0.05, 5.0, p, seed=seed + i)
+        out.append(w)
+    return out

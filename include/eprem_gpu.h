@@ -351,6 +351,62 @@ int eprem_gpu_read_kernel_timing(eprem_gpu_run *run, eprem_kernel_time_t *out);
  * kernels above are held against.  No reference counterpart. */
 int eprem_gpu_alu_peak(int precision, double *tflops);
 
+/* ---- Synthetic state, autotuning and ensembles ----------------------------
+ * None of these has a counterpart in the reference, which runs one
+ * simulation per process, seeds f by spawning shells and has one kernel
+ * shape per operator. */
+
+/* f = sepSeedFunction(E, r) (src/energeticParticlesBoundary.c:67-116) times
+ * (1 + perturbation U(-1,1)) per (stream, node, energy), isotropic in mu, at
+ * the current node positions; U is the top 53 bits of splitmix64(seed) at
+ * index (stream*N + node)*E + energy + 1.  Builds large synthetic states on
+ * the device without a host copy of f.  Synchronizes. */
+int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double perturbation);
+
+/* Time the streaming-kernel shapes that fit this run (FP32 form: variants 3,
+ * 2, 1 of eprem_params_t.stream_variant) on a scratch copy of its first 96
+ * streams and keep the fastest; *chosen_variant receives it.  The run's f
+ * and statistics are not touched.  The FP64 form has one shape.  Allocates
+ * and frees scratch; synchronizes. */
+int eprem_gpu_autotune(eprem_gpu_run *run, int *chosen_variant);
+/* Force a streaming-kernel shape (EPREM_GPU_ERR_ARG if it does not fit). */
+int eprem_gpu_set_stream_variant(eprem_gpu_run *run, int variant);
+
+/* A set of independent runs (different sizes and parameters allowed, all on
+ * the current device, analytic background) stepped together.  The first
+ * eprem_gpu_ensemble_step captures one driver step of every run --
+ * moveNodes(tDel), updateMhd(t + tDel), updateEnergeticParticles, t += tDel,
+ * the order of src/eprem.c:620-671 -- into one CUDA graph with one branch per
+ * run; each later step is one launch of that graph.  Each run's time t lives
+ * on the device (set_time / get_time, zero at creation).  Until
+ * eprem_gpu_ensemble_synchronize returns, the member runs must not be used
+ * on their own.  Failures inside a step are reported by synchronize, with the
+ * first failing run's status. */
+typedef struct eprem_gpu_ensemble eprem_gpu_ensemble;
+int eprem_gpu_ensemble_create(eprem_gpu_run *const *runs, int num_runs,
+                              eprem_gpu_ensemble **out);
+int eprem_gpu_ensemble_destroy(eprem_gpu_ensemble *ens);
+int eprem_gpu_ensemble_set_time(eprem_gpu_ensemble *ens, const double *t_global);
+int eprem_gpu_ensemble_get_time(eprem_gpu_ensemble *ens, double *t_global);
+/* Autotune one run per size class (precision, mu bin, cluster shape) and give
+ * its choice to the others of the class; chosen_variants (may be NULL)
+ * receives one variant per run.  The next step captures a new graph. */
+int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *ens, int *chosen_variants);
+int eprem_gpu_ensemble_step(eprem_gpu_ensemble *ens);
+int eprem_gpu_ensemble_synchronize(eprem_gpu_ensemble *ens);
+/* The cudaStream_t the graph launches on (as void*). */
+void *eprem_gpu_ensemble_stream(eprem_gpu_ensemble *ens);
+
+/* ---- Learned surrogate building blocks (no reference counterpart) ---------
+ * c[m x n] = a[m x k] * bt[n x k]^T (+ bias[n]) on the tensor cores
+ * (tcgen05, bf16 operands, fp32 accumulation in tensor memory).  Device
+ * pointers: a, bt bf16 with k contiguous (lda, ldb >= k, multiples of 8), c
+ * fp32 (ldc >= n), bias fp32 or NULL; k a multiple of 8.  Runs on `stream`
+ * (a cudaStream_t, NULL for the default stream) and synchronizes it.
+ * EPREM_GPU_ERR_CUDA if a wait on the tensor cores timed out. */
+int eprem_gpu_gemm_bf16(const void *a, int lda, const void *bt, int ldb, const float *bias,
+                        float *c, int ldc, int m, int n, int k, void *stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *eprem_gpu_last_error(void);
 

@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "eprem_gpu.h")
 
 def header_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(eprem_gpu_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(eprem_gpu_[a-z0-9_]+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
