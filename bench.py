@@ -37,6 +37,14 @@ METRIC = "cell-updates/s (node*E*mu) plain FP64 vs chosen form at <=1e-3 rel flu
 UNIT = "cell-updates/s"
 FLOPS_PER_CELL_SUBCYCLE = {"stream": 8.0, "focus": 11.0, "change": 11.0}
 BYTES_PER_CELL_UPDATE = {"fp64": 32.0, "fp32": 16.0}
+# DRAM bytes (read + write) per cell per launch of the dominant kernel, from
+# one ncu capture of the 96-stream subset (profiles/k_stream2_fp32_96streams.txt,
+# profiles/k_stream_fp64_96streams.txt, profiles/k_focus32_k_change32_fp32_96streams.txt):
+# traffic per launch / 96*1000*50*40 cells; traffic grows with the number of
+# (stream, energy) slabs, so it scales to a full launch by the cells processed.
+NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1503.2466e6 / 192e6,
+                           ("stream", "fp64"): 3054.831e6 / 192e6,
+                           ("node", "fp32"): 1488.048e6 / 192e6}
 
 
 # ---------------------------------------------------------------------------
@@ -57,6 +65,8 @@ def parse():
     ap.add_argument("--ensemble-runs", type=int, default=8,
                     help="members of the 64-run batched ensemble to step (first n)")
     ap.add_argument("--ensemble-steps", type=int, default=2)
+    ap.add_argument("--skip-surrogate", action="store_true")
+    ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     ap.add_argument("--mas-steps", type=int, default=2)
     ap.add_argument("--profile-step", choices=["fp32", "fp64"], default=None,
                     help="run one EP sub-step of the 96-stream subset and exit "
@@ -241,7 +251,10 @@ def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
         "achieved": round(achieved, 3), "peak": round(peak_tflops, 3), "unit": "TFLOP/s",
         "frac": round(achieved / peak_tflops, 4),
         "peak_source": "measured FMA-chain kernel on this GPU (eprem_gpu_alu_peak)",
-        "traffic": None,
+        "traffic": (NCU_DRAM_BYTES_PER_CELL[(kind, form)] * cells
+                    if (kind, form) in NCU_DRAM_BYTES_PER_CELL else None),
+        "traffic_unit": "bytes per launch (ncu DRAM read+write, 96-stream capture scaled by cells)",
+        "algorithmic_bytes_per_launch": bytes_per_launch,
         "launches": launches, "mean_launch_ms": round(total_ms / launches, 3),
         "hbm_achieved_gbs": round(bytes_per_launch / mean_s / 1e9, 2),
         "hbm_peak_gbs": hbm_peak,
@@ -420,6 +433,8 @@ def ours(args, rank, ws, dist):
             "flux_rel_err_fp32_vs_fp64": flux_err,
             "flux_err_steps": 2,
         }
+        if not args.skip_surrogate:
+            plain["split_and_surrogate"] = surrogate_case(args, EpremRun, abi, W, j64, sub)
         r64.close()
         r32.close()
 
@@ -645,6 +660,61 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     ens.close()
     for r in runs:
         r.close()
+    return out
+
+
+def surrogate_case(args, EpremRun, abi, W, j64, sub):
+    """The split form and the surrogate form on the 96-stream subset of the
+    precision-at-scale workload: the surrogate is trained on rows of ten
+    successive states of that workload (plain split steps as targets), its
+    residual tolerance calibrated on them, then one step of each form is
+    timed and its flux compared with the FP64 reference form (j64)."""
+    import torch
+    from eprem_gb300.runtime import (NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE, Surrogate,
+                                     set_node_phase, surrogate_counts)
+    t0 = time.perf_counter()
+    src, g, nodes = make_state(sub, abi.EPREM_FP32, EpremRun, abi, W)
+    f0 = host_f(sub, nodes, g, W, pinned=False)
+    src.upload_f(f0)
+    sur = Surrogate(seed=7, chunk_rows=1 << 20)
+    sur.reserve(6_000_000)
+    n = 0
+    t = sub.params.t_del
+    for k in range(10):
+        n = sur.collect(src, rate=0.1, seed=1000 + k)
+        t = step(src, t, sub)
+    src.close()
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    l0 = sur.train(1, 8192, 1e-3)
+    l1 = sur.train(args.surrogate_train_steps, 8192, 1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    tol = sur.calibrate(0.999, 1.5)
+    out = {"samples": n, "collect_s": round(t_collect, 2), "train_steps": args.surrogate_train_steps,
+           "batch": 8192, "train_s": round(t_train, 2), "loss_first": l0, "loss_last": l1,
+           "tolerance": tol}
+    for label, mode in (("split", NODE_PHASE_SPLIT), ("surrogate", NODE_PHASE_SURROGATE)):
+        r, _, _ = make_state(sub, abi.EPREM_FP32, EpremRun, abi, W)
+        r.upload_f(f0)
+        set_node_phase(r, mode, sur if mode == NODE_PHASE_SURROGATE else None)
+        tt = step(r, sub.params.t_del, sub)
+        r.synchronize()
+        ms, _, kt, _, _ = timed_steps(r, sub, 1, tt)
+        j = r.omni_flux()
+        mask = j64 > 1e-30 * j64.max()
+        cu = sub.cells * sub.params.num_ep_steps
+        entry = {"value": cu / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                 "node_phase_ms": kt["node"][1],
+                 "flux_rel_err_vs_fp64_reference_form":
+                     float(np.max(np.abs(j[mask] - j64[mask]) / j64[mask]))}
+        if mode == NODE_PHASE_SURROGATE:
+            kept, fb = surrogate_counts(r)
+            entry["rows_kept"] = kept
+            entry["rows_fallback"] = fb
+        out[label] = entry
+        r.close()
+    sur.close()
     return out
 
 

@@ -80,6 +80,7 @@ struct RunView {
   int num_ep_steps, max_subcycles;
   int check_seed, use_bc, use_stream, use_focus, use_change;
   int focus_alg, change_alg;
+  int relax_in_stream;     // 0 in the split form (relaxation with the focusing, node phase)
 };
 
 __device__ __forceinline__ double *node_field(const RunView &r, int field) {

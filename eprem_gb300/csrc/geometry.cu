@@ -158,6 +158,10 @@ int launch_geometry(const RunView &r, cudaStream_t st, double norm_radius, doubl
   if (blocks > 152 * 32) blocks = 152 * 32;
   k_node_prep<<<blocks, 256, 0, st>>>(r, norm_radius, neg_beta, mfp_type, mfp_power, bs_au);
   size_t smem = (size_t)r.N * (3 * sizeof(double) + sizeof(int));
+  // per launch: runs of different sizes share the kernel's attribute
+  if (cudaFuncSetAttribute(k_stream_list, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return EPREM_GPU_ERR_CUDA;
   k_stream_list<<<r.S, 32, smem, st>>>(r);
   *launches += 2;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;

@@ -83,4 +83,29 @@ int launch_mas_move_nodes(const RunView &r, const MasView &mv, double dt, cudaSt
 int launch_gemm_bf16(const void *A, int lda, const void *Bt, int ldb, const float *bias,
                      float *C, int ldc, int M, int N, int K, int *err, cudaStream_t st);
 
+// surrogate.cu -- split focusing + relaxation step and the learned surrogate
+// (40 mu cells, FP32 form); row ranges [row0, row0 + nrows) of the S*N*E rows
+int launch_split_focus_relax(const RunView &r, size_t row0, size_t nrows, const uint8_t *mask,
+                             cudaStream_t st, uint64_t *launches);
+int launch_surr_sample(const RunView &r, float *xs, float *ts, unsigned long long *count,
+                       unsigned long long cap, unsigned long long seed, float rate,
+                       cudaStream_t st);
+int launch_surr_features(const RunView &r, size_t row0, size_t nrows, void *X, cudaStream_t st,
+                         uint64_t *launches);
+int launch_surr_apply(const RunView &r, size_t row0, size_t nrows, const float *Y, int ldy,
+                      float tol, uint8_t *reject, unsigned long long *counts, cudaStream_t st,
+                      uint64_t *launches);
+int launch_surr_residual(const float *xs, const float *ts, size_t n, const float *mu32,
+                         float *res, cudaStream_t st);
+int launch_to_bf16(const float *in, void *out, size_t n, cudaStream_t st);
+int launch_gelu_bf16(const float *Z, void *H, size_t n, cudaStream_t st);
+int launch_mse_grad(const float *Y, const float *T, size_t rows, float *dY, void *dYb,
+                    double *loss, cudaStream_t st);
+int launch_gelu_back(const float *dH, const float *Z, float *dZ, void *dZb, size_t n,
+                     cudaStream_t st);
+int launch_transpose_bf16(const void *in, void *out, int R, int C, cudaStream_t st);
+int launch_colsum(const float *in, int R, int C, float *out, cudaStream_t st);
+int launch_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, int step,
+                cudaStream_t st);
+
 }  // namespace eprem

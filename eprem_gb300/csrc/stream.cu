@@ -129,7 +129,7 @@ __global__ void __launch_bounds__((StreamShape<Real, MMAX, RegCoef>::T), 1)
     const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
     const double dsi = r.ds_i[sN + i];
     const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
-    emt = exp(-dtProp / tau);
+    emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;  // split form: node phase relaxes
     const double seedv = seed_value(r, ec, r.seed_radial[gidx]);
     const Real *fp = reinterpret_cast<const Real *>(r.f) + (gidx * r.E + e) * M;
 #pragma unroll

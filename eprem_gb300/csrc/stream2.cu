@@ -103,7 +103,8 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
       const double dsi = r.ds_i[sN + il];
       const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
-      const double emt = exp(-dtProp / tau);
+      // split form: the relaxation runs in the node phase instead
+      const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
       const double seedv = seed_value(r, ec, r.seed_radial[gidx]);
       const float seedf = to_real<float>(seedv);
       const float *fp = reinterpret_cast<const float *>(r.f) + (gidx * r.E + e) * M;

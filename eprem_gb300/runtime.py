@@ -21,6 +21,7 @@ from . import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libeprem_gpu.so")
 DP = C.POINTER(C.c_double)
+FP = C.POINTER(C.c_float)
 
 # Every entry point of include/eprem_gpu.h: (name, restype, argtypes)
 EXPORTS = [
@@ -63,6 +64,25 @@ EXPORTS = [
     ("eprem_gpu_gemm_bf16", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_void_p]),
+    ("eprem_gpu_surrogate_create", C.c_int, [C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]),
+    ("eprem_gpu_surrogate_destroy", C.c_int, [C.c_void_p]),
+    ("eprem_gpu_surrogate_num_params", C.c_int64, []),
+    ("eprem_gpu_surrogate_get_params", C.c_int, [C.c_void_p, FP, C.c_int64]),
+    ("eprem_gpu_surrogate_set_params", C.c_int, [C.c_void_p, FP, C.c_int64]),
+    ("eprem_gpu_surrogate_reserve", C.c_int, [C.c_void_p, C.c_int64]),
+    ("eprem_gpu_surrogate_collect", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_uint64,
+                                              C.POINTER(C.c_int64)]),
+    ("eprem_gpu_surrogate_train", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                            C.POINTER(C.c_double)]),
+    ("eprem_gpu_surrogate_loss_grad", C.c_int, [C.c_void_p, FP, FP, C.c_int,
+                                                C.POINTER(C.c_double), FP]),
+    ("eprem_gpu_surrogate_evaluate", C.c_int, [C.c_void_p, FP, C.c_int, FP]),
+    ("eprem_gpu_surrogate_calibrate", C.c_int, [C.c_void_p, C.c_double, C.c_double,
+                                                C.POINTER(C.c_double)]),
+    ("eprem_gpu_surrogate_set_tolerance", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_set_node_phase", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("eprem_gpu_surrogate_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64),
+                                             C.POINTER(C.c_uint64)]),
     ("eprem_gpu_last_error", C.c_char_p, []),
 ]
 
@@ -309,3 +329,105 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+NODE_PHASE_REFERENCE, NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE = 0, 1, 2
+
+
+def _fp(a: np.ndarray):
+    if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("expected a C-contiguous float32 array")
+    return a.ctypes.data_as(FP)
+
+
+class Surrogate:
+    """The learned focusing + scattering step (MLP 48-256-256-48, bf16 on
+    the tensor cores): training set collection, training, calibration."""
+
+    def __init__(self, seed: int = 1, chunk_rows: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.eprem_gpu_surrogate_create(int(seed), int(chunk_rows), C.byref(h)))
+        self.handle = h
+        self.num_params = int(self.lib.eprem_gpu_surrogate_num_params())
+
+    def _check(self, rc: int):
+        if rc != abi.EPREM_GPU_OK:
+            raise EpremGpuError(rc, self.lib.eprem_gpu_last_error().decode())
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, dtype=np.float32)
+        self._check(self.lib.eprem_gpu_surrogate_get_params(self.handle, _fp(out), out.size))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.lib.eprem_gpu_surrogate_set_params(self.handle, _fp(p), p.size))
+
+    def reserve(self, capacity: int):
+        self._check(self.lib.eprem_gpu_surrogate_reserve(self.handle, int(capacity)))
+
+    def collect(self, run: EpremRun, rate: float, seed: int) -> int:
+        n = C.c_int64()
+        self._check(self.lib.eprem_gpu_surrogate_collect(self.handle, run.handle, float(rate),
+                                                         int(seed), C.byref(n)))
+        return n.value
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        self._check(self.lib.eprem_gpu_surrogate_train(self.handle, int(steps), int(batch),
+                                                       float(lr), C.byref(loss)))
+        return loss.value
+
+    def loss_grad(self, x: np.ndarray, t: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(self.num_params, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.eprem_gpu_surrogate_loss_grad(self.handle, _fp(x), _fp(t),
+                                                           x.shape[0], C.byref(loss), _fp(g)))
+        return loss.value, g
+
+    def evaluate(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((x.shape[0], 48), dtype=np.float32)
+        self._check(self.lib.eprem_gpu_surrogate_evaluate(self.handle, _fp(x), x.shape[0],
+                                                          _fp(y)))
+        return y
+
+    def calibrate(self, quantile: float = 0.999, margin: float = 1.5) -> float:
+        tol = C.c_double()
+        self._check(self.lib.eprem_gpu_surrogate_calibrate(self.handle, float(quantile),
+                                                           float(margin), C.byref(tol)))
+        return tol.value
+
+    def set_tolerance(self, tol: float):
+        self._check(self.lib.eprem_gpu_surrogate_set_tolerance(self.handle, float(tol)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eprem_gpu_surrogate_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_node_phase(run: EpremRun, mode: int, surrogate: Surrogate | None = None):
+    lib = load_library()
+    rc = lib.eprem_gpu_set_node_phase(run.handle, int(mode),
+                                      surrogate.handle if surrogate is not None else None)
+    if rc != abi.EPREM_GPU_OK:
+        raise EpremGpuError(rc, lib.eprem_gpu_last_error().decode())
+
+
+def surrogate_counts(run: EpremRun) -> tuple[int, int]:
+    lib = load_library()
+    k, f = C.c_uint64(), C.c_uint64()
+    rc = lib.eprem_gpu_surrogate_counts(run.handle, C.byref(k), C.byref(f))
+    if rc != abi.EPREM_GPU_OK:
+        raise EpremGpuError(rc, lib.eprem_gpu_last_error().decode())
+    return k.value, f.value

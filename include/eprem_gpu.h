@@ -407,6 +407,68 @@ void *eprem_gpu_ensemble_stream(eprem_gpu_ensemble *ens);
 int eprem_gpu_gemm_bf16(const void *a, int lda, const void *bt, int ldb, const float *bias,
                         float *c, int ldc, int m, int n, int k, void *stream);
 
+/* ---- Split form and the learned surrogate (no reference counterpart) -------
+ * Node phase of each EP sub-step:
+ *   REFERENCE  the reference's scheme: relaxation inside every streaming
+ *              sub-cycle, then focusing and adiabatic change;
+ *   SPLIT      streaming without relaxation; per (node, energy) row the
+ *              focusing sub-cycles and then one exact relaxation over the
+ *              sub-step, f = iso + (f - iso) exp(-dt/tau); adiabatic change;
+ *   SURROGATE  as SPLIT, with the row step predicted by the surrogate MLP,
+ *              projected to conserve sum_mu f exactly (FP64 sums), and
+ *              recomputed by the SPLIT kernel wherever its Crank-Nicolson
+ *              residual exceeds the surrogate's tolerance.
+ * SPLIT and SURROGATE need the FP32 form with Euler operators, focusing on
+ * and 40 mu cells.  They change the reference's operator splitting: their
+ * flux error against the FP64 reference form is measured and reported. */
+enum {
+  EPREM_NODE_PHASE_REFERENCE = 0,
+  EPREM_NODE_PHASE_SPLIT = 1,
+  EPREM_NODE_PHASE_SURROGATE = 2
+};
+typedef struct eprem_gpu_surrogate eprem_gpu_surrogate;
+
+/* MLP 48 -> 256 -> 256 -> 48 (tanh-form GELU), bf16 weights and fp32
+ * accumulation on the tensor cores; fp32 master parameters, Adam.  Inputs:
+ * ln f(mu) minus its mean (40), asinh(a dt/dmu), asinh(b dt/dmu), 1 -
+ * exp(-dt/tau), zero padding; outputs: the change of ln f(mu) (40 used).
+ * chunk_rows: rows per inference chunk (device buffers ~2.3 KB per row;
+ * 0 = 524288).  Weights start Xavier-uniform from splitmix64(seed). */
+int eprem_gpu_surrogate_create(uint64_t seed, int chunk_rows, eprem_gpu_surrogate **out);
+int eprem_gpu_surrogate_destroy(eprem_gpu_surrogate *s);
+/* Parameters, fp32, flat: W1[256][48], b1[256], W2[256][256], b2[256],
+ * W3[48][256], b3[48] (weights as [out][in]). */
+int64_t eprem_gpu_surrogate_num_params(void);
+int eprem_gpu_surrogate_get_params(eprem_gpu_surrogate *s, float *params, int64_t n);
+int eprem_gpu_surrogate_set_params(eprem_gpu_surrogate *s, const float *params, int64_t n);
+/* Training set: room for `capacity` rows (emptied); collect adds the rows of
+ * the run's current state chosen at `rate` by a hash of (seed, row), each
+ * with its SPLIT step as the target; *total = rows held. */
+int eprem_gpu_surrogate_reserve(eprem_gpu_surrogate *s, int64_t capacity);
+int eprem_gpu_surrogate_collect(eprem_gpu_surrogate *s, eprem_gpu_run *run, double rate,
+                                uint64_t seed, int64_t *total);
+/* `steps` Adam steps (learning rate lr) on random windows of `batch` rows
+ * (a multiple of 8, <= 16384) by the library's forward and backward
+ * kernels; *last_loss = mean squared error of the last batch. */
+int eprem_gpu_surrogate_train(eprem_gpu_surrogate *s, int steps, int batch, double lr,
+                              double *last_loss);
+/* One forward and backward pass on host rows (x: rows x 48, t: rows x 40,
+ * rows a multiple of 8, <= 16384): mean squared error and its gradient in
+ * the parameter layout above; no update.  evaluate: outputs y (rows x 48). */
+int eprem_gpu_surrogate_loss_grad(eprem_gpu_surrogate *s, const float *x, const float *t,
+                                  int rows, double *loss, float *grad);
+int eprem_gpu_surrogate_evaluate(eprem_gpu_surrogate *s, const float *x, int rows, float *y);
+/* Residual tolerance: the `quantile` of the collected plain rows' residuals
+ * times `margin`; or set directly. */
+int eprem_gpu_surrogate_calibrate(eprem_gpu_surrogate *s, double quantile, double margin,
+                                  double *tol);
+int eprem_gpu_surrogate_set_tolerance(eprem_gpu_surrogate *s, double tol);
+/* Choose the node phase of a run (the surrogate for SURROGATE, else NULL). */
+int eprem_gpu_set_node_phase(eprem_gpu_run *run, int mode, eprem_gpu_surrogate *s);
+/* Rows the surrogate kept and rows recomputed by the plain kernel since the
+ * node phase was set. */
+int eprem_gpu_surrogate_counts(eprem_gpu_run *run, uint64_t *kept, uint64_t *fallback);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *eprem_gpu_last_error(void);
 

@@ -31,7 +31,8 @@ def _start(w, orc, precision):
 @pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
 def test_ensemble_step_equals_individual_steps(oracle_lib, precision):
     ws = _members()
-    t0 = [w.params.t_del, 2 * w.params.t_del, 3 * w.params.t_del]
+    td = ws[0].params.t_del
+    t0 = [td, 2 * td, 3 * td]
     single = [_start(w, oracle_lib, precision) for w in ws]
     batched = [_start(w, oracle_lib, precision) for w in ws]
     for run, w, t in zip(single, ws, t0):
