@@ -664,13 +664,18 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
 
 
 def surrogate_case(args, EpremRun, abi, W, j64, sub):
-    """The split form and the surrogate form on the 96-stream subset of the
-    precision-at-scale workload: the surrogate is trained on rows of ten
-    successive states of that workload (plain split steps as targets), its
-    residual tolerance calibrated on them, then one step of each form is
-    timed and its flux compared with the FP64 reference form (j64)."""
+    """The learned focusing step and the split form on the 96-stream subset
+    of the precision-at-scale workload.  The surrogate is trained on rows of
+    ten successive states (the plain focusing of each row as the target), its
+    residual tolerance calibrated on them; then one step of each form is
+    timed and its flux compared with the FP64 reference form (j64):
+      * surrogate_focus: the reference's scheme, focusing by the surrogate
+        (rows failing the residual check by the plain kernel);
+      * split: relaxation moved from the streaming sub-cycles to one exact
+        step after the focusing (plain kernels) -- a change of the operator
+        splitting, reported for its error."""
     import torch
-    from eprem_gb300.runtime import (NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE, Surrogate,
+    from eprem_gb300.runtime import (NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE_FOCUS, Surrogate,
                                      set_node_phase, surrogate_counts)
     t0 = time.perf_counter()
     src, g, nodes = make_state(sub, abi.EPREM_FP32, EpremRun, abi, W)
@@ -694,10 +699,10 @@ def surrogate_case(args, EpremRun, abi, W, j64, sub):
     out = {"samples": n, "collect_s": round(t_collect, 2), "train_steps": args.surrogate_train_steps,
            "batch": 8192, "train_s": round(t_train, 2), "loss_first": l0, "loss_last": l1,
            "tolerance": tol}
-    for label, mode in (("split", NODE_PHASE_SPLIT), ("surrogate", NODE_PHASE_SURROGATE)):
+    for label, mode in (("surrogate_focus", NODE_PHASE_SURROGATE_FOCUS), ("split", NODE_PHASE_SPLIT)):
         r, _, _ = make_state(sub, abi.EPREM_FP32, EpremRun, abi, W)
         r.upload_f(f0)
-        set_node_phase(r, mode, sur if mode == NODE_PHASE_SURROGATE else None)
+        set_node_phase(r, mode, sur if mode == NODE_PHASE_SURROGATE_FOCUS else None)
         tt = step(r, sub.params.t_del, sub)
         r.synchronize()
         ms, _, kt, _, _ = timed_steps(r, sub, 1, tt)
@@ -708,7 +713,7 @@ def surrogate_case(args, EpremRun, abi, W, j64, sub):
                  "node_phase_ms": kt["node"][1],
                  "flux_rel_err_vs_fp64_reference_form":
                      float(np.max(np.abs(j[mask] - j64[mask]) / j64[mask]))}
-        if mode == NODE_PHASE_SURROGATE:
+        if mode == NODE_PHASE_SURROGATE_FOCUS:
             kept, fb = surrogate_counts(r)
             entry["rows_kept"] = kept
             entry["rows_fallback"] = fb

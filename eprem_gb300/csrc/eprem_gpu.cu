@@ -708,7 +708,7 @@ extern "C" int eprem_gpu_init_seed_population(eprem_gpu_run *r, uint64_t seed,
 // streams (the kernel that takes 90 % of a step) and keeps the fastest.  The
 // copy has its own status block, so the run's statistics are untouched.
 namespace {
-constexpr int kTuneVariants[] = {3, 2, 1};
+constexpr int kTuneVariants[] = {4, 3, 2, 1};
 
 int tune_stream(eprem_gpu_run *r, int *chosen) {
   const eprem_params_t &p = r->params;
@@ -842,7 +842,7 @@ extern "C" int eprem_gpu_ensemble_create(eprem_gpu_run *const *runs, int n,
     if (runs[i]->mas_ready)
       return fail(EPREM_GPU_ERR_UNSUPPORTED,
                   "ensemble steps use the analytic background; MAS runs step one by one");
-    if (runs[i]->node_mode == EPREM_NODE_PHASE_SURROGATE)
+    if (runs[i]->surr)
       return fail(EPREM_GPU_ERR_UNSUPPORTED, "surrogate-form runs step one by one");
     for (int j = 0; j < i; j++)
       if (runs[j] == runs[i]) return fail(EPREM_GPU_ERR_ARG, "run listed twice in ensemble");
@@ -1439,11 +1439,13 @@ extern "C" int eprem_gpu_set_node_phase(eprem_gpu_run *r, int mode, eprem_gpu_su
     r->surr = nullptr;
     return EPREM_GPU_OK;
   }
-  if (mode != EPREM_NODE_PHASE_SPLIT && mode != EPREM_NODE_PHASE_SURROGATE)
+  if (mode != EPREM_NODE_PHASE_SPLIT && mode != EPREM_NODE_PHASE_SURROGATE &&
+      mode != EPREM_NODE_PHASE_SURROGATE_FOCUS)
     return fail(EPREM_GPU_ERR_ARG, "unknown node phase");
   const int rc = surr_check_run(r);
   if (rc) return rc;
-  if (mode == EPREM_NODE_PHASE_SURROGATE) {
+  const bool surrogate = mode != EPREM_NODE_PHASE_SPLIT;
+  if (surrogate) {
     if (!s) return fail(EPREM_GPU_ERR_ARG, "the surrogate form needs a surrogate");
     if (s->device != r->device) return fail(EPREM_GPU_ERR_ARG, "surrogate on another device");
     if (!r->d_surr_counts) CK(cudaMalloc(&r->d_surr_counts, 2 * sizeof(unsigned long long)));
@@ -1452,8 +1454,8 @@ extern "C" int eprem_gpu_set_node_phase(eprem_gpu_run *r, int mode, eprem_gpu_su
     CK(cudaStreamSynchronize(r->stream));
   }
   r->node_mode = mode;
-  r->v.relax_in_stream = 0;
-  r->surr = mode == EPREM_NODE_PHASE_SURROGATE ? s : nullptr;
+  r->v.relax_in_stream = mode == EPREM_NODE_PHASE_SURROGATE_FOCUS ? 1 : 0;
+  r->surr = surrogate ? s : nullptr;
   return EPREM_GPU_OK;
 }
 

@@ -280,10 +280,14 @@ static int threads_for(int mmax) {
 }
 
 // variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
-// 3 several list nodes per thread (stream2.cu).  The FP64 form always keeps the
+// 3 several list nodes per thread (stream2.cu), 4 the same with packed fp32x2
+// arithmetic (even cell counts per mu half).  The FP64 form always keeps the
 // coefficients in shared memory; the automatic FP32 choice is variant 3.
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
-  if (precision == EPREM_FP32 && (variant == 0 || variant == 3) && plan_stream2(N, M, m0, plan) == 0)
+  if (precision == EPREM_FP32 && variant == 4 && plan_stream2(N, M, m0, true, plan) == 0)
+    return 0;
+  if (precision == EPREM_FP32 && (variant == 0 || variant == 3) &&
+      plan_stream2(N, M, m0, false, plan) == 0)
     return 0;
   int mmax = 0;
   for (int b : kStreamBins)

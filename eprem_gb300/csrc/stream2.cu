@@ -42,7 +42,10 @@ constexpr size_t stream2_smem_bytes() {
   return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
 }
 
-template <int MMAX>
+// PACK: the upwind and relaxation arithmetic on pairs of mu cells with the
+// packed fp32x2 instructions (two cells per instruction, the same roundings as
+// the scalar fused multiply-adds); needs an even number of cells per half.
+template <int MMAX, bool PACK>
 __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr int NPT = Stream2Shape<MMAX>::NPT;
@@ -177,50 +180,126 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       __syncthreads();
     const float *my_hi = hi(p, warp);
     const float *my_lo = lo(p, warp + 1);
-    float acc[NPT];
+    if constexpr (PACK) {
+      const float2 neg1 = make_float2(-1.f, -1.f);
+      float2 acc2[NPT];
 #pragma unroll
-    for (int q = 0; q < NPT; ++q) acc[q] = 0.f;
-    // mu < 0: upwind from the outer neighbour (list node + 1), old values
+      for (int q = 0; q < NPT; ++q) acc2[q] = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int j = 0; j < H; ++j) {
-      if (j < nL) {
-        float del = dl0 + (float)j * ddel;
-        // opaque to loop-invariant code motion: otherwise the compiler hoists
-        // every mult*del product out of the sub-cycle loop into registers
-        asm volatile("" : "+f"(del));
-        float nb = __shfl_down_sync(FULL, Lf[0][j], 1);
-        if (lane == 31) nb = my_lo[j];
+      for (int h = 0; h < H / 2; ++h) {
+        const int j = 2 * h;
+        if (j < nL) {
+          float d0 = dl0 + (float)j * ddel, d1 = dl0 + (float)(j + 1) * ddel;
+          asm volatile("" : "+f"(d0), "+f"(d1));
+          const float2 del2 = make_float2(d0, d1);
+          float nb0 = __shfl_down_sync(FULL, Lf[0][j], 1);
+          float nb1 = __shfl_down_sync(FULL, Lf[0][j + 1], 1);
+          if (lane == 31) {
+            nb0 = my_lo[j];
+            nb1 = my_lo[j + 1];
+          }
 #pragma unroll
-        for (int q = 0; q < NPT; ++q) {
-          const float right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][j] : nb;
-          Lf[q][j] = Lf[q][j] + (mlo[q] * del) * (Lf[q][j] - right);
-          acc[q] += Lf[q][j];
+          for (int q = 0; q < NPT; ++q) {
+            const int qn = q + 1 < NPT ? q + 1 : q;
+            const float2 cur = make_float2(Lf[q][j], Lf[q][j + 1]);
+            const float2 right =
+                (q + 1 < NPT) ? make_float2(Lf[qn][j], Lf[qn][j + 1]) : make_float2(nb0, nb1);
+            const float2 c2 = __fmul2_rn(make_float2(mlo[q], mlo[q]), del2);
+            const float2 nw = __ffma2_rn(c2, __ffma2_rn(right, neg1, cur), cur);
+            Lf[q][j] = nw.x;
+            Lf[q][j + 1] = nw.y;
+            acc2[q] = __fadd2_rn(acc2[q], nw);
+          }
         }
       }
-    }
-    // mu >= 0: upwind from the inner neighbour (list node - 1), old values
 #pragma unroll
-    for (int j = 0; j < H; ++j) {
-      if (j < nR) {
-        float del = dr0 + (float)j * ddel;
-        asm volatile("" : "+f"(del));
-        float nb = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
-        if (lane == 0) nb = my_hi[j];
+      for (int h = 0; h < H / 2; ++h) {
+        const int j = 2 * h;
+        if (j < nR) {
+          float d0 = dr0 + (float)j * ddel, d1 = dr0 + (float)(j + 1) * ddel;
+          asm volatile("" : "+f"(d0), "+f"(d1));
+          const float2 del2 = make_float2(d0, d1);
+          float nb0 = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
+          float nb1 = __shfl_up_sync(FULL, Rf[NPT - 1][j + 1], 1);
+          if (lane == 0) {
+            nb0 = my_hi[j];
+            nb1 = my_hi[j + 1];
+          }
 #pragma unroll
-        for (int q = NPT - 1; q >= 0; --q) {
-          const float left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][j] : nb;
-          Rf[q][j] = Rf[q][j] + (mhi[q] * del) * (left - Rf[q][j]);
-          acc[q] += Rf[q][j];
+          for (int q = NPT - 1; q >= 0; --q) {
+            const int qp = q > 0 ? q - 1 : 0;
+            const float2 cur = make_float2(Rf[q][j], Rf[q][j + 1]);
+            const float2 left =
+                (q > 0) ? make_float2(Rf[qp][j], Rf[qp][j + 1]) : make_float2(nb0, nb1);
+            const float2 c2 = __fmul2_rn(make_float2(mhi[q], mhi[q]), del2);
+            const float2 nw = __ffma2_rn(c2, __ffma2_rn(cur, neg1, left), cur);
+            Rf[q][j] = nw.x;
+            Rf[q][j + 1] = nw.y;
+            acc2[q] = __fadd2_rn(acc2[q], nw);
+          }
         }
       }
-    }
 #pragma unroll
-    for (int q = 0; q < NPT; ++q) {
-      const float iso = (inv_m * acc[q]) * om[q];
+      for (int q = 0; q < NPT; ++q) {
+        const float iso = (inv_m * (acc2[q].x + acc2[q].y)) * om[q];
+        const float2 iso2 = make_float2(iso, iso), em2 = make_float2(em[q], em[q]);
 #pragma unroll
+        for (int h = 0; h < H / 2; ++h) {
+          const int j = 2 * h;
+          const float2 a = __ffma2_rn(make_float2(Lf[q][j], Lf[q][j + 1]), em2, iso2);
+          const float2 b = __ffma2_rn(make_float2(Rf[q][j], Rf[q][j + 1]), em2, iso2);
+          Lf[q][j] = a.x;
+          Lf[q][j + 1] = a.y;
+          Rf[q][j] = b.x;
+          Rf[q][j + 1] = b.y;
+        }
+      }
+    } else {
+      float acc[NPT];
+  #pragma unroll
+      for (int q = 0; q < NPT; ++q) acc[q] = 0.f;
+      // mu < 0: upwind from the outer neighbour (list node + 1), old values
+  #pragma unroll
       for (int j = 0; j < H; ++j) {
-        Lf[q][j] = Lf[q][j] * em[q] + iso;
-        Rf[q][j] = Rf[q][j] * em[q] + iso;
+        if (j < nL) {
+          float del = dl0 + (float)j * ddel;
+          // opaque to loop-invariant code motion: otherwise the compiler hoists
+          // every mult*del product out of the sub-cycle loop into registers
+          asm volatile("" : "+f"(del));
+          float nb = __shfl_down_sync(FULL, Lf[0][j], 1);
+          if (lane == 31) nb = my_lo[j];
+  #pragma unroll
+          for (int q = 0; q < NPT; ++q) {
+            const float right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][j] : nb;
+            Lf[q][j] = Lf[q][j] + (mlo[q] * del) * (Lf[q][j] - right);
+            acc[q] += Lf[q][j];
+          }
+        }
+      }
+      // mu >= 0: upwind from the inner neighbour (list node - 1), old values
+  #pragma unroll
+      for (int j = 0; j < H; ++j) {
+        if (j < nR) {
+          float del = dr0 + (float)j * ddel;
+          asm volatile("" : "+f"(del));
+          float nb = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
+          if (lane == 0) nb = my_hi[j];
+  #pragma unroll
+          for (int q = NPT - 1; q >= 0; --q) {
+            const float left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][j] : nb;
+            Rf[q][j] = Rf[q][j] + (mhi[q] * del) * (left - Rf[q][j]);
+            acc[q] += Rf[q][j];
+          }
+        }
+      }
+  #pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const float iso = (inv_m * acc[q]) * om[q];
+  #pragma unroll
+        for (int j = 0; j < H; ++j) {
+          Lf[q][j] = Lf[q][j] * em[q] + iso;
+          Rf[q][j] = Rf[q][j] * em[q] + iso;
+        }
       }
     }
   }
@@ -259,7 +338,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   if (C > 1) cluster.sync();
 }
 
-int plan_stream2(int N, int M, int m0, StreamPlan *plan) {
+int plan_stream2(int N, int M, int m0, bool packed, StreamPlan *plan) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
@@ -277,15 +356,17 @@ int plan_stream2(int N, int M, int m0, StreamPlan *plan) {
   plan->mmax = mmax;
   plan->threads = T;
   plan->reg_coef = 2;  // marks the several-nodes-per-thread kernel
+  plan->packed = packed ? 1 : 0;
+  if (packed && ((m0 & 1) || ((M - m0) & 1))) return EPREM_GPU_ERR_ARG;  // pairs of cells
   plan->cluster = (N + npt * T - 1) / (npt * T);
   return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
 }
 
-template <int MMAX>
+template <int MMAX, bool PACK>
 static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, cudaStream_t st) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr size_t dyn = stream2_smem_bytes<MMAX>();
-  auto kern = k_stream2<MMAX>;
+  auto kern = k_stream2<MMAX, PACK>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
@@ -301,18 +382,23 @@ static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, cudaS
   return cudaLaunchKernelEx(&cfg, kern, r, m0);
 }
 
+template <bool PACK>
+static cudaError_t launch_mmax(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st) {
+  switch (pl.mmax) {
+    case 8: return launch_stream2_t<8, PACK>(r, pl.cluster, m0, st);
+    case 16: return launch_stream2_t<16, PACK>(r, pl.cluster, m0, st);
+    case 24: return launch_stream2_t<24, PACK>(r, pl.cluster, m0, st);
+    case 32: return launch_stream2_t<32, PACK>(r, pl.cluster, m0, st);
+    case 40: return launch_stream2_t<40, PACK>(r, pl.cluster, m0, st);
+    case 48: return launch_stream2_t<48, PACK>(r, pl.cluster, m0, st);
+    default: return launch_stream2_t<64, PACK>(r, pl.cluster, m0, st);
+  }
+}
+
 int launch_stream2(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st,
                    uint64_t *launches) {
-  cudaError_t err;
-  switch (pl.mmax) {
-    case 8: err = launch_stream2_t<8>(r, pl.cluster, m0, st); break;
-    case 16: err = launch_stream2_t<16>(r, pl.cluster, m0, st); break;
-    case 24: err = launch_stream2_t<24>(r, pl.cluster, m0, st); break;
-    case 32: err = launch_stream2_t<32>(r, pl.cluster, m0, st); break;
-    case 40: err = launch_stream2_t<40>(r, pl.cluster, m0, st); break;
-    case 48: err = launch_stream2_t<48>(r, pl.cluster, m0, st); break;
-    default: err = launch_stream2_t<64>(r, pl.cluster, m0, st); break;
-  }
+  const cudaError_t err = pl.packed ? launch_mmax<true>(r, pl, m0, st)
+                                    : launch_mmax<false>(r, pl, m0, st);
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

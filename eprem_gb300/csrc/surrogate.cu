@@ -1,6 +1,11 @@
 // surrogate.cu -- the split focusing + scattering step and its learned
 // surrogate (no counterpart in the reference).
 //
+// Surrogate of the focusing step.  With the relaxation left inside the
+// streaming sub-cycles (the reference's scheme), the node-phase row step is
+// the focusing alone: the surrogate then changes nothing in the operator
+// splitting.
+//
 // Split form.  The reference relaxes f towards its mu-average inside every
 // streaming sub-cycle (src/energeticParticles.c:2406-2426).  In the split
 // form streaming runs without it, and the node phase applies, per (node, E)
@@ -29,6 +34,11 @@ constexpr int kSurM = 40;
 constexpr int kSurIn = 48;
 constexpr int kSurOut = 48;
 constexpr int kRowThreads = 128;
+// ln f features and ln f changes are clamped: beyond these the row sits at the
+// floor, the network's output is not trusted and the residual check sends the
+// row to the plain kernel
+constexpr float kFeatClamp = 16.f;
+constexpr float kTargetClamp = 8.f;
 
 __device__ __forceinline__ float gelu_f(float z) {
   const float u = 0.7978845608f * (z + 0.044715f * z * z * z);
@@ -56,8 +66,11 @@ __device__ __forceinline__ RowOp row_op(const RunView &r, const NodeCoef32 &c, s
   op.b = c.b;
   op.sc = c.scale_f;
   op.ns = c.ns_f;
+  // relaxation in the node phase only in the split form; in the reference
+  // scheme it stays inside the streaming sub-cycles and the row step is the
+  // focusing alone (e = 1)
   const float tau = vi * ((float)r.ec[e].rig_lamo * (float)r.mfp_node[g]);
-  op.e = expf(-(float)r.dt / tau);
+  op.e = r.relax_in_stream ? 1.f : expf(-(float)r.dt / tau);
   return op;
 }
 
@@ -106,7 +119,7 @@ __device__ __forceinline__ void row_features(const float (&lnf)[kSurM], const Ro
   for (int m = 0; m < kSurM; ++m) mean += lnf[m];
   mean *= 1.f / kSurM;
 #pragma unroll
-  for (int m = 0; m < kSurM; ++m) x[m] = lnf[m] - mean;
+  for (int m = 0; m < kSurM; ++m) x[m] = fminf(fmaxf(lnf[m] - mean, -kFeatClamp), kFeatClamp);
   const float full = op.sc * (float)op.ns;  // dt / dmu
   x[40] = asinhf(op.a * full);
   x[41] = asinhf(op.b * full);
@@ -213,7 +226,8 @@ __global__ void __launch_bounds__(kRowThreads)
 #pragma unroll
   for (int m = 0; m < kSurIn; ++m) xo[m] = x[m];
 #pragma unroll
-  for (int m = 0; m < kSurM; ++m) to[m] = logf(fmaxf(fr[m], FLT_MIN)) - lnf[m];
+  for (int m = 0; m < kSurM; ++m)
+    to[m] = fminf(fmaxf(logf(fmaxf(fr[m], FLT_MIN)) - lnf[m], -kTargetClamp), kTargetClamp);
 }
 
 // ---- inference: features of a chunk of rows ---------------------------------

@@ -331,7 +331,7 @@ class Ensemble:
             pass
 
 
-NODE_PHASE_REFERENCE, NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE = 0, 1, 2
+NODE_PHASE_REFERENCE, NODE_PHASE_SPLIT, NODE_PHASE_SURROGATE, NODE_PHASE_SURROGATE_FOCUS = 0, 1, 2, 3
 
 
 def _fp(a: np.ndarray):

@@ -127,7 +127,8 @@ typedef struct {
                                        with coefficients in registers, 2 one
                                        node per thread with coefficients in
                                        shared memory, 3 several nodes per
-                                       thread                                 */
+                                       thread, 4 as 3 with packed fp32x2
+                                       arithmetic (even cells per mu half)    */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids
@@ -363,8 +364,8 @@ int eprem_gpu_alu_peak(int precision, double *tflops);
  * the device without a host copy of f.  Synchronizes. */
 int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double perturbation);
 
-/* Time the streaming-kernel shapes that fit this run (FP32 form: variants 3,
- * 2, 1 of eprem_params_t.stream_variant) on a scratch copy of its first 96
+/* Time the streaming-kernel shapes that fit this run (FP32 form: variants 4,
+ * 3, 2, 1 of eprem_params_t.stream_variant) on a scratch copy of its first 96
  * streams and keep the fastest; *chosen_variant receives it.  The run's f
  * and statistics are not touched.  The FP64 form has one shape.  Allocates
  * and frees scratch; synchronizes. */
@@ -417,14 +418,20 @@ int eprem_gpu_gemm_bf16(const void *a, int lda, const void *bt, int ldb, const f
  *   SURROGATE  as SPLIT, with the row step predicted by the surrogate MLP,
  *              projected to conserve sum_mu f exactly (FP64 sums), and
  *              recomputed by the SPLIT kernel wherever its Crank-Nicolson
- *              residual exceeds the surrogate's tolerance.
- * SPLIT and SURROGATE need the FP32 form with Euler operators, focusing on
- * and 40 mu cells.  They change the reference's operator splitting: their
- * flux error against the FP64 reference form is measured and reported. */
+ *              residual exceeds the surrogate's tolerance;
+ *   SURROGATE_FOCUS  the reference's scheme (relaxation inside streaming)
+ *              with the focusing sub-cycles predicted by the surrogate,
+ *              projected and checked the same way (fallback: the focusing
+ *              kernel).  The operator splitting is the reference's.
+ * All but REFERENCE need the FP32 form with Euler operators, focusing on and
+ * 40 mu cells.  SPLIT and SURROGATE change the reference's operator
+ * splitting; every form's flux error against the FP64 reference form is
+ * measured and reported. */
 enum {
   EPREM_NODE_PHASE_REFERENCE = 0,
   EPREM_NODE_PHASE_SPLIT = 1,
-  EPREM_NODE_PHASE_SURROGATE = 2
+  EPREM_NODE_PHASE_SURROGATE = 2,
+  EPREM_NODE_PHASE_SURROGATE_FOCUS = 3
 };
 typedef struct eprem_gpu_surrogate eprem_gpu_surrogate;
 
@@ -443,7 +450,9 @@ int eprem_gpu_surrogate_get_params(eprem_gpu_surrogate *s, float *params, int64_
 int eprem_gpu_surrogate_set_params(eprem_gpu_surrogate *s, const float *params, int64_t n);
 /* Training set: room for `capacity` rows (emptied); collect adds the rows of
  * the run's current state chosen at `rate` by a hash of (seed, row), each
- * with its SPLIT step as the target; *total = rows held. */
+ * with the run's plain row step as the target (the focusing alone for a run
+ * in the reference scheme, focusing + relaxation for a split-form run);
+ * *total = rows held. */
 int eprem_gpu_surrogate_reserve(eprem_gpu_surrogate *s, int64_t capacity);
 int eprem_gpu_surrogate_collect(eprem_gpu_surrogate *s, eprem_gpu_run *run, double rate,
                                 uint64_t seed, int64_t *total);

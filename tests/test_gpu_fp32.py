@@ -57,14 +57,15 @@ def test_fp32_sub_cycle_counts_equal_fp64(oracle_lib):
 @pytest.mark.parametrize("nodes", [400, 1100])
 def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
     """The FP32 streaming shapes (one node per thread with register or
-    shared-memory coefficients, several nodes per thread) compute the same
-    update up to float rounding; 1100 nodes needs multi-CTA clusters."""
+    shared-memory coefficients, several nodes per thread, the same with packed
+    fp32x2 arithmetic) compute the same update up to float rounding; 1100
+    nodes needs multi-CTA clusters."""
     w = W.custom(1, 1, nodes, 3, 40, num_ep_steps=2, use_adiabatic_focus=0,
                  use_adiabatic_change=0)
     d, g, f, nodes_arr = primed_state(w, oracle_lib)
     f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes_arr)
     outs = []
-    for variant in (1, 2, 3):
+    for variant in (1, 2, 3, 4):
         w.params.stream_variant = variant
         run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
         run.upload_f(f)
@@ -75,9 +76,9 @@ def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
     w.params.stream_variant = 0
     # FP32 rounding accumulates over the streaming sub-cycles (several
     # hundred at 1100 nodes), most in the far tail of f
-    for v, o in zip((1, 2, 3), outs):
+    for v, o in zip((1, 2, 3, 4), outs):
         err = np.max(np.abs(o - f_ref) / f_ref)
         assert err <= 1e-3, f"variant {v} vs FP64 oracle: {err:.3e}"
-    for v, o in zip((1, 2), outs[:2]):
+    for v, o in zip((1, 2, 4), outs[:2] + outs[3:]):
         err = np.max(np.abs(o - outs[2]) / outs[2])
         assert err <= 1e-4, f"variant {v} vs variant 3: {err:.3e}"
