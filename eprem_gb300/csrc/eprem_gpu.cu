@@ -708,7 +708,7 @@ extern "C" int eprem_gpu_init_seed_population(eprem_gpu_run *r, uint64_t seed,
 // streams (the kernel that takes 90 % of a step) and keeps the fastest.  The
 // copy has its own status block, so the run's statistics are untouched.
 namespace {
-constexpr int kTuneVariants[] = {4, 3, 2, 1};
+constexpr int kTuneVariants[] = {5, 4, 3, 2, 1};
 
 int tune_stream(eprem_gpu_run *r, int *chosen) {
   const eprem_params_t &p = r->params;

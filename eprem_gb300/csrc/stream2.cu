@@ -45,7 +45,9 @@ constexpr size_t stream2_smem_bytes() {
 // PACK: the upwind and relaxation arithmetic on pairs of mu cells with the
 // packed fp32x2 instructions (two cells per instruction, the same roundings as
 // the scalar fused multiply-adds); needs an even number of cells per half.
-template <int MMAX, bool PACK>
+// FILLED: both mu halves fill their MMAX/2 register slots (M = MMAX, m0 = M/2),
+// so every cell guard is known at compile time.
+template <int MMAX, bool PACK, bool FILLED>
 __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr int NPT = Stream2Shape<MMAX>::NPT;
@@ -63,7 +65,8 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   const int e = r.E - 1 - (int)blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int M = r.M, N = r.N;
-  const int nL = m0, nR = M - m0;  // cells moving toward the inner / outer end
+  // cells moving toward the inner / outer end
+  const int nL = FILLED ? H : m0, nR = FILLED ? H : M - m0;
   const int L = r.list_size[s];
   if (L < 3) return;
 
@@ -90,13 +93,12 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   // per node: mult for each upwind direction (zero where the reference leaves
   // the cell unchanged: first list node for mu >= 0, last for mu < 0),
   // relaxation factor exp(-dtProp/tau) and 1 - it, boundary seed
-  float mhi[NPT], mlo[NPT], em[NPT], om[NPT], bcv[NPT];
-  bool bc[NPT];
+  float mhi[NPT], mlo[NPT], em[NPT], om[NPT];
+  __shared__ float s_bcv[3];  // seeds of list nodes 0..2, the boundary (CTA rank 0)
   const double vdt = ec.vgrid * dtProp;
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
-    mhi[q] = mlo[q] = em[q] = om[q] = bcv[q] = 0.f;
-    bc[q] = false;
+    mhi[q] = mlo[q] = em[q] = om[q] = 0.f;
 #pragma unroll
     for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = 0.f;
     const int il = i0 + q;
@@ -128,8 +130,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       mlo[q] = (il == L - 1) ? 0.f : (float)mult;
       em[q] = (float)emt;
       om[q] = (float)(1.0 - emt);
-      bc[q] = r.use_bc && il < 3;
-      bcv[q] = seedf;
+      if (il < 3) s_bcv[il] = seedf;
     }
   }
   // del_fac(mu) = v dtProp mugrid(mu), mugrid(mu) = -1 + (mu + 1/2) dmu
@@ -146,13 +147,16 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
 
   for (int step = 0; step < nsteps; ++step) {
     const int p = step & 1;
-    if (crank == 0 && warp == 0) {  // the boundary nodes (list 0..2) live in warp 0
+    if (r.use_bc && crank == 0 && warp == 0) {  // list nodes 0..2 live in warp 0
 #pragma unroll
-      for (int q = 0; q < NPT; ++q)
-        if (bc[q]) {
+      for (int q = 0; q < NPT; ++q) {
+        const int il = i0 + q;
+        if (il < 3) {
+          const float b = s_bcv[il];
 #pragma unroll
-          for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = bcv[q];
+          for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = b;
         }
+      }
     }
     if (lane == 31) {  // last node's outward half for the next warp's first node
       float *dst = hi(p, warp + 1);
@@ -338,7 +342,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   if (C > 1) cluster.sync();
 }
 
-int plan_stream2(int N, int M, int m0, bool packed, StreamPlan *plan) {
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
@@ -357,16 +361,20 @@ int plan_stream2(int N, int M, int m0, bool packed, StreamPlan *plan) {
   plan->threads = T;
   plan->reg_coef = 2;  // marks the several-nodes-per-thread kernel
   plan->packed = packed ? 1 : 0;
+  plan->filled = 0;
   if (packed && ((m0 & 1) || ((M - m0) & 1))) return EPREM_GPU_ERR_ARG;  // pairs of cells
+  if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
+  plan->filled = filled ? 1 : 0;
   plan->cluster = (N + npt * T - 1) / (npt * T);
   return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
 }
 
 template <int MMAX, bool PACK>
-static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, cudaStream_t st) {
+static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, bool full,
+                                    cudaStream_t st) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr size_t dyn = stream2_smem_bytes<MMAX>();
-  auto kern = k_stream2<MMAX, PACK>;
+  auto kern = full ? k_stream2<MMAX, PACK, true> : k_stream2<MMAX, PACK, false>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
@@ -385,13 +393,13 @@ static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, cudaS
 template <bool PACK>
 static cudaError_t launch_mmax(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st) {
   switch (pl.mmax) {
-    case 8: return launch_stream2_t<8, PACK>(r, pl.cluster, m0, st);
-    case 16: return launch_stream2_t<16, PACK>(r, pl.cluster, m0, st);
-    case 24: return launch_stream2_t<24, PACK>(r, pl.cluster, m0, st);
-    case 32: return launch_stream2_t<32, PACK>(r, pl.cluster, m0, st);
-    case 40: return launch_stream2_t<40, PACK>(r, pl.cluster, m0, st);
-    case 48: return launch_stream2_t<48, PACK>(r, pl.cluster, m0, st);
-    default: return launch_stream2_t<64, PACK>(r, pl.cluster, m0, st);
+    case 8: return launch_stream2_t<8, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 16: return launch_stream2_t<16, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 24: return launch_stream2_t<24, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 32: return launch_stream2_t<32, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 40: return launch_stream2_t<40, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 48: return launch_stream2_t<48, PACK>(r, pl.cluster, m0, pl.filled, st);
+    default: return launch_stream2_t<64, PACK>(r, pl.cluster, m0, pl.filled, st);
   }
 }
 

@@ -122,13 +122,16 @@ typedef struct {
                                        update stops with ERR_SUBCYCLES (0 means
                                        1,000,000).  The reference has no cap. */
   int32_t stream_variant;           /* streaming-kernel shape in the FP32 form
-                                       (tuning; results agree to rounding): 0
-                                       automatic (= 3), 1 one node per thread
-                                       with coefficients in registers, 2 one
-                                       node per thread with coefficients in
-                                       shared memory, 3 several nodes per
-                                       thread, 4 as 3 with packed fp32x2
-                                       arithmetic (even cells per mu half)    */
+                                       (tuning; results agree to rounding):
+                                       0 automatic (4 where both mu halves
+                                       hold even cell counts, else 3);
+                                       1 one node per thread, coefficients in
+                                       registers; 2 one node per thread,
+                                       coefficients in shared memory;
+                                       3 several nodes per thread; 4 as 3
+                                       with packed fp32x2 arithmetic; 5 as 4
+                                       with compile-time cell guards (M = 8,
+                                       16, ..., 64 and m0 = M/2)            */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids

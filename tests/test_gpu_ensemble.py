@@ -92,7 +92,7 @@ def test_autotune_keeps_a_correct_shape(oracle_lib):
     run.upload_f(f)
     run.upload_nodes(nodes)
     v = run.autotune()
-    assert v in (1, 2, 3, 4)
+    assert v in (1, 2, 3, 4, 5)
     # the scratch copy leaves the state alone
     np.testing.assert_array_equal(run.download_f(), f.astype(np.float32).astype(np.float64))
     run.update_energetic_particles(0.0)
@@ -106,7 +106,7 @@ def test_ensemble_autotune_by_size_class(oracle_lib):
     runs = [_start(w, oracle_lib, abi.EPREM_FP32) for w in ws]
     ens = Ensemble(runs)
     chosen = ens.autotune()
-    assert len(chosen) == 3 and all(v in (1, 2, 3, 4) for v in chosen)
+    assert len(chosen) == 3 and all(v in (1, 2, 3, 4, 5) for v in chosen)
     ens.set_time(0.0)
     ens.step()
     ens.synchronize()
