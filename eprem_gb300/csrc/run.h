@@ -1,0 +1,104 @@
+// run.h -- private to the ABI layer (eprem_gpu.cu, ensemble.cu,
+// surrogate_host.cu): the state behind an eprem_gpu_run handle and the error
+// helpers every entry point uses.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/eprem_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace eprem {
+
+// Failure of the calling thread's last ABI call (eprem_gpu_last_error).
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+constexpr int kMaxDevices = 64;  // per-device tables (static buffers, error flags)
+
+}  // namespace eprem
+
+#define CK(call)                                                  \
+  do {                                                            \
+    cudaError_t _e = (call);                                      \
+    if (_e != cudaSuccess) return eprem::cuda_fail(_e, #call);    \
+  } while (0)
+
+struct eprem_gpu_run {
+  eprem_dims_t dims;
+  eprem_params_t params;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  eprem::RunView v{};
+  eprem::MhdParams mhd{};
+  eprem::StreamPlan splan{};
+  eprem::NodePlan nplan{};
+  int m0 = 0;
+  double norm_radius = 0, neg_beta = 0;
+  void *d_f = nullptr;
+  double *d_nodes = nullptr, *d_mugrid = nullptr;
+  float *d_mugrid32 = nullptr;
+  eprem::NodeCoef32 *d_coef32 = nullptr;
+  eprem::EnergyConsts *d_ec = nullptr;
+  int *d_list = nullptr, *d_list_size = nullptr;
+  double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;
+  eprem::DevStatus *d_status = nullptr, *h_status = nullptr;
+  double *d_stage = nullptr;
+  size_t stage_elems = 0;
+  double *d_flux = nullptr;
+  uint64_t launches = 0;
+  // optional per-launch timing: events recorded around each kernel launch
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> ev_pending;  // (kind, index of start event)
+  size_t ev_used = 0;
+  // node phase: reference, split or surrogate (EPREM_NODE_PHASE_*)
+  int node_mode = 0;
+  struct eprem_gpu_surrogate *surr = nullptr;
+  unsigned long long *d_surr_counts = nullptr;  // [kept, fallback] rows
+  uint8_t *d_reject = nullptr;
+  // MAS background: device copies of the loaded time slices
+  bool mas_ready = false;  // eprem_gpu_mas_init done
+  bool mas_on = false, mas_selected = false;  // updateMhd uses MAS; slots chosen
+  std::vector<std::vector<void *>> mas_allocs;
+  std::vector<eprem::MasSlotDev> mas_slots;
+  std::vector<char> mas_loaded;
+  eprem::MasView mv{};
+  size_t cells() const {
+    return (size_t)dims.num_streams * dims.num_nodes * dims.num_energies * dims.num_mu;
+  }
+  size_t sn() const { return (size_t)dims.num_streams * dims.num_nodes; }
+};
+
+namespace eprem {
+
+// Runs one launch helper, bracketed by events when timing is on.
+template <typename Fn>
+inline int timed(eprem_gpu_run *r, int kind, Fn &&launch) {
+  if (!r->timing) return launch();
+  if (r->ev_used + 2 > r->ev_pool.size()) {
+    for (int i = 0; i < 64; i++) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) return EPREM_GPU_ERR_CUDA;
+      r->ev_pool.push_back(ev);
+    }
+  }
+  const size_t i0 = r->ev_used;
+  r->ev_used += 2;
+  cudaEventRecord(r->ev_pool[i0], r->stream);
+  int rc = launch();
+  cudaEventRecord(r->ev_pool[i0 + 1], r->stream);
+  r->ev_pending.push_back({kind, (int)i0});
+  return rc;
+}
+
+// Reads the status block (synchronising), reports a device failure in the
+// reference's words and, with reset_stats, hands over and restarts the log
+// statistics.
+int check_status(eprem_gpu_run *r, bool reset_stats, eprem_ep_stats_t *stats);
+// The node phase of one EP sub-step in the split and surrogate forms.
+int split_node_phase(eprem_gpu_run *r);
+
+}  // namespace eprem
