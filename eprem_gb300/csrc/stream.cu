@@ -283,10 +283,11 @@ static int threads_for(int mmax) {
 // 3 several list nodes per thread (stream2.cu), 4 the same with packed fp32x2
 // arithmetic (even cell counts per mu half), 5 as 4 with the cell guards
 // resolved at compile time (M fills its bin, m0 = M/2).  The automatic FP32
-// choice is 4 where it fits, else 3.  The FP64 form always keeps the
+// choice is the first of 5, 4, 3 that fits.  The FP64 form always keeps the
 // coefficients in shared memory.
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
-  if (precision == EPREM_FP32 && variant == 5 && plan_stream2(N, M, m0, true, true, plan) == 0)
+  if (precision == EPREM_FP32 && (variant == 0 || variant == 5) &&
+      plan_stream2(N, M, m0, true, true, plan) == 0)
     return 0;
   if (precision == EPREM_FP32 && (variant == 0 || variant == 4) &&
       plan_stream2(N, M, m0, true, false, plan) == 0)

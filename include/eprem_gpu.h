@@ -123,8 +123,8 @@ typedef struct {
                                        1,000,000).  The reference has no cap. */
   int32_t stream_variant;           /* streaming-kernel shape in the FP32 form
                                        (tuning; results agree to rounding):
-                                       0 automatic (4 where both mu halves
-                                       hold even cell counts, else 3);
+                                       0 automatic (the first of 5, 4, 3
+                                       that fits these sizes);
                                        1 one node per thread, coefficients in
                                        registers; 2 one node per thread,
                                        coefficients in shared memory;
