@@ -20,14 +20,13 @@ struct StreamPlan {
   int reg_coef;  // coefficients in registers (1), shared memory (0); 2: stream2.cu
   int packed;    // stream2.cu: fp32x2 arithmetic on pairs of mu cells
   int filled;    // stream2.cu: M fills the bin, m0 = M/2 (guards known at compile time)
-  int shape;     // stream2.cu: CTA shape, 0 the default table, 1 / 2 wider CTAs
 };
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan);
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches);
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 // stream2.cu -- FP32 streaming, two list nodes per thread (plan.reg_coef == 2)
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan);
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                    uint64_t *launches);
 

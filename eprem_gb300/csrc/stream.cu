@@ -282,22 +282,18 @@ static int threads_for(int mmax) {
 // variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
 // 3 several list nodes per thread (stream2.cu), 4 the same with packed fp32x2
 // arithmetic (even cell counts per mu half), 5 as 4 with the cell guards
-// resolved at compile time (M fills its bin, m0 = M/2), 6 / 7 as 5 in wider
-// CTAs (12 / 16 warps).  The automatic FP32 choice is the first of 5, 4, 3
-// that fits.  The FP64 form always keeps the
+// resolved at compile time (M fills its bin, m0 = M/2).  The automatic FP32
+// choice is the first of 5, 4, 3 that fits.  The FP64 form always keeps the
 // coefficients in shared memory.
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
-  if (precision == EPREM_FP32 && (variant == 6 || variant == 7) &&
-      plan_stream2(N, M, m0, true, true, variant - 5, plan) == 0)
-    return 0;
   if (precision == EPREM_FP32 && (variant == 0 || variant == 5) &&
-      plan_stream2(N, M, m0, true, true, 0, plan) == 0)
+      plan_stream2(N, M, m0, true, true, plan) == 0)
     return 0;
   if (precision == EPREM_FP32 && (variant == 0 || variant == 4) &&
-      plan_stream2(N, M, m0, true, false, 0, plan) == 0)
+      plan_stream2(N, M, m0, true, false, plan) == 0)
     return 0;
   if (precision == EPREM_FP32 && (variant == 0 || variant == 3) &&
-      plan_stream2(N, M, m0, false, false, 0, plan) == 0)
+      plan_stream2(N, M, m0, false, false, plan) == 0)
     return 0;
   int mmax = 0;
   for (int b : kStreamBins)

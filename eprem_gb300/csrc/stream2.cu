@@ -18,8 +18,6 @@
 // 1000-node stream fits one CTA.
 #include <cooperative_groups.h>
 
-#include <type_traits>
-
 #include "common.cuh"
 #include "kernels.h"
 
@@ -30,24 +28,18 @@ namespace eprem {
 // Threads per CTA and list nodes per thread for each mu bin: NPT * T >= 1024
 // where registers allow (a 1000-node stream in one CTA), the f halves of all
 // NPT nodes plus ~45 scalars inside the register cap of T threads.
-template <int MMAX, int SHAPE = 0> struct Stream2Shape;
-// Wider CTAs with fewer nodes per thread (more warps per SM, some spilling):
-// shape 1 keeps 12 warps, shape 2 16 warps; both hold >= 1024 nodes.
-template <int MMAX> struct Stream2Shape<MMAX, 1> {
-  static constexpr int T = MMAX <= 24 ? 512 : 384, NPT = MMAX <= 24 ? 2 : (MMAX <= 40 ? 3 : 2);
-};
-template <int MMAX> struct Stream2Shape<MMAX, 2> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<8, 0> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<16, 0> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<24, 0> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<32, 0> { static constexpr int T = 256, NPT = 4; };
-template <> struct Stream2Shape<40, 0> { static constexpr int T = 256, NPT = 4; };
-template <> struct Stream2Shape<48, 0> { static constexpr int T = 256, NPT = 3; };
-template <> struct Stream2Shape<64, 0> { static constexpr int T = 256, NPT = 2; };
+template <int MMAX> struct Stream2Shape;
+template <> struct Stream2Shape<8> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<16> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<24> { static constexpr int T = 512, NPT = 2; };
+template <> struct Stream2Shape<32> { static constexpr int T = 256, NPT = 4; };
+template <> struct Stream2Shape<40> { static constexpr int T = 256, NPT = 4; };
+template <> struct Stream2Shape<48> { static constexpr int T = 256, NPT = 3; };
+template <> struct Stream2Shape<64> { static constexpr int T = 256, NPT = 2; };
 
-template <int MMAX, int SHAPE>
+template <int MMAX>
 constexpr size_t stream2_smem_bytes() {
-  return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX, SHAPE>::T / 32 + 1) * (MMAX / 2);
+  return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
 }
 
 // PACK: the upwind and relaxation arithmetic on pairs of mu cells with the
@@ -55,10 +47,10 @@ constexpr size_t stream2_smem_bytes() {
 // the scalar fused multiply-adds); needs an even number of cells per half.
 // FILLED: both mu halves fill their MMAX/2 register slots (M = MMAX, m0 = M/2),
 // so every cell guard is known at compile time.
-template <int MMAX, bool PACK, bool FILLED, int SHAPE>
-__global__ void __launch_bounds__((Stream2Shape<MMAX, SHAPE>::T), 1) k_stream2(RunView r, int m0) {
-  constexpr int T = Stream2Shape<MMAX, SHAPE>::T;
-  constexpr int NPT = Stream2Shape<MMAX, SHAPE>::NPT;
+template <int MMAX, bool PACK, bool FILLED>
+__global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
+  constexpr int T = Stream2Shape<MMAX>::T;
+  constexpr int NPT = Stream2Shape<MMAX>::NPT;
   constexpr int W = T / 32;
   constexpr int H = MMAX / 2;  // register slots per direction (mu < 0, mu >= 0)
   constexpr unsigned FULL = 0xffffffffu;
@@ -350,35 +342,20 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX, SHAPE>::T), 1) k_stream2(R
   if (C > 1) cluster.sync();
 }
 
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan) {
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
-  if (shape && !(packed && filled)) return EPREM_GPU_ERR_ARG;  // wide shapes: packed, filled
-  int T = 0, npt = 0;
-  auto pick = [&](auto tag) {
-    using Sh = decltype(tag);
-    T = Sh::T;
-    npt = Sh::NPT;
-  };
-  auto by_shape = [&](auto m) {
-    constexpr int MM = decltype(m)::value;
-    if (shape == 1)
-      pick(Stream2Shape<MM, 1>{});
-    else if (shape == 2)
-      pick(Stream2Shape<MM, 2>{});
-    else
-      pick(Stream2Shape<MM, 0>{});
-  };
+  int T, npt;
   switch (mmax) {
-    case 8: by_shape(std::integral_constant<int, 8>{}); break;
-    case 16: by_shape(std::integral_constant<int, 16>{}); break;
-    case 24: by_shape(std::integral_constant<int, 24>{}); break;
-    case 32: by_shape(std::integral_constant<int, 32>{}); break;
-    case 40: by_shape(std::integral_constant<int, 40>{}); break;
-    case 48: by_shape(std::integral_constant<int, 48>{}); break;
-    default: by_shape(std::integral_constant<int, 64>{}); break;
+    case 8: T = Stream2Shape<8>::T; npt = Stream2Shape<8>::NPT; break;
+    case 16: T = Stream2Shape<16>::T; npt = Stream2Shape<16>::NPT; break;
+    case 24: T = Stream2Shape<24>::T; npt = Stream2Shape<24>::NPT; break;
+    case 32: T = Stream2Shape<32>::T; npt = Stream2Shape<32>::NPT; break;
+    case 40: T = Stream2Shape<40>::T; npt = Stream2Shape<40>::NPT; break;
+    case 48: T = Stream2Shape<48>::T; npt = Stream2Shape<48>::NPT; break;
+    default: T = Stream2Shape<64>::T; npt = Stream2Shape<64>::NPT; break;
   }
   plan->mmax = mmax;
   plan->threads = T;
@@ -388,16 +365,16 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, Stre
   if (packed && ((m0 & 1) || ((M - m0) & 1))) return EPREM_GPU_ERR_ARG;  // pairs of cells
   if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
   plan->filled = filled ? 1 : 0;
-  plan->shape = shape;
   plan->cluster = (N + npt * T - 1) / (npt * T);
   return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
 }
 
-template <int MMAX, bool PACK, bool FILLED, int SHAPE>
-static cudaError_t launch_shape(const RunView &r, int cluster, int m0, cudaStream_t st) {
-  constexpr int T = Stream2Shape<MMAX, SHAPE>::T;
-  constexpr size_t dyn = stream2_smem_bytes<MMAX, SHAPE>();
-  auto kern = k_stream2<MMAX, PACK, FILLED, SHAPE>;
+template <int MMAX, bool PACK>
+static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, bool full,
+                                    cudaStream_t st) {
+  constexpr int T = Stream2Shape<MMAX>::T;
+  constexpr size_t dyn = stream2_smem_bytes<MMAX>();
+  auto kern = full ? k_stream2<MMAX, PACK, true> : k_stream2<MMAX, PACK, false>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
@@ -413,27 +390,16 @@ static cudaError_t launch_shape(const RunView &r, int cluster, int m0, cudaStrea
   return cudaLaunchKernelEx(&cfg, kern, r, m0);
 }
 
-template <int MMAX, bool PACK>
-static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int m0,
-                                    cudaStream_t st) {
-  if constexpr (PACK) {
-    if (pl.filled && pl.shape == 1) return launch_shape<MMAX, true, true, 1>(r, pl.cluster, m0, st);
-    if (pl.filled && pl.shape == 2) return launch_shape<MMAX, true, true, 2>(r, pl.cluster, m0, st);
-  }
-  return pl.filled ? launch_shape<MMAX, PACK, true, 0>(r, pl.cluster, m0, st)
-                   : launch_shape<MMAX, PACK, false, 0>(r, pl.cluster, m0, st);
-}
-
 template <bool PACK>
 static cudaError_t launch_mmax(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st) {
   switch (pl.mmax) {
-    case 8: return launch_stream2_t<8, PACK>(r, pl, m0, st);
-    case 16: return launch_stream2_t<16, PACK>(r, pl, m0, st);
-    case 24: return launch_stream2_t<24, PACK>(r, pl, m0, st);
-    case 32: return launch_stream2_t<32, PACK>(r, pl, m0, st);
-    case 40: return launch_stream2_t<40, PACK>(r, pl, m0, st);
-    case 48: return launch_stream2_t<48, PACK>(r, pl, m0, st);
-    default: return launch_stream2_t<64, PACK>(r, pl, m0, st);
+    case 8: return launch_stream2_t<8, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 16: return launch_stream2_t<16, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 24: return launch_stream2_t<24, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 32: return launch_stream2_t<32, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 40: return launch_stream2_t<40, PACK>(r, pl.cluster, m0, pl.filled, st);
+    case 48: return launch_stream2_t<48, PACK>(r, pl.cluster, m0, pl.filled, st);
+    default: return launch_stream2_t<64, PACK>(r, pl.cluster, m0, pl.filled, st);
   }
 }
 
