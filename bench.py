@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--ensemble-runs", type=int, default=8,
                     help="members of the 64-run batched ensemble to step (first n)")
     ap.add_argument("--ensemble-steps", type=int, default=2)
+    ap.add_argument("--ensemble-only", action="store_true",
+                    help="measure only the batched ensemble (with --ensemble-runs 64: the full set)")
     ap.add_argument("--skip-surrogate", action="store_true")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     ap.add_argument("--mas-steps", type=int, default=2)
@@ -771,6 +773,11 @@ def main():
     args = parse()
     if args.profile_step:
         profile_step(args)
+        return
+    if args.ensemble_only:
+        from eprem_gb300 import Ensemble, EpremRun, abi, workloads as W
+        out = ensemble_case(args, EpremRun, Ensemble, abi, W)
+        print(json.dumps({"metric": METRIC, "unit": UNIT, "ensemble": out}), flush=True)
         return
     rank, ws, dist = dist_setup()
     try:

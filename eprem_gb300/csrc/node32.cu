@@ -18,7 +18,8 @@
 //     Those rows are evaluated with the reference's expressions, without
 //     fused multiply-adds;
 //   * k_focus32, every EP sub-step: one thread per (node, energy) row, its M
-//     cells and the split face coefficients max(q,0), min(q,0) in registers;
+//     cells and the split face coefficients max(q,0), min(q,0) in registers
+//     (the CTA's rows staged through shared memory with coalesced copies);
 //   * k_change32, every EP sub-step: one thread per (node, mu) column (a warp
 //     reads 32 consecutive mu of one energy: coalesced), ln f in shared
 //     memory.
@@ -175,64 +176,107 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
 }
 
 // ---- focusing: one (node, energy) row per thread ---------------------------
+// A CTA's 128 rows are contiguous in f: they pass through shared memory
+// (float4 loads and stores, rows padded to an odd pitch so each thread's row
+// reads are free of bank conflicts) instead of one strided row per thread.
 template <int P>
 __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
+  extern __shared__ float tile[];  // [kFocusThreads][pitch]
   const int E = r.E, M = r.M, N = r.N;
+  const int pitch = M | 1;
   const size_t rows = (size_t)r.S * N * E;
-  const size_t it = (size_t)blockIdx.x * kFocusThreads + threadIdx.x;
-  if (it >= rows) return;
-  const size_t g = it / E;
-  const int e = (int)(it - g * E);
-  const NodeCoef32 c = r.coef32[g];
-  if (!c.ok) return;
-  float *row = reinterpret_cast<float *>(r.f) + it * M;
-  float fr[P];
+  const size_t it0 = (size_t)blockIdx.x * kFocusThreads;
+  const int nrows = (int)((rows - it0) < (size_t)kFocusThreads ? (rows - it0) : kFocusThreads);
+  const int tid = threadIdx.x;
+  float *base = reinterpret_cast<float *>(r.f) + it0 * M;
+  const int nval = nrows * M;
+  const float inv_m = 1.f / (float)M;  // row = floor((i + 1/2) / M), exact for i < 2^16
+  // it0 * M is a multiple of 4 floats (it0 a multiple of 128): 16-byte aligned
+  const int nvec = nval / 4;
+  for (int v = tid; v < nvec; v += kFocusThreads) {
+    const float4 x = reinterpret_cast<const float4 *>(base)[v];
+    const float xs[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-  for (int m = 0; m < P; ++m)
-    if (m < M) fr[m] = row[m];
-  if (c.ns_f > 0) {
-    const float v = r.ec[e].v32, vi = r.ec[e].vi32;
-    const float a = -(v * c.dlnbds) - (2.f * vi) * c.dupar;
-    const float b = c.b, sc = c.scale_f;
-    // face m (between cells m-1 and m), m = 1..M-1: q = dt_sub/dmu times the
-    // mean of the two cell velocities; flux = max(q,0) f[m-1] + min(q,0) f[m]
-    float qp[P], qn[P];
-    float vel_prev = 0.f;
-#pragma unroll
-    for (int m = 0; m < P; ++m) {
-      qp[m] = qn[m] = 0.f;
-      if (m < M) {
-        const float mu = r.mugrid32[m];
-        const float vel = 0.5f * (1.f - mu * mu) * (a + mu * b);
-        if (m >= 1) {
-          const float q = sc * 0.5f * (vel + vel_prev);
-          qp[m] = fmaxf(q, 0.f);
-          qn[m] = fminf(q, 0.f);
-        }
-        vel_prev = vel;
-      }
+    for (int k = 0; k < 4; k++) {
+      const int i = 4 * v + k, rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+      tile[rr * pitch + cc] = xs[k];
     }
-    for (int s = 0; s < c.ns_f; ++s) {
-      float gprev = 0.f;
+  }
+  for (int i = 4 * nvec + tid; i < nval; i += kFocusThreads) {
+    const int rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+    tile[rr * pitch + cc] = base[i];
+  }
+  __syncthreads();
+  if (tid < nrows) {
+    const size_t it = it0 + tid;
+    const size_t g = it / E;
+    const int e = (int)(it - g * E);
+    const NodeCoef32 c = r.coef32[g];
+    if (c.ok) {
+      float *row = tile + tid * pitch;
+      float fr[P];
+#pragma unroll
+      for (int m = 0; m < P; ++m)
+        if (m < M) fr[m] = row[m];
+      if (c.ns_f > 0) {
+        const float v = r.ec[e].v32, vi = r.ec[e].vi32;
+        const float a = -(v * c.dlnbds) - (2.f * vi) * c.dupar;
+        const float b = c.b, sc = c.scale_f;
+        // face m (between cells m-1 and m), m = 1..M-1: q = dt_sub/dmu times the
+        // mean of the two cell velocities; flux = max(q,0) f[m-1] + min(q,0) f[m]
+        float qp[P], qn[P];
+        float vel_prev = 0.f;
+#pragma unroll
+        for (int m = 0; m < P; ++m) {
+          qp[m] = qn[m] = 0.f;
+          if (m < M) {
+            const float mu = r.mugrid32[m];
+            const float vel = 0.5f * (1.f - mu * mu) * (a + mu * b);
+            if (m >= 1) {
+              const float q = sc * 0.5f * (vel + vel_prev);
+              qp[m] = fmaxf(q, 0.f);
+              qn[m] = fminf(q, 0.f);
+            }
+            vel_prev = vel;
+          }
+        }
+        for (int s = 0; s < c.ns_f; ++s) {
+          float gprev = 0.f;
+#pragma unroll
+          for (int m = 0; m < P; ++m) {
+            if (m < M) {
+              float gnext = 0.f;
+              if (m + 1 < M && m + 1 < P) gnext = fmaf(qn[m + 1], fr[m + 1], qp[m + 1] * fr[m]);
+              fr[m] = fr[m] - (gnext - gprev);
+              gprev = gnext;
+            }
+          }
+        }
+      }
+      int code = 0;
 #pragma unroll
       for (int m = 0; m < P; ++m) {
         if (m < M) {
-          float gnext = 0.f;
-          if (m + 1 < M && m + 1 < P) gnext = fmaf(qn[m + 1], fr[m + 1], qp[m + 1] * fr[m]);
-          fr[m] = fr[m] - (gnext - gprev);
-          gprev = gnext;
+          const float v = fr[m];
+          if (bad_value(v, &code)) set_error(r.status, code, 2, (int)(g / N), (int)(g % N), e, m);
+          row[m] = v < FLT_MIN ? FLT_MIN : v;
         }
       }
     }
   }
-  int code = 0;
+  __syncthreads();
+  for (int v = tid; v < nvec; v += kFocusThreads) {
+    float xs[4];
 #pragma unroll
-  for (int m = 0; m < P; ++m) {
-    if (m < M) {
-      const float v = fr[m];
-      if (bad_value(v, &code)) set_error(r.status, code, 2, (int)(g / N), (int)(g % N), e, m);
-      row[m] = v < FLT_MIN ? FLT_MIN : v;
+    for (int k = 0; k < 4; k++) {
+      const int i = 4 * v + k, rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+      xs[k] = tile[rr * pitch + cc];
     }
+    reinterpret_cast<float4 *>(base)[v] = make_float4(xs[0], xs[1], xs[2], xs[3]);
+  }
+  for (int i = 4 * nvec + tid; i < nval; i += kFocusThreads) {
+    const int rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+    base[i] = tile[rr * pitch + cc];
   }
 }
 
@@ -325,7 +369,9 @@ int launch_node32_setup(const RunView &r, cudaStream_t st, uint64_t *launches) {
 template <int P>
 static void launch_focus_t(const RunView &r, cudaStream_t st) {
   const size_t rows = (size_t)r.S * r.N * r.E;
-  k_focus32<P><<<(unsigned)((rows + kFocusThreads - 1) / kFocusThreads), kFocusThreads, 0, st>>>(r);
+  const size_t smem = (size_t)kFocusThreads * (r.M | 1) * sizeof(float);
+  k_focus32<P><<<(unsigned)((rows + kFocusThreads - 1) / kFocusThreads), kFocusThreads, smem, st>>>(
+      r);
 }
 
 static void launch_change(const RunView &r, cudaStream_t st) {
