@@ -189,6 +189,10 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
     ec[i].seed_exp = exp(-(grids->egrid[i] / normE0));
     ec[i].v32 = (float)grids->vgrid[i];
     ec[i].vi32 = (float)grids->vgrid_i[i];
+    ec[i].rig_lamo32 = (float)ec[i].rig_lamo;
+    const double norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);
+    ec[i].seed32 =
+        (float)(norm_j0 * ec[i].seed_power * ec[i].seed_exp / p.bf_xi / (2.0 * grids->egrid[i]));
   }
   std::vector<float> mu32(M);
   for (int m = 0; m < M; m++) mu32[m] = (float)grids->mugrid[m];

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   float mhi[NPT], mlo[NPT], em[NPT], om[NPT];
   __shared__ float s_bcv[3];  // seeds of list nodes 0..2, the boundary (CTA rank 0)
   const double vdt = ec.vgrid * dtProp;
+  const float dtp = (float)dtProp, dtp_i = (float)dtProp_i;
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
     mhi[q] = mlo[q] = em[q] = om[q] = 0.f;
@@ -105,31 +106,33 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
     if (il < L) {
       const int k = r.list[sN + il];
       const size_t gidx = sN + k;
-      const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
-      const double dsi = r.ds_i[sN + il];
-      const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
+      // stencil coefficients in FP32 (the FP64 pipe would take a tenth of the
+      // launch for them): tau = lambda / v, mult = ds_i * min(tau / dtProp, 1),
+      // the relaxation factor and its complement, the seed (floored at FLT_MIN)
+      const float tau = ec.vi32 * (ec.rig_lamo32 * (float)r.mfp_node[gidx]);
+      const float dsi = (float)r.ds_i[sN + il];
+      const float mult = (dtp > tau) ? dsi * tau * dtp_i : dsi;
       // split form: the relaxation runs in the node phase instead
-      const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
-      const double seedv = seed_value(r, ec, r.seed_radial[gidx]);
-      const float seedf = to_real<float>(seedv);
+      const float x = r.relax_in_stream ? -dtp / tau : 0.f;
+      const float seedf = fmaxf(ec.seed32 * (float)r.seed_radial[gidx], FLT_MIN);
       const float *fp = reinterpret_cast<const float *>(r.f) + (gidx * r.E + e) * M;
 #pragma unroll
       for (int j = 0; j < H; ++j) {
         if (j < nL) {
           float v = fp[j];
-          if (r.check_seed && (double)v < seedv) v = seedf;
+          if (r.check_seed && v < seedf) v = seedf;
           Lf[q][j] = v;
         }
         if (j < nR) {
           float v = fp[m0 + j];
-          if (r.check_seed && (double)v < seedv) v = seedf;
+          if (r.check_seed && v < seedf) v = seedf;
           Rf[q][j] = v;
         }
       }
-      mhi[q] = (il == 0) ? 0.f : (float)mult;
-      mlo[q] = (il == L - 1) ? 0.f : (float)mult;
-      em[q] = (float)emt;
-      om[q] = (float)(1.0 - emt);
+      mhi[q] = (il == 0) ? 0.f : mult;
+      mlo[q] = (il == L - 1) ? 0.f : mult;
+      em[q] = expf(x);
+      om[q] = -expm1f(x);
       if (il < 3) s_bcv[il] = seedf;
     }
   }
