@@ -45,9 +45,6 @@ struct EnergyConsts {
   double seed_power;     // pow(E/normE1, -gamma)           (src/energeticParticlesBoundary.c:101)
   double seed_exp;       // exp(-(E/normE0))                (:102)
   float v32, vi32;       // vgrid, vgrid_i rounded to float (FP32 stencils)
-  float rig_lamo32;      // rig_lamo rounded to float
-  float seed32;          // seed value without its radial factor:
-                         // normJ0 power exp / xi / (2 E), rounded to float
 };
 
 // Per-node coefficients of the FP32 focusing / change kernels, fixed for one
@@ -76,6 +73,7 @@ struct RunView {
   double *seed_radial;     // [S*N]   pow(r/normRadius, -beta)
   double *mfp_node;        // [S*N]   pow(r*rScale, a) or pow(BsAu/B, b)
   NodeCoef32 *coef32;      // [S*N]   FP32 form only
+  float4 *scoef;           // [S][E][N] FP32 streaming coefficients (stream2.cu)
   DevStatus *status;
   // parameters
   double r_scale, dt, dt_full, dmu, dlnp;

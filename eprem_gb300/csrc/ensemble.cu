@@ -26,6 +26,8 @@ int tune_stream(eprem_gpu_run *r, int *chosen) {
                            p.mfp_type == 2 ? p.mfp_b_power : p.mfp_radial_power, p.mhd_bs_au,
                            &r->launches);
   if (rc) return cuda_fail(cudaGetLastError(), "autotune geometry launch");
+  if (r->d_scoef && launch_stream2_coef(r->v, r->stream, &r->launches))
+    return cuda_fail(cudaGetLastError(), "autotune coefficient launch");
   const int S_sub = r->dims.num_streams < 96 ? r->dims.num_streams : 96;
   const size_t n = (size_t)S_sub * r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
   void *f = nullptr;

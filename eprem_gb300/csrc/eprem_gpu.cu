@@ -159,6 +159,9 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   if (e == cudaSuccess) e = dalloc(&r->d_mugrid, (size_t)M);
   if (e == cudaSuccess) e = dalloc(&r->d_mugrid32, (size_t)M);
   if (e == cudaSuccess && fast32) e = dalloc(&r->d_coef32, SN);
+  // FP32 streaming coefficients (any FP32 run may be tuned to stream2.cu)
+  if (e == cudaSuccess && dims->precision == EPREM_FP32 && params->use_parallel_diffusion > 0)
+    e = dalloc(&r->d_scoef, SN * (size_t)dims->num_energies);
   if (e == cudaSuccess) e = dalloc(&r->d_ec, (size_t)E);
   if (e == cudaSuccess) e = dalloc(&r->d_list, SN);
   if (e == cudaSuccess) e = dalloc(&r->d_list_size, (size_t)S);
@@ -189,10 +192,6 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
     ec[i].seed_exp = exp(-(grids->egrid[i] / normE0));
     ec[i].v32 = (float)grids->vgrid[i];
     ec[i].vi32 = (float)grids->vgrid_i[i];
-    ec[i].rig_lamo32 = (float)ec[i].rig_lamo;
-    const double norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);
-    ec[i].seed32 =
-        (float)(norm_j0 * ec[i].seed_power * ec[i].seed_exp / p.bf_xi / (2.0 * grids->egrid[i]));
   }
   std::vector<float> mu32(M);
   for (int m = 0; m < M; m++) mu32[m] = (float)grids->mugrid[m];
@@ -221,6 +220,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.mugrid = r->d_mugrid;
   v.mugrid32 = r->d_mugrid32;
   v.coef32 = r->d_coef32;
+  v.scoef = r->d_scoef;
   v.ec = r->d_ec;
   v.list = r->d_list;
   v.list_size = r->d_list_size;
@@ -275,6 +275,7 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_surr_counts);
   cudaFree(r->d_reject);
   cudaFree(r->d_coef32);
+  cudaFree(r->d_scoef);
   cudaFree(r->d_ec);
   cudaFree(r->d_list);
   cudaFree(r->d_list_size);
@@ -379,6 +380,11 @@ extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_g
                            &r->launches);
   });
   if (rc) return cuda_fail(cudaGetLastError(), "geometry launch");
+  if (r->v.use_stream && r->splan.reg_coef == 2) {
+    rc = timed(r, EPREM_KERNEL_GEOMETRY,
+               [&] { return launch_stream2_coef(r->v, r->stream, &r->launches); });
+    if (rc) return cuda_fail(cudaGetLastError(), "streaming coefficient launch");
+  }
   if (r->nplan.fast32 && (r->v.use_focus || r->v.use_change)) {
     rc = timed(r, EPREM_KERNEL_NODE,
                [&] { return launch_node32_setup(r->v, r->stream, &r->launches); });

@@ -27,6 +27,8 @@ int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 // stream2.cu -- FP32 streaming, two list nodes per thread (plan.reg_coef == 2)
 int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan);
+// once per updateEnergeticParticles call, before the stream2 launches
+int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                    uint64_t *launches);
 

@@ -41,6 +41,7 @@ struct eprem_gpu_run {
   double *d_nodes = nullptr, *d_mugrid = nullptr;
   float *d_mugrid32 = nullptr;
   eprem::NodeCoef32 *d_coef32 = nullptr;
+  float4 *d_scoef = nullptr;
   eprem::EnergyConsts *d_ec = nullptr;
   int *d_list = nullptr, *d_list_size = nullptr;
   double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;

@@ -79,7 +79,6 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   }
   const int nsteps = (int)nst;
   const double dtProp = r.dt / (1.0 * nsteps);
-  const double dtProp_i = 1.0 / dtProp;
   if (crank == 0 && tid == 0) {
     atomicMax(&r.status->max_stream, nsteps);
     atomicAdd(&r.status->stream_cs, (unsigned long long)nsteps * L * M);
@@ -96,7 +95,9 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   float mhi[NPT], mlo[NPT], em[NPT], om[NPT];
   __shared__ float s_bcv[3];  // seeds of list nodes 0..2, the boundary (CTA rank 0)
   const double vdt = ec.vgrid * dtProp;
-  const float dtp = (float)dtProp, dtp_i = (float)dtProp_i;
+  // per list node: mult, relaxation factor and its complement, seed, made
+  // in FP64 once per call (k_stream2_coef) and rounded to float
+  const float4 *cf = r.scoef + ((size_t)s * r.E + e) * N;
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
     mhi[q] = mlo[q] = em[q] = om[q] = 0.f;
@@ -106,21 +107,14 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
     if (il < L) {
       const int k = r.list[sN + il];
       const size_t gidx = sN + k;
-      // stencil coefficients in FP32 (the FP64 pipe would take a tenth of the
-      // launch for them): tau = lambda / v, mult = ds_i * min(tau / dtProp, 1),
-      // the relaxation factor and its complement, the seed (floored at FLT_MIN)
-      const float tau = ec.vi32 * (ec.rig_lamo32 * (float)r.mfp_node[gidx]);
-      const float dsi = (float)r.ds_i[sN + il];
-      const float mult = (dtp > tau) ? dsi * tau * dtp_i : dsi;
-      // split form: the relaxation runs in the node phase instead
-      const float x = r.relax_in_stream ? -dtp / tau : 0.f;
-      const float seedf = fmaxf(ec.seed32 * (float)r.seed_radial[gidx], FLT_MIN);
+      const float4 c = cf[il];
+      const float seedf = c.w;
       const float *fp = reinterpret_cast<const float *>(r.f) + (gidx * r.E + e) * M;
 #pragma unroll
       for (int j = 0; j < H; ++j) {
         if (j < nL) {
           float v = fp[j];
-          if (r.check_seed && v < seedf) v = seedf;
+          if (r.check_seed && v < seedf) v = seedf;  // as (double)v < seed: no float between
           Lf[q][j] = v;
         }
         if (j < nR) {
@@ -129,10 +123,10 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
           Rf[q][j] = v;
         }
       }
-      mhi[q] = (il == 0) ? 0.f : mult;
-      mlo[q] = (il == L - 1) ? 0.f : mult;
-      em[q] = expf(x);
-      om[q] = -expm1f(x);
+      mhi[q] = (il == 0) ? 0.f : c.x;
+      mlo[q] = (il == L - 1) ? 0.f : c.x;
+      em[q] = c.y;
+      om[q] = c.z;
       if (il < 3) s_bcv[il] = seedf;
     }
   }
@@ -343,6 +337,50 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
     }
   }
   if (C > 1) cluster.sync();
+}
+
+// Per (stream, energy, list node): mult = ds_i min(tau / dtProp, 1), the
+// relaxation factor exp(-dtProp / tau) and 1 - it, and the seed -- the
+// reference's expressions in FP64 (src/energeticParticles.c:2300-2350),
+// rounded to float once per call: the FP32 streaming kernels read them
+// instead of spending FP64 pipe time on them at every launch.
+__global__ void k_stream2_coef(RunView r) {
+  const size_t total = (size_t)r.S * r.E * r.N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int il = (int)(i % r.N);
+    const size_t se = i / r.N;
+    const int e = (int)(se % r.E);
+    const int s = (int)(se / r.E);
+    const int L = r.list_size[s];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (il < L) {
+      const EnergyConsts ec = r.ec[e];
+      const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
+      const double nst = floor(r.dt / dtMin + 1.0);
+      const double dtProp = r.dt / (1.0 * (nst >= 1.0 ? nst : 1.0));
+      const double dtProp_i = 1.0 / dtProp;
+      const size_t sN = (size_t)s * r.N;
+      const size_t gidx = sN + r.list[sN + il];
+      const double tau = ec.vgrid_i * (ec.rig_lamo * r.mfp_node[gidx]);
+      const double dsi = r.ds_i[sN + il];
+      const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
+      // split form: the relaxation runs in the node phase instead
+      const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
+      out = make_float4((float)mult, (float)emt, (float)(1.0 - emt),
+                        to_real<float>(seed_value(r, ec, r.seed_radial[gidx])));
+    }
+    r.scoef[i] = out;
+  }
+}
+
+int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches) {
+  const size_t total = (size_t)r.S * r.E * r.N;
+  size_t b = (total + 255) / 256;
+  if (b > 152 * 64) b = 152 * 64;
+  k_stream2_coef<<<(unsigned)b, 256, 0, st>>>(r);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
 int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan) {
