@@ -285,6 +285,9 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_mfp_node);
   cudaFree(r->d_status);
   cudaFree(r->d_stage);
+  for (cudaEvent_t ev : r->stage_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
   cudaFree(r->d_flux);
   for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
   for (auto &slot : r->mas_allocs)
@@ -296,18 +299,25 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
 }
 
 static int ensure_stage(eprem_gpu_run *r, size_t elems) {
+  if (!r->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &ev : r->stage_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
   if (r->stage_elems >= elems) return EPREM_GPU_OK;
   cudaFree(r->d_stage);
   r->d_stage = nullptr;
   r->stage_elems = 0;
-  CK(cudaMalloc(&r->d_stage, elems * sizeof(double)));
+  CK(cudaMalloc(&r->d_stage, 2 * elems * sizeof(double)));
   r->stage_elems = elems;
   return EPREM_GPU_OK;
 }
 
 // Chunk of doubles staged at a time when converting f for the FP32 form.
-static const size_t kStageChunk = (size_t)1 << 27;
+static const size_t kStageChunk = (size_t)1 << 26;
 
+// Upload of an FP32-form f: chunk k goes host -> staging buffer k%2 on the
+// copy stream, then is converted on the run's stream; a buffer is refilled
+// only after its previous conversion has finished.
 extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
   if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
   const size_t n = r->cells();
@@ -318,17 +328,28 @@ extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
   const size_t chunk = n < kStageChunk ? n : kStageChunk;
   int rc = ensure_stage(r, chunk);
   if (rc) return rc;
-  for (size_t off = 0; off < n; off += chunk) {
+  cudaEvent_t *converted = r->stage_ev, *copied = r->stage_ev + 2;
+  CK(cudaEventRecord(converted[0], r->stream));  // the run's earlier work
+  CK(cudaEventRecord(converted[1], r->stream));
+  size_t k = 0;
+  for (size_t off = 0; off < n; off += chunk, ++k) {
     const size_t c = (n - off) < chunk ? (n - off) : chunk;
-    CK(cudaMemcpyAsync(r->d_stage, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->stream));
-    rc = launch_convert_f(r->v, r->d_stage,
-                          reinterpret_cast<double *>(static_cast<float *>(r->d_f) + off), 1, c,
-                          r->stream, &r->launches);
+    double *buf = r->d_stage + (k & 1) * r->stage_elems;
+    CK(cudaStreamWaitEvent(r->copy_stream, converted[k & 1], 0));
+    CK(cudaMemcpyAsync(buf, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->copy_stream));
+    CK(cudaEventRecord(copied[k & 1], r->copy_stream));
+    CK(cudaStreamWaitEvent(r->stream, copied[k & 1], 0));
+    rc = launch_convert_f(r->v, buf, reinterpret_cast<double *>(static_cast<float *>(r->d_f) + off),
+                          1, c, r->stream, &r->launches);
     if (rc) return fail(rc, "conversion kernel launch failed");
+    CK(cudaEventRecord(converted[k & 1], r->stream));
   }
   return EPREM_GPU_OK;
 }
 
+// Download of an FP32-form f: chunk k is converted into staging buffer k%2
+// on the run's stream, then copied to the host on the copy stream; the run's
+// stream waits for the last copy.
 extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
   if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
   const size_t n = r->cells();
@@ -338,14 +359,25 @@ extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
     const size_t chunk = n < kStageChunk ? n : kStageChunk;
     int rc = ensure_stage(r, chunk);
     if (rc) return rc;
-    for (size_t off = 0; off < n; off += chunk) {
+    cudaEvent_t *converted = r->stage_ev, *copied = r->stage_ev + 2;
+    CK(cudaEventRecord(copied[0], r->copy_stream));
+    CK(cudaEventRecord(copied[1], r->copy_stream));
+    size_t k = 0;
+    for (size_t off = 0; off < n; off += chunk, ++k) {
       const size_t c = (n - off) < chunk ? (n - off) : chunk;
+      double *buf = r->d_stage + (k & 1) * r->stage_elems;
+      CK(cudaStreamWaitEvent(r->stream, copied[k & 1], 0));
       rc = launch_convert_f(r->v,
                             reinterpret_cast<const double *>(static_cast<const float *>(r->d_f) + off),
-                            r->d_stage, 0, c, r->stream, &r->launches);
+                            buf, 0, c, r->stream, &r->launches);
       if (rc) return fail(rc, "conversion kernel launch failed");
-      CK(cudaMemcpyAsync(f + off, r->d_stage, c * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+      CK(cudaEventRecord(converted[k & 1], r->stream));
+      CK(cudaStreamWaitEvent(r->copy_stream, converted[k & 1], 0));
+      CK(cudaMemcpyAsync(f + off, buf, c * sizeof(double), cudaMemcpyDeviceToHost, r->copy_stream));
+      CK(cudaEventRecord(copied[k & 1], r->copy_stream));
     }
+    CK(cudaEventRecord(copied[0], r->copy_stream));
+    CK(cudaStreamWaitEvent(r->stream, copied[0], 0));
   }
   return check_status(r, false, nullptr);
 }

@@ -46,8 +46,12 @@ struct eprem_gpu_run {
   int *d_list = nullptr, *d_list_size = nullptr;
   double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;
   eprem::DevStatus *d_status = nullptr, *h_status = nullptr;
-  double *d_stage = nullptr;
+  // FP32 form: two staging buffers of FP64 chunks; host copies run on their
+  // own stream and overlap the conversion of the other buffer
+  double *d_stage = nullptr;  // [2][stage_elems]
   size_t stage_elems = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_ev[4] = {};  // converted[2], copied[2]
   double *d_flux = nullptr;
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch
