@@ -313,11 +313,11 @@ static int ensure_stage(eprem_gpu_run *r, size_t elems) {
 }
 
 // Chunk of doubles staged at a time when converting f for the FP32 form.
-static const size_t kStageChunk = (size_t)1 << 26;
+static const size_t kStageChunk = (size_t)1 << 27;
 
-// Upload of an FP32-form f: chunk k goes host -> staging buffer k%2 on the
-// copy stream, then is converted on the run's stream; a buffer is refilled
-// only after its previous conversion has finished.
+// Upload of an FP32-form f: chunks of FP64 host values through a staging
+// buffer, converted on the run's stream (the host-to-device copies run at the
+// link's rate in stream order; the conversion is short beside them).
 extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
   if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
   const size_t n = r->cells();
@@ -328,21 +328,17 @@ extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
   const size_t chunk = n < kStageChunk ? n : kStageChunk;
   int rc = ensure_stage(r, chunk);
   if (rc) return rc;
-  cudaEvent_t *converted = r->stage_ev, *copied = r->stage_ev + 2;
-  CK(cudaEventRecord(converted[0], r->stream));  // the run's earlier work
-  CK(cudaEventRecord(converted[1], r->stream));
+  // the copy stream's downloads may still read the staging buffers
+  CK(cudaEventRecord(r->stage_ev[2], r->copy_stream));
+  CK(cudaStreamWaitEvent(r->stream, r->stage_ev[2], 0));
   size_t k = 0;
   for (size_t off = 0; off < n; off += chunk, ++k) {
     const size_t c = (n - off) < chunk ? (n - off) : chunk;
     double *buf = r->d_stage + (k & 1) * r->stage_elems;
-    CK(cudaStreamWaitEvent(r->copy_stream, converted[k & 1], 0));
-    CK(cudaMemcpyAsync(buf, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->copy_stream));
-    CK(cudaEventRecord(copied[k & 1], r->copy_stream));
-    CK(cudaStreamWaitEvent(r->stream, copied[k & 1], 0));
+    CK(cudaMemcpyAsync(buf, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->stream));
     rc = launch_convert_f(r->v, buf, reinterpret_cast<double *>(static_cast<float *>(r->d_f) + off),
                           1, c, r->stream, &r->launches);
     if (rc) return fail(rc, "conversion kernel launch failed");
-    CK(cudaEventRecord(converted[k & 1], r->stream));
   }
   return EPREM_GPU_OK;
 }

@@ -46,8 +46,8 @@ struct eprem_gpu_run {
   int *d_list = nullptr, *d_list_size = nullptr;
   double *d_ds_i = nullptr, *d_ds_min = nullptr, *d_seed_radial = nullptr, *d_mfp_node = nullptr;
   eprem::DevStatus *d_status = nullptr, *h_status = nullptr;
-  // FP32 form: two staging buffers of FP64 chunks; host copies run on their
-  // own stream and overlap the conversion of the other buffer
+  // FP32 form: two staging buffers of FP64 chunks; downloads copy to the
+  // host on their own stream, overlapping the conversion of the other buffer
   double *d_stage = nullptr;  // [2][stage_elems]
   size_t stage_elems = 0;
   cudaStream_t copy_stream = nullptr;
