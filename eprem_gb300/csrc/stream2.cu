@@ -158,22 +158,41 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
     if (lane == 31) {  // last node's outward half for the next warp's first node
       float *dst = hi(p, warp + 1);
       float *rdst = (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H : nullptr;
+      if constexpr (FILLED && H % 4 == 0) {  // whole half, 16-byte slots (H * 4 B rows)
 #pragma unroll
-      for (int j = 0; j < H; ++j)
-        if (j < nR) {
-          dst[j] = Rf[NPT - 1][j];
-          if (rdst) rdst[j] = Rf[NPT - 1][j];
+        for (int j = 0; j < H; j += 4) {
+          const float4 v = make_float4(Rf[NPT - 1][j], Rf[NPT - 1][j + 1], Rf[NPT - 1][j + 2],
+                                       Rf[NPT - 1][j + 3]);
+          *reinterpret_cast<float4 *>(dst + j) = v;
+          if (rdst) *reinterpret_cast<float4 *>(rdst + j) = v;
         }
+      } else {
+#pragma unroll
+        for (int j = 0; j < H; ++j)
+          if (j < nR) {
+            dst[j] = Rf[NPT - 1][j];
+            if (rdst) rdst[j] = Rf[NPT - 1][j];
+          }
+      }
     }
     if (lane == 0) {  // first node's inward half for the previous warp's last node
       float *dst = lo(p, warp);
       float *rdst = (warp == 0 && prev_loW) ? prev_loW + ((p * 2 + 1) * (W + 1) + W) * H : nullptr;
+      if constexpr (FILLED && H % 4 == 0) {
 #pragma unroll
-      for (int j = 0; j < H; ++j)
-        if (j < nL) {
-          dst[j] = Lf[0][j];
-          if (rdst) rdst[j] = Lf[0][j];
+        for (int j = 0; j < H; j += 4) {
+          const float4 v = make_float4(Lf[0][j], Lf[0][j + 1], Lf[0][j + 2], Lf[0][j + 3]);
+          *reinterpret_cast<float4 *>(dst + j) = v;
+          if (rdst) *reinterpret_cast<float4 *>(rdst + j) = v;
         }
+      } else {
+#pragma unroll
+        for (int j = 0; j < H; ++j)
+          if (j < nL) {
+            dst[j] = Lf[0][j];
+            if (rdst) rdst[j] = Lf[0][j];
+          }
+      }
     }
     if (C > 1)
       cluster.sync();
@@ -196,8 +215,9 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
           float nb0 = __shfl_down_sync(FULL, Lf[0][j], 1);
           float nb1 = __shfl_down_sync(FULL, Lf[0][j + 1], 1);
           if (lane == 31) {
-            nb0 = my_lo[j];
-            nb1 = my_lo[j + 1];
+            const float2 h2 = *reinterpret_cast<const float2 *>(my_lo + j);
+            nb0 = h2.x;
+            nb1 = h2.y;
           }
 #pragma unroll
           for (int q = 0; q < NPT; ++q) {
@@ -223,8 +243,9 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
           float nb0 = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
           float nb1 = __shfl_up_sync(FULL, Rf[NPT - 1][j + 1], 1);
           if (lane == 0) {
-            nb0 = my_hi[j];
-            nb1 = my_hi[j + 1];
+            const float2 h2 = *reinterpret_cast<const float2 *>(my_hi + j);
+            nb0 = h2.x;
+            nb1 = h2.y;
           }
 #pragma unroll
           for (int q = NPT - 1; q >= 0; --q) {
