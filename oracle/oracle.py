@@ -24,11 +24,14 @@ DP = C.POINTER(C.c_double)
 
 
 def build(ref: bool = False, reference_root: str = "/root/reference") -> None:
-    """Compile liboracle.so (and the reference harness when asked and the
-    reference tree is present)."""
+    """Compile liboracle.so and, when asked and the reference tree is
+    present, the reference harness (libeprem_ref.so), the reference's own
+    driver (eprem_ref) and the driver over the drop-in and this restatement
+    (eprem_oracle_dropin)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if ref and os.path.isdir(os.path.join(reference_root, "src")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"])
+        subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref", "ref-dropin",
+                               f"REF={reference_root}"])
 
 
 def _dp(a: np.ndarray):

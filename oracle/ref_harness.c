@@ -4,12 +4,10 @@
  * oracle/_ref/libeprem_ref.so.  TEST INFRASTRUCTURE ONLY: it exists to pin
  * the CPU restatement (eprem_oracle.c) against the reference itself.
  *
- * It supplies what the reference links against but the container lacks:
- *   - a one-rank MPI (MPI_COMM_WORLD of size 1: gathers and scatters are
- *     copies, sends to MPI_PROC_NULL do nothing, windows are malloc'd);
- *   - libconfig / netCDF / HDF5 entry points that report failure (the harness
- *     fills the reference's `config` struct directly and never asks for I/O);
- *   - the timer globals that src/eprem.c defines.
+ * With ref_shims.c (one-rank MPI, config reader, netCDF capture) it
+ * supplies what the reference links against but the container lacks, plus
+ * the timer globals that src/eprem.c defines; the harness fills the
+ * reference's `config` struct directly and asks for no file I/O.
  * and a small C API (ref_*) that loads a state in the include/eprem_gpu.h
  * layout into the reference globals, calls the reference entry points
  * (updateEnergeticParticles, updateMhd, moveNodes) and reads the state back.
@@ -44,12 +42,10 @@
 #include "../include/eprem_gpu.h"
 
 /* ---- timers (defined by src/eprem.c:409-423 in the reference binary) ---- */
-#ifndef REF_HARNESS_NO_TIMERS
 double timer_diffusestream, timer_adiabaticfocus, timer_adiabaticchange,
     timer_diffuseshell, timer_driftshell, timer_eptotal, timer_mas_io,
     timer_eprem_io, timer_init, timer_other, timer_wall, timer_start,
     timer_MPIgatherscatter, timer_MPIsendrecv;
-#endif
 
 extern Index_t maxsubcycles_energychange, maxsubcycles_focusing;
 extern Scalar_t min_tau;
@@ -59,183 +55,11 @@ extern Index_t **computeLines;
 static jmp_buf ref_abort_jmp;
 static int ref_abort_armed = 0;
 
-/* ---- one-rank MPI ------------------------------------------------------- */
-#define REF_MAX_TYPES 256
-static size_t ref_type_size[REF_MAX_TYPES] = {0, 4, 8, 4, 8};
-static int ref_ntypes = 5;
-#define REF_MAX_WINS 4096
-static void *ref_win_ptr[REF_MAX_WINS];
-static int ref_nwins = 1;
-
-static size_t tsize(MPI_Datatype t) {
-  return (t > 0 && t < ref_ntypes) ? ref_type_size[t] : 0;
-}
-static int new_type(size_t size, MPI_Datatype *out) {
-  if (ref_ntypes >= REF_MAX_TYPES) return 1;
-  ref_type_size[ref_ntypes] = size;
-  *out = ref_ntypes++;
-  return 0;
-}
-
-double MPI_Wtime(void) {
-  struct timespec ts;
-  clock_gettime(CLOCK_MONOTONIC, &ts);
-  return ts.tv_sec + 1e-9 * ts.tv_nsec;
-}
-int MPI_Init_thread(int *a, char ***b, int req, int *prov) { (void)a; (void)b; *prov = req; return 0; }
-int MPI_Finalize(void) { return 0; }
-int MPI_Abort(MPI_Comm c, int code) {
-  (void)c;
-  if (ref_abort_armed) longjmp(ref_abort_jmp, code ? code : 2);
-  exit(code);
-}
-int MPI_Barrier(MPI_Comm c) { (void)c; return 0; }
-int MPI_Comm_rank(MPI_Comm c, int *r) { (void)c; *r = 0; return 0; }
-int MPI_Comm_size(MPI_Comm c, int *n) { (void)c; *n = 1; return 0; }
-int MPI_Comm_split_type(MPI_Comm c, int t, int k, MPI_Info i, MPI_Comm *o) {
-  (void)t; (void)k; (void)i; *o = c; return 0;
-}
-int MPI_Get_address(const void *p, MPI_Aint *a) { *a = (MPI_Aint)(ptrdiff_t)p; return 0; }
-int MPI_Type_commit(MPI_Datatype *t) { (void)t; return 0; }
-int MPI_Type_contiguous(int n, MPI_Datatype old, MPI_Datatype *out) {
-  return new_type((size_t)n * tsize(old), out);
-}
-int MPI_Type_create_struct(int n, const int bl[], const MPI_Aint disp[],
-                           const MPI_Datatype types[], MPI_Datatype *out) {
-  size_t ext = 0;
-  for (int i = 0; i < n; i++) {
-    size_t end = (size_t)disp[i] + (size_t)bl[i] * tsize(types[i]);
-    if (end > ext) ext = end;
-  }
-  ext = (ext + 7) & ~(size_t)7;
-  return new_type(ext, out);
-}
-int MPI_Type_create_hvector(int n, int bl, MPI_Aint stride, MPI_Datatype old,
-                            MPI_Datatype *out) {
-  size_t ext = n > 0 ? (size_t)(n - 1) * (size_t)stride + (size_t)bl * tsize(old) : 0;
-  return new_type(ext, out);
-}
-int MPI_Igatherv(const void *sb, int sc, MPI_Datatype st, void *rb, const int rc[],
-                 const int displs[], MPI_Datatype rt, int root, MPI_Comm c, MPI_Request *rq) {
-  (void)rc; (void)root; (void)c;
-  memmove((char *)rb + (size_t)displs[0] * tsize(rt), sb, (size_t)sc * tsize(st));
-  *rq = 0;
-  return 0;
-}
-int MPI_Iscatterv(const void *sb, const int sc[], const int displs[], MPI_Datatype st, void *rb,
-                  int rc, MPI_Datatype rt, int root, MPI_Comm c, MPI_Request *rq) {
-  (void)sc; (void)root; (void)c;
-  memmove(rb, (const char *)sb + (size_t)displs[0] * tsize(st), (size_t)rc * tsize(rt));
-  *rq = 0;
-  return 0;
-}
-int MPI_Gatherv(const void *sb, int sc, MPI_Datatype st, void *rb, const int rc[],
-                const int displs[], MPI_Datatype rt, int root, MPI_Comm c) {
-  MPI_Request r;
-  return MPI_Igatherv(sb, sc, st, rb, rc, displs, rt, root, c, &r);
-}
-int MPI_Isend(const void *b, int n, MPI_Datatype t, int d, int tag, MPI_Comm c, MPI_Request *r) {
-  (void)b; (void)n; (void)t; (void)d; (void)tag; (void)c; *r = 0; return 0;
-}
-int MPI_Irecv(void *b, int n, MPI_Datatype t, int s, int tag, MPI_Comm c, MPI_Request *r) {
-  (void)b; (void)n; (void)t; (void)s; (void)tag; (void)c; *r = 0; return 0;
-}
-int MPI_Send(const void *b, int n, MPI_Datatype t, int d, int tag, MPI_Comm c) {
-  (void)b; (void)n; (void)t; (void)d; (void)tag; (void)c; return 0;
-}
-int MPI_Waitall(int n, MPI_Request r[], MPI_Status s[]) { (void)n; (void)r; (void)s; return 0; }
-int MPI_Reduce(const void *sb, void *rb, int n, MPI_Datatype t, MPI_Op op, int root, MPI_Comm c) {
-  (void)op; (void)root; (void)c;
-  memmove(rb, sb, (size_t)n * tsize(t));
-  return 0;
-}
-int MPI_Allgather(const void *sb, int sc, MPI_Datatype st, void *rb, int rc, MPI_Datatype rt,
-                  MPI_Comm c) {
-  (void)rc; (void)rt; (void)c;
-  memmove(rb, sb, (size_t)sc * tsize(st));
-  return 0;
-}
-int MPI_Win_allocate_shared(MPI_Aint size, int du, MPI_Info i, MPI_Comm c, void *base, MPI_Win *w) {
-  (void)du; (void)i; (void)c;
-  if (ref_nwins >= REF_MAX_WINS) return 1;
-  void *p = calloc(size > 0 ? (size_t)size : 1, 1);
-  ref_win_ptr[ref_nwins] = p;
-  *(void **)base = p;
-  *w = ref_nwins++;
-  return 0;
-}
-int MPI_Win_shared_query(MPI_Win w, int rank, MPI_Aint *size, int *du, void *base) {
-  (void)rank;
-  *size = 0;
-  *du = 1;
-  *(void **)base = (w > 0 && w < ref_nwins) ? ref_win_ptr[w] : NULL;
-  return 0;
-}
-int MPI_Win_lock_all(int a, MPI_Win w) { (void)a; (void)w; return 0; }
-int MPI_Win_unlock_all(MPI_Win w) { (void)w; return 0; }
-int MPI_Win_sync(MPI_Win w) { (void)w; return 0; }
-int MPI_Win_free(MPI_Win *w) {
-  if (*w > 0 && *w < ref_nwins) { free(ref_win_ptr[*w]); ref_win_ptr[*w] = NULL; }
-  return 0;
-}
-
-/* ---- libconfig / netCDF / HDF5: never used by the harness --------------- */
-void config_init(config_t *c) { (void)c; }
-void config_destroy(config_t *c) { (void)c; }
-int config_read_file(config_t *c, const char *f) { (void)c; (void)f; return 0; }
-int config_error_line(const config_t *c) { (void)c; return 0; }
-const char *config_error_text(const config_t *c) { (void)c; return "no config reader in harness"; }
-int config_lookup_int(const config_t *c, const char *p, int *v) { (void)c; (void)p; (void)v; return 0; }
-int config_lookup_float(const config_t *c, const char *p, double *v) { (void)c; (void)p; (void)v; return 0; }
-int config_lookup_string(const config_t *c, const char *p, const char **v) { (void)c; (void)p; (void)v; return 0; }
-config_setting_t *config_lookup(const config_t *c, const char *p) { (void)c; (void)p; return NULL; }
-double config_setting_get_float_elem(const config_setting_t *s, int i) { (void)s; (void)i; return 0.0; }
-
-#define NC_FAIL (-1)
-const char *nc_strerror(int e) { (void)e; return "no netCDF in harness"; }
-int nc_create(const char *p, int m, int *id) { (void)p; (void)m; (void)id; return NC_FAIL; }
-int nc_open(const char *p, int m, int *id) { (void)p; (void)m; (void)id; return NC_FAIL; }
-int nc_close(int id) { (void)id; return NC_FAIL; }
-int nc_enddef(int id) { (void)id; return NC_FAIL; }
-int nc_def_dim(int id, const char *n, size_t l, int *d) { (void)id; (void)n; (void)l; (void)d; return NC_FAIL; }
-int nc_def_var(int id, const char *n, nc_type t, int nd, const int *d, int *v) {
-  (void)id; (void)n; (void)t; (void)nd; (void)d; (void)v; return NC_FAIL;
-}
-int nc_inq_varid(int id, const char *n, int *v) { (void)id; (void)n; (void)v; return NC_FAIL; }
-int nc_put_att_text(int id, int v, const char *n, size_t l, const char *t) {
-  (void)id; (void)v; (void)n; (void)l; (void)t; return NC_FAIL;
-}
-int nc_put_att_double(int id, int v, const char *n, nc_type t, size_t l, const double *x) {
-  (void)id; (void)v; (void)n; (void)t; (void)l; (void)x; return NC_FAIL;
-}
-int nc_put_var(int id, int v, const void *x) { (void)id; (void)v; (void)x; return NC_FAIL; }
-int nc_put_var_double(int id, int v, const double *x) { (void)id; (void)v; (void)x; return NC_FAIL; }
-int nc_put_var1_double(int id, int v, const size_t *i, const double *x) {
-  (void)id; (void)v; (void)i; (void)x; return NC_FAIL;
-}
-int nc_put_vara_double(int id, int v, const size_t *s, const size_t *c, const double *x) {
-  (void)id; (void)v; (void)s; (void)c; (void)x; return NC_FAIL;
-}
-int nc_put_vara_int(int id, int v, const size_t *s, const size_t *c, const int *x) {
-  (void)id; (void)v; (void)s; (void)c; (void)x; return NC_FAIL;
-}
-int nc_put_varm_double(int id, int v, const size_t *s, const size_t *c, const ptrdiff_t *st,
-                       const ptrdiff_t *im, const double *x) {
-  (void)id; (void)v; (void)s; (void)c; (void)st; (void)im; (void)x; return NC_FAIL;
-}
-
-hid_t H5Fopen(const char *n, unsigned f, hid_t p) { (void)n; (void)f; (void)p; return -1; }
-herr_t H5Fclose(hid_t h) { (void)h; return -1; }
-hid_t H5Dopen2(hid_t h, const char *n, hid_t p) { (void)h; (void)n; (void)p; return -1; }
-herr_t H5Dclose(hid_t h) { (void)h; return -1; }
-hid_t H5Dget_type(hid_t h) { (void)h; return -1; }
-hid_t H5Dget_space(hid_t h) { (void)h; return -1; }
-int H5Tequal(hid_t a, hid_t b) { (void)a; (void)b; return 0; }
-herr_t H5Tclose(hid_t h) { (void)h; return -1; }
-herr_t H5Sclose(hid_t h) { (void)h; return -1; }
-hssize_t H5Sget_simple_extent_npoints(hid_t h) { (void)h; return -1; }
-herr_t H5Dread(hid_t a, hid_t b, hid_t c, hid_t d, hid_t e, void *x) {
-  (void)a; (void)b; (void)c; (void)d; (void)e; (void)x; return -1;
+/* MPI, libconfig, netCDF and HDF5 come from ref_shims.c. */
+extern void (*refshim_abort_hook)(int code);
+extern size_t refshim_type_size(MPI_Datatype t);
+static void ref_abort(int code) {
+  if (ref_abort_armed) longjmp(ref_abort_jmp, code);
 }
 
 /* ---- harness API -------------------------------------------------------- */
@@ -435,6 +259,7 @@ int ref_update_energetic_particles(double tg, eprem_ep_stats_t *st) {
   maxsubcycles_energychange = 0;
   maxsubcycles_focusing = 0;
   min_tau = DBL_MAX;
+  refshim_abort_hook = ref_abort;
   ref_abort_armed = 1;
   int code = setjmp(ref_abort_jmp);
   if (code == 0) updateEnergeticParticles();
@@ -457,7 +282,7 @@ int ref_move_nodes(double dt) {
 }
 
 int ref_node_t_size(void) { return (int)sizeof(Node_t); }
-int ref_node_T_extent(void) { return (int)tsize(Node_T); }
+int ref_node_T_extent(void) { return (int)refshim_type_size(Node_T); }
 
 /* ---- MAS background ------------------------------------------------------ */
 /* Point the reference's MAS globals (src/readMAS.h) at caller arrays, as

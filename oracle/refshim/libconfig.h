@@ -1,11 +1,12 @@
 /* Declarations of the libconfig calls made by the EPREM reference's
- * configuration.c, so that file compiles into the oracle library.  The oracle
- * never reads a config file: the harness fills the reference's `config`
- * struct directly.  Test infrastructure, not part of the product. */
+ * configuration.c.  Defined by oracle/ref_shims.c, which reads the libconfig
+ * file syntax; the per-operator harness never reads a file and fills the
+ * reference's `config` struct directly.  Test infrastructure, not part of the
+ * product. */
 #ifndef EPREM_REFSHIM_LIBCONFIG_H
 #define EPREM_REFSHIM_LIBCONFIG_H
-typedef struct config_t { int unused; } config_t;
-typedef struct config_setting_t { int unused; } config_setting_t;
+typedef struct config_t { void *impl; } config_t;
+typedef struct config_setting_t config_setting_t;
 #define CONFIG_TRUE 1
 #define CONFIG_FALSE 0
 void config_init(config_t *);

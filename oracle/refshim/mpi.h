@@ -1,7 +1,7 @@
-/* One-rank MPI declarations used only to compile the EPREM reference sources
- * into the per-operator oracle library.  Nothing here talks to other
- * processes: the definitions in ref_harness.c behave as MPI_COMM_WORLD with a
- * single rank.  Test infrastructure, not part of the product. */
+/* One-rank MPI declarations used to compile the EPREM reference sources into
+ * the oracle harness.  Nothing here talks to other processes: the definitions
+ * in oracle/ref_shims.c behave as MPI_COMM_WORLD with a single rank.  Test
+ * infrastructure, not part of the product. */
 #ifndef EPREM_REFSHIM_MPI_H
 #define EPREM_REFSHIM_MPI_H
 #include <stddef.h>

@@ -1,6 +1,7 @@
-/* Declarations of the netCDF calls made by the EPREM reference's output code,
- * so that it links into the oracle library.  The oracle writes no files.
- * Test infrastructure, not part of the product. */
+/* Declarations of the netCDF calls made by the EPREM reference's output code.
+ * Defined by oracle/ref_shims.c as an in-memory capture that writes each
+ * closed dataset to <path>.cap.  Test infrastructure, not part of the
+ * product. */
 #ifndef EPREM_REFSHIM_NETCDF_H
 #define EPREM_REFSHIM_NETCDF_H
 #include <stddef.h>
@@ -24,6 +25,7 @@ int nc_put_att_text(int, int, const char *, size_t, const char *);
 int nc_put_att_double(int, int, const char *, nc_type, size_t, const double *);
 int nc_put_var(int, int, const void *);
 int nc_put_var_double(int, int, const double *);
+int nc_put_var1_double(int, int, const size_t *, const double *);
 int nc_put_vara_double(int, int, const size_t *, const size_t *, const double *);
 int nc_put_vara_int(int, int, const size_t *, const size_t *, const int *);
 int nc_put_varm_double(int, int, const size_t *, const size_t *, const ptrdiff_t *, const ptrdiff_t *, const double *);
