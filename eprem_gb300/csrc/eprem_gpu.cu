@@ -556,6 +556,17 @@ extern "C" int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
   return EPREM_GPU_OK;
 }
 
+extern "C" int eprem_gpu_set_time_step(eprem_gpu_run *r, double t_del) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (!(t_del > 0.0) || !std::isfinite(t_del)) return fail(EPREM_GPU_ERR_ARG, "t_del must be finite and > 0");
+  // every launch takes the run view by value: later launches see the new step
+  r->params.t_del = t_del;
+  r->v.dt = t_del / (1.0 * r->params.num_ep_steps);  // src/energeticParticles.c:99
+  r->v.dt_full = r->v.dt * r->params.num_ep_steps;
+  r->mhd.t_del = t_del;
+  return EPREM_GPU_OK;
+}
+
 extern "C" int eprem_gpu_omni_flux(eprem_gpu_run *r, double *out) {
   if (!r || !out) return fail(EPREM_GPU_ERR_ARG, "null argument");
   const size_t n = r->sn() * r->dims.num_energies;

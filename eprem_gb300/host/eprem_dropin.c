@@ -48,6 +48,7 @@
 #include "eprem_gpu.h"
 
 static eprem_gpu_run *dropin_run = NULL;
+static double dropin_t_del = 0.0;   /* config.tDel as last passed to the run */
 static double *dropin_f = NULL;     /* [S][N][E][M] host staging of eParts   */
 static double *dropin_nodes = NULL; /* [field][S*N] host staging of grid[]   */
 static size_t dropin_sn = 0, dropin_cells = 0;
@@ -169,11 +170,21 @@ static void dropin_init(void) {
   g.dlnp = dlnp;
   g.dmu = dmu;
   dropin_check(eprem_gpu_create(&d, &p, &g, &dropin_run), "eprem_gpu_create");
+  dropin_t_del = config.tDel;
   dropin_sn = (size_t)d.num_streams * d.num_nodes;
   dropin_cells = dropin_sn * d.num_energies * d.num_mu;
   dropin_f = (double *)malloc(sizeof(double) * dropin_cells);
   dropin_nodes = (double *)malloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
   if (!dropin_f || !dropin_nodes) panic("GPU path: host staging allocation failed");
+}
+
+/* SetDT (src/simCore.c:800-880) changes config.tDel between steps of a
+ * MAS-coupled run: pass the current value on before each call. */
+static void dropin_sync_step(void) {
+  if (config.tDel != dropin_t_del) {
+    dropin_check(eprem_gpu_set_time_step(dropin_run, config.tDel), "time step");
+    dropin_t_del = config.tDel;
+  }
 }
 
 /* grid[] shells 1..N of every stream <-> nodes[field][s*N+k] (k = shell-1) */
@@ -223,6 +234,7 @@ static void dropin_unpack_f(void) {
 
 void updateEnergeticParticles(void) {
   dropin_init();
+  dropin_sync_step();
   double t0 = MPI_Wtime();
   dropin_pack_f();
   dropin_pack_nodes(DROPIN_EP_IN);
@@ -300,6 +312,7 @@ static void dropin_mas_sync(void) {
 
 void updateMhd(void) {
   dropin_init();
+  dropin_sync_step();
   const uint64_t all = EPREM_NODE_MASK_ALL;
   if (mhdGridStatus == MHD_MAS) {
     dropin_mas_sync();
@@ -316,6 +329,7 @@ void updateMhd(void) {
 
 void moveNodes(Scalar_t dt) {
   dropin_init();
+  dropin_sync_step();
   const uint64_t mv = EPREM_NODE_MASK(EPREM_NODE_RX) | EPREM_NODE_MASK(EPREM_NODE_RY) |
                       EPREM_NODE_MASK(EPREM_NODE_RZ) | EPREM_NODE_MASK(EPREM_NODE_RMAG) |
                       EPREM_NODE_MASK(EPREM_NODE_VVEC_X) | EPREM_NODE_MASK(EPREM_NODE_VVEC_Y) |
@@ -330,6 +344,7 @@ void moveNodes(Scalar_t dt) {
 
 void masMoveNodes(Scalar_t dt) {
   dropin_init();
+  dropin_sync_step();
   dropin_mas_sync();
   const uint64_t all = EPREM_NODE_MASK_ALL;
   dropin_pack_nodes(all);

@@ -36,6 +36,7 @@ EXPORTS = [
     ("eprem_gpu_read_stats", C.c_int, [C.c_void_p, C.POINTER(abi.EpStats)]),
     ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_set_time_step", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_omni_flux_static", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_synchronize", C.c_int, [C.c_void_p]),
@@ -203,6 +204,11 @@ class EpremRun:
     def move_nodes(self, dt: float):
         """moveNodes (src/simCore.c:737-785)."""
         self._check(self.lib.eprem_gpu_move_nodes(self.handle, dt))
+
+    def set_time_step(self, t_del: float):
+        """A new config.tDel from the next call on, as SetDT
+        (src/simCore.c:800-880) sets it in MAS-coupled runs."""
+        self._check(self.lib.eprem_gpu_set_time_step(self.handle, t_del))
 
     # -- MAS background ------------------------------------------------------
     def mas_init(self, mas_params: abi.MasParams):

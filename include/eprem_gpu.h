@@ -253,6 +253,15 @@ int eprem_gpu_update_mhd(eprem_gpu_run *run, double t_global);
  * the node's flow velocity (src/simCore.c:737-785, delrFlow src/flow.c:162-196). */
 int eprem_gpu_move_nodes(eprem_gpu_run *run, double dt);
 
+/* The step length config.tDel (AU/c), which MAS-coupled runs change between
+ * steps: SetDT (src/simCore.c:800-880) sets it to the spacing of the MAS
+ * slice times around t_global.  It sets the EP sub-step dt = t_del /
+ * numEpSteps (src/energeticParticles.c:99) and the time scale of the
+ * background's divV.  Takes effect from the next call; an ensemble captured
+ * before the change keeps the step it captured (rebuild it).  t_del must be
+ * finite and > 0. */
+int eprem_gpu_set_time_step(eprem_gpu_run *run, double t_del);
+
 /* Omnidirectional flux J = 2 E <f>_mu per (stream, node, energy), the
  * quantity computeFlux writes (src/unifiedOutput.c:153-180), without its
  * output unit scale.  out: S*N*E doubles, host memory.  Synchronizes. */

@@ -111,6 +111,12 @@ int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, "moveNodes");
 }
 
+int eprem_gpu_set_time_step(eprem_gpu_run *r, double t_del) {
+  if (!(t_del > 0.0)) return abi_fail(EPREM_GPU_ERR_ARG, "t_del must be > 0");
+  r->p.t_del = t_del;
+  return EPREM_GPU_OK;
+}
+
 int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp) {
   r->mas.p = *mp;
   r->mas.slot0 = &r->slot[0];

@@ -22,7 +22,8 @@
  *     oracle/digest.py: every variable with its type, shape (the unlimited
  *     dimension at its current length), scale_factor / add_offset and values;
  *     unwritten values hold netCDF's default fill values.
- *   - HDF5: entry points that report failure (MAS file input is not read).
+ *   - HDF5: a read-only reader of the file-format subset the MAS slice files
+ *     use (see the HDF5 section below).
  */
 #include <limits.h>
 #include <stdint.h>
@@ -856,18 +857,299 @@ int nc_close(int id) {
 }
 
 /* ======================================================================== */
-/* HDF5: MAS file input is not read                                          */
+/* HDF5: the subset the MAS slice files use                                  */
 /* ======================================================================== */
-hid_t H5Fopen(const char *n, unsigned f, hid_t p) { (void)n; (void)f; (void)p; return -1; }
-herr_t H5Fclose(hid_t h) { (void)h; return -1; }
-hid_t H5Dopen2(hid_t h, const char *n, hid_t p) { (void)h; (void)n; (void)p; return -1; }
-herr_t H5Dclose(hid_t h) { (void)h; return -1; }
-hid_t H5Dget_type(hid_t h) { (void)h; return -1; }
-hid_t H5Dget_space(hid_t h) { (void)h; return -1; }
-int H5Tequal(hid_t a, hid_t b) { (void)a; (void)b; return 0; }
-herr_t H5Tclose(hid_t h) { (void)h; return -1; }
-herr_t H5Sclose(hid_t h) { (void)h; return -1; }
-hssize_t H5Sget_simple_extent_npoints(hid_t h) { (void)h; return -1; }
-herr_t H5Dread(hid_t a, hid_t b, hid_t c, hid_t d, hid_t e, void *x) {
-  (void)a; (void)b; (void)c; (void)d; (void)e; (void)x; return -1;
+/* Read-only, whole file in memory.  Follows the published HDF5 file format:
+ * superblock version 0 or 1; the root group's symbol table (version-1 B-tree
+ * of group nodes, symbol table nodes "SNOD", local heap "HEAP" for names);
+ * version-1 object headers with continuation blocks; dataspace, datatype and
+ * data layout messages (layout versions 1-3, contiguous or compact storage).
+ * Datasets must be IEEE floats or integers in little-endian order; chunked
+ * or filtered storage, other superblock versions and nested groups are
+ * refused (the open fails).  Handles: files, datasets, their dataspaces and
+ * datatypes share one table; the datatype handle of a little-endian 4-byte
+ * float is H5T_NATIVE_FLOAT and of an 8-byte one H5T_NATIVE_DOUBLE. */
+#define H5S_MAX_OBJ 1024
+#define H5S_MAX_RANK 8
+typedef struct {
+  int kind;            /* 0 free, 1 file, 2 dataset, 3 dataspace */
+  unsigned char *buf;  /* file: contents */
+  size_t size;
+  int so, sl;          /* sizes of offsets and lengths */
+  uint64_t root_btree, root_heap_data;
+  int file;            /* dataset / dataspace: owning file handle */
+  int rank;
+  uint64_t dims[H5S_MAX_RANK];
+  int tclass, tsize, tbig;  /* datatype class (0 int, 1 float), size, big-endian */
+  int layout;          /* 0 compact, 1 contiguous */
+  uint64_t addr, nbytes;
+  size_t compact_at;   /* compact data offset in buf */
+} h5s_obj;
+static h5s_obj h5s_tab[H5S_MAX_OBJ];
+#define H5S_BASE 100  /* handles are H5S_BASE + table index (small values are type constants) */
+
+static int h5s_new(int kind) {
+  for (int k = 0; k < H5S_MAX_OBJ; k++)
+    if (h5s_tab[k].kind == 0) {
+      memset(&h5s_tab[k], 0, sizeof(h5s_tab[k]));
+      h5s_tab[k].kind = kind;
+      return k;
+    }
+  return -1;
+}
+static h5s_obj *h5s_get(hid_t h, int kind) {
+  const long long k = (long long)h - H5S_BASE;
+  return (k >= 0 && k < H5S_MAX_OBJ && h5s_tab[k].kind == kind) ? &h5s_tab[k] : NULL;
+}
+static int h5s_rd(const h5s_obj *f, uint64_t at, int n, uint64_t *v) {
+  if (at + (uint64_t)n > f->size) return -1;
+  uint64_t x = 0;
+  for (int i = n - 1; i >= 0; i--) x = (x << 8) | f->buf[at + (uint64_t)i];
+  *v = x;
+  return 0;
+}
+#define H5RD(f, at, n, v) do { if (h5s_rd((f), (at), (n), (v))) return -1; } while (0)
+
+hid_t H5Fopen(const char *name, unsigned flags, hid_t plist) {
+  (void)flags; (void)plist;
+  FILE *fp = fopen(name, "rb");
+  if (!fp) return -1;
+  fseek(fp, 0, SEEK_END);
+  long sz = ftell(fp);
+  fseek(fp, 0, SEEK_SET);
+  if (sz < 96) { fclose(fp); return -1; }
+  int k = h5s_new(1);
+  if (k < 0) { fclose(fp); return -1; }
+  h5s_obj *f = &h5s_tab[k];
+  f->buf = (unsigned char *)malloc((size_t)sz);
+  f->size = fread(f->buf, 1, (size_t)sz, fp);
+  fclose(fp);
+  static const unsigned char sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+  const int ver = f->size >= 16 ? f->buf[8] : -1;
+  if (memcmp(f->buf, sig, 8) != 0 || (ver != 0 && ver != 1) || f->buf[13] != 8 ||
+      f->buf[14] != 8) {
+    free(f->buf);
+    f->kind = 0;
+    return -1;
+  }
+  f->so = f->buf[13];
+  f->sl = f->buf[14];
+  /* 24 fixed bytes (+4 in version 1), four addresses, then the root entry:
+   * link name offset, object header address, cache type, reserved, scratch
+   * pad holding the B-tree and local heap addresses (cache type 1). */
+  const uint64_t root = 24 + (ver == 1 ? 4 : 0) + 4 * 8;
+  uint64_t cache, heap, hdata;
+  if (h5s_rd(f, root + 16, 4, &cache) || cache != 1 ||
+      h5s_rd(f, root + 24, 8, &f->root_btree) || h5s_rd(f, root + 32, 8, &heap) ||
+      heap + 32 > f->size || memcmp(f->buf + heap, "HEAP", 4) != 0 ||
+      h5s_rd(f, heap + 24, 8, &hdata)) {
+    free(f->buf);
+    f->kind = 0;
+    return -1;
+  }
+  f->root_heap_data = hdata;
+  return H5S_BASE + k;
+}
+herr_t H5Fclose(hid_t h) {
+  h5s_obj *f = h5s_get(h, 1);
+  if (!f) return -1;
+  free(f->buf);
+  f->kind = 0;
+  return 0;
+}
+
+/* Object header address of `name` under the B-tree node at `node`, or 0. */
+static uint64_t h5s_find(const h5s_obj *f, uint64_t node, const char *name, int depth) {
+  if (depth > 16 || node + 24 > f->size || memcmp(f->buf + node, "TREE", 4) != 0 ||
+      f->buf[node + 4] != 0)
+    return 0;
+  const int level = f->buf[node + 5];
+  uint64_t n;
+  if (h5s_rd(f, node + 6, 2, &n)) return 0;
+  uint64_t p = node + 8 + 16;  /* after the two sibling addresses */
+  for (uint64_t i = 0; i < n; i++) {
+    uint64_t child;
+    p += 8;  /* key: heap offset */
+    if (h5s_rd(f, p, 8, &child)) return 0;
+    p += 8;
+    if (level > 0) {
+      const uint64_t r = h5s_find(f, child, name, depth + 1);
+      if (r) return r;
+      continue;
+    }
+    if (child + 8 > f->size || memcmp(f->buf + child, "SNOD", 4) != 0) return 0;
+    uint64_t ns;
+    if (h5s_rd(f, child + 6, 2, &ns)) return 0;
+    for (uint64_t e = 0; e < ns; e++) {
+      const uint64_t ent = child + 8 + 40 * e;
+      uint64_t lno, oh;
+      if (h5s_rd(f, ent, 8, &lno) || h5s_rd(f, ent + 8, 8, &oh)) return 0;
+      const uint64_t at = f->root_heap_data + lno;
+      if (at >= f->size) return 0;
+      const size_t maxlen = f->size - at;
+      if (strnlen((const char *)f->buf + at, maxlen) < maxlen &&
+          strcmp((const char *)f->buf + at, name) == 0)
+        return oh;
+    }
+  }
+  return 0;
+}
+
+static int h5s_message(const h5s_obj *f, h5s_obj *d, int type, uint64_t at, uint64_t len) {
+  if (at + len > f->size) return -1;
+  uint64_t v;
+  if (type == 0x0001) { /* dataspace */
+    const int ver = f->buf[at], rank = f->buf[at + 1];
+    if (rank > H5S_MAX_RANK || (ver != 1 && ver != 2)) return -1;
+    const uint64_t dims_at = at + (ver == 1 ? 8 : 4);
+    d->rank = rank;
+    for (int k = 0; k < rank; k++) { H5RD(f, dims_at + 8 * (uint64_t)k, 8, &v); d->dims[k] = v; }
+  } else if (type == 0x0003) { /* datatype */
+    d->tclass = f->buf[at] & 0x0f;
+    d->tbig = f->buf[at + 1] & 1;
+    H5RD(f, at + 4, 4, &v);
+    d->tsize = (int)v;
+  } else if (type == 0x0008) { /* data layout */
+    const int ver = f->buf[at];
+    if (ver == 3) {
+      const int cls = f->buf[at + 1];
+      if (cls == 1) {
+        d->layout = 1;
+        H5RD(f, at + 2, 8, &d->addr);
+        H5RD(f, at + 10, 8, &d->nbytes);
+      } else if (cls == 0) {
+        d->layout = 0;
+        H5RD(f, at + 2, 2, &v);
+        d->nbytes = v;
+        d->compact_at = (size_t)(at + 4);
+      } else {
+        return -1; /* chunked */
+      }
+    } else if (ver == 1 || ver == 2) {
+      const int nd = f->buf[at + 1], cls = f->buf[at + 2];
+      if (cls == 1) {
+        d->layout = 1;
+        H5RD(f, at + 8, 8, &d->addr);
+        d->nbytes = (uint64_t)-1; /* from the dataspace */
+      } else if (cls == 0) {
+        d->layout = 0;
+        const uint64_t sz_at = at + 8 + 4 * (uint64_t)nd;
+        H5RD(f, sz_at, 4, &v);
+        d->nbytes = v;
+        d->compact_at = (size_t)(sz_at + 4);
+      } else {
+        return -1;
+      }
+    } else {
+      return -1;
+    }
+  } else if (type == 0x000B) { /* filter pipeline: not supported */
+    return -1;
+  }
+  return 0;
+}
+
+hid_t H5Dopen2(hid_t file, const char *name, hid_t plist) {
+  (void)plist;
+  h5s_obj *f = h5s_get(file, 1);
+  if (!f || !name) return -1;
+  const uint64_t oh = h5s_find(f, f->root_btree, name, 0);
+  if (!oh || oh + 16 > f->size || f->buf[oh] != 1) return -1;
+  const int fk = (int)(f - h5s_tab);
+  int k = h5s_new(2);
+  if (k < 0) return -1;
+  f = &h5s_tab[fk];
+  h5s_obj *d = &h5s_tab[k];
+  d->file = H5S_BASE + fk;
+  d->tclass = -1;
+  d->layout = -1;
+  uint64_t nmsg, hsize;
+  if (h5s_rd(f, oh + 2, 2, &nmsg) || h5s_rd(f, oh + 8, 4, &hsize)) { d->kind = 0; return -1; }
+  /* message blocks: the header's own, then continuation blocks */
+  uint64_t blk_at[64], blk_len[64];
+  int nblk = 1, seen = 0;
+  blk_at[0] = oh + 16;
+  blk_len[0] = hsize;
+  for (int b = 0; b < nblk && (uint64_t)seen < nmsg; b++) {
+    uint64_t p = blk_at[b];
+    const uint64_t end = blk_at[b] + blk_len[b];
+    while (p + 8 <= end && (uint64_t)seen < nmsg) {
+      uint64_t type, len;
+      if (h5s_rd(f, p, 2, &type) || h5s_rd(f, p + 2, 2, &len)) { d->kind = 0; return -1; }
+      if (type == 0x0010) {
+        uint64_t ca, cl;
+        if (nblk >= 64 || h5s_rd(f, p + 8, 8, &ca) || h5s_rd(f, p + 16, 8, &cl)) {
+          d->kind = 0;
+          return -1;
+        }
+        blk_at[nblk] = ca;
+        blk_len[nblk++] = cl;
+      } else if (h5s_message(f, d, (int)type, p + 8, len)) {
+        d->kind = 0;
+        return -1;
+      }
+      seen++;
+      p += 8 + len;
+    }
+  }
+  if (d->layout < 0 || d->tclass < 0 || d->tbig) { d->kind = 0; return -1; }
+  uint64_t npts = 1;
+  for (int r = 0; r < d->rank; r++) npts *= d->dims[r];
+  const uint64_t need = npts * (uint64_t)d->tsize;
+  if (d->nbytes == (uint64_t)-1) d->nbytes = need;
+  const uint64_t start = d->layout == 1 ? d->addr : d->compact_at;
+  if (d->nbytes < need || start + need > f->size) { d->kind = 0; return -1; }
+  return H5S_BASE + k;
+}
+herr_t H5Dclose(hid_t h) {
+  h5s_obj *d = h5s_get(h, 2);
+  if (!d) return -1;
+  d->kind = 0;
+  return 0;
+}
+hid_t H5Dget_type(hid_t h) {
+  h5s_obj *d = h5s_get(h, 2);
+  if (!d) return -1;
+  if (d->tclass == 1 && d->tsize == 4) return H5T_NATIVE_FLOAT;
+  if (d->tclass == 1 && d->tsize == 8) return H5T_NATIVE_DOUBLE;
+  return 3; /* some other type */
+}
+int H5Tequal(hid_t a, hid_t b) { return a >= 0 && a == b; }
+herr_t H5Tclose(hid_t h) { return h >= 0 ? 0 : -1; }
+hid_t H5Dget_space(hid_t h) {
+  h5s_obj *d = h5s_get(h, 2);
+  if (!d) return -1;
+  int k = h5s_new(3);
+  if (k < 0) return -1;
+  d = h5s_get(h, 2);
+  h5s_tab[k].rank = d->rank;
+  memcpy(h5s_tab[k].dims, d->dims, sizeof(d->dims));
+  return H5S_BASE + k;
+}
+herr_t H5Sclose(hid_t h) {
+  h5s_obj *s = h5s_get(h, 3);
+  if (!s) return -1;
+  s->kind = 0;
+  return 0;
+}
+hssize_t H5Sget_simple_extent_npoints(hid_t h) {
+  h5s_obj *s = h5s_get(h, 3);
+  if (!s) return -1;
+  hssize_t n = 1;
+  for (int r = 0; r < s->rank; r++) n *= (hssize_t)s->dims[r];
+  return n;
+}
+/* Whole-dataset reads only (H5S_ALL selections) into a buffer of the file's
+ * own type. */
+herr_t H5Dread(hid_t dset, hid_t memtype, hid_t memspace, hid_t filespace, hid_t xfer, void *out) {
+  (void)xfer;
+  h5s_obj *d = h5s_get(dset, 2);
+  if (!d || memspace != H5S_ALL || filespace != H5S_ALL || memtype != H5Dget_type(dset)) return -1;
+  h5s_obj *f = h5s_get(d->file, 1);
+  if (!f) return -1;
+  uint64_t npts = 1;
+  for (int r = 0; r < d->rank; r++) npts *= d->dims[r];
+  const uint64_t start = d->layout == 1 ? d->addr : d->compact_at;
+  memcpy(out, f->buf + start, (size_t)(npts * (uint64_t)d->tsize));
+  return 0;
 }

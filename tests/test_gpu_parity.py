@@ -144,6 +144,41 @@ def test_mhd_and_node_push_match_oracle(oracle_lib):
         assert err <= tol, (name, err)
 
 
+def test_time_step_change_between_calls(oracle_lib):
+    """SetDT (src/simCore.c:800-880) changes config.tDel between the steps of
+    a MAS-coupled run; eprem_gpu_set_time_step passes the new step on.  One
+    update at the configured step, then the step cut to a third: f against
+    the oracle run with the same two steps, and the background's divV (which
+    divides by the step) after updateMhd."""
+    import ctypes as C
+    w = W.testsuite_like("cone", 1, 1, 40)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    gs, keep = W.grids_struct(g)
+    p2 = abi.Params.from_buffer_copy(w.params)
+    p2.t_del = w.params.t_del / 3.0
+    f_ref, n_ref = f.copy(), nodes.copy()
+    for p in (w.params, p2):
+        rc, _, err = oracle_lib.update_energetic_particles(d, p, gs, f_ref, n_ref, nthreads=8)
+        assert rc == 0, err
+    t = 1.0 / W.DAY
+    oracle_lib.update_mhd(d, p2, n_ref, t)
+    run = EpremRun(d, w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles(0.0)
+    run.set_time_step(p2.t_del)
+    run.update_energetic_particles(0.0)
+    run.update_mhd(t)
+    f_gpu = run.download_f()
+    n_gpu = run.download_nodes()
+    with pytest.raises(RuntimeError):
+        run.set_time_step(0.0)
+    run.close()
+    assert rel_err(f_gpu, f_ref) <= F_RTOL
+    divv, divv_ref = n_gpu[abi.NODE["DIVV"]], n_ref[abi.NODE["DIVV"]]
+    assert np.max(np.abs(divv - divv_ref)) <= 1e-10 * np.max(np.abs(divv_ref))
+
+
 def test_omni_flux_matches_oracle(oracle_lib):
     w = W.custom(1, 1, 30, 8, 6)
     d, g, f, nodes = primed_state(w, oracle_lib)

@@ -1,23 +1,26 @@
 """Whole runs of the reference's own testsuite, checked against its goldens.
 
 The reference's testsuite (testsuite/run_test_suite.sh in the reference) runs
-the EPREM driver on the `seed`, `wind` and `cone` configurations and passes a
-case when the text digest of its observer output is identical to the stored
+the EPREM driver on five configurations -- `seed`, `wind`, `cone` (ideal
+shock), `mas_wind` and `mas_cme` (MAS-coupled, HDF5 slice input) -- and passes
+a case when the text digest of its observer output is identical to the stored
 testsuite/<case>/reference/eprem_digest.txt (SHA-256 of every variable plus
 6-significant-figure statistics); its eprem.log records the per-step
 sub-cycle maxima and minimum tau.
 
 Two binaries are run on each case (oracle/Makefile, reference tree needed):
   * eprem_ref: the reference's unchanged driver and sources with the one-rank
-    MPI, config reader and netCDF capture of oracle/ref_shims.c -- shows the
-    harness reproduces the goldens (they were made with 6 MPI ranks);
+    MPI, config reader, netCDF capture and HDF5 reader of oracle/ref_shims.c
+    -- shows the harness reproduces the goldens (they were made with 6 MPI
+    ranks);
   * eprem_oracle_dropin: the same driver with updateEnergeticParticles,
-    updateMhd and moveNodes resolved to eprem_gb300/host/eprem_dropin.c over
-    the CPU restatement -- pins the restatement and the drop-in's packing of
-    the reference globals on whole runs (shell spawning, the ideal shock,
-    output), bit for bit.
-The reference run of `cone` (about 2.5 minutes) runs when EPREM_SLOW_TESTS is
-set; the drop-in run of `cone` always runs.
+    updateMhd, moveNodes and masMoveNodes resolved to
+    eprem_gb300/host/eprem_dropin.c over the CPU restatement -- pins the
+    restatement and the drop-in's handling of the reference globals on whole
+    runs (shell spawning, the ideal shock, MAS slices and SetDT's time-step
+    changes, output), bit for bit.
+The reference's own runs of `cone` and `mas_wind` (2.5 and 3 minutes) run
+when EPREM_SLOW_TESTS is set; every drop-in run always runs.
 """
 import concurrent.futures as cf
 import os
@@ -35,13 +38,14 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "testsuite")),
                                 reason="reference source tree not present")
 
-CASES = ["seed", "wind", "cone"]
+CASES = ["seed", "wind", "cone", "mas_wind", "mas_cme"]
+SLOW_REF = {"cone", "mas_wind"}
 SLOW = bool(os.environ.get("EPREM_SLOW_TESTS"))
 
 
 def _runs():
     out = [("eprem_oracle_dropin", c) for c in CASES]
-    out += [("eprem_ref", c) for c in CASES if c != "cone" or SLOW]
+    out += [("eprem_ref", c) for c in CASES if c not in SLOW_REF or SLOW]
     return out
 
 
@@ -54,8 +58,12 @@ def testsuite_runs(tmp_path_factory):
 
     def run(key):
         exe, case = key
-        d = base / f"{exe}_{case}"
-        d.mkdir()
+        # the testsuite's layout: <case>/run holds the config, MAS inputs are
+        # read from ../input/data/
+        top = base / f"{exe}_{case}"
+        d = top / "run"
+        d.mkdir(parents=True)
+        os.symlink(os.path.join(REF, "testsuite", case, "input"), top / "input")
         shutil.copy(os.path.join(REF, "testsuite", case, "input", "eprem_input_file"), d)
         env = dict(os.environ, EPREM_ORACLE_THREADS="4")
         with open(d / "eprem.log", "w") as lo, open(d / "eprem.err", "w") as le:
@@ -72,8 +80,8 @@ def testsuite_runs(tmp_path_factory):
 
 def _params(key):
     exe, case = key
-    marks = [] if (exe != "eprem_ref" or case != "cone" or SLOW) else [
-        pytest.mark.skip(reason="set EPREM_SLOW_TESTS for the reference's own cone run")]
+    marks = [] if (exe != "eprem_ref" or case not in SLOW_REF or SLOW) else [
+        pytest.mark.skip(reason="set EPREM_SLOW_TESTS for the reference's own run of this case")]
     return pytest.param(exe, case, marks=marks, id=f"{exe}-{case}")
 
 
