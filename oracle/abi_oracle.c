@@ -11,6 +11,16 @@
  * runs (grid construction, shell spawning, output, ideal shock), both the
  * restatement and the drop-in's packing of the reference globals into the
  * ABI's arrays -- the packing the GPU build uses unchanged.
+ *
+ * Recording (for tests/golden/make_testsuite_calls.py): with
+ * EPREM_ORACLE_RECORD=<dir>, every compute call (updateEnergeticParticles,
+ * updateMhd, moveNodes, masMoveNodes, numbered from 0 in call order) appends
+ * "<index> <kind> <argument>" to <dir>/calls.txt; with
+ * EPREM_ORACLE_RECORD_AT=<i,j,...> as well, the inputs of calls i, j, ...
+ * (dimensions, parameters, grids, f, every node field, the MAS slots) are
+ * written to <dir>/call_<i>.rec before the call runs, as named arrays:
+ * int32 name length, name, int32 type (0 float64, 1 float32, 2 int32, 3 raw
+ * bytes), int64 count, values.
  */
 #include <float.h>
 #include <stdio.h>
@@ -35,6 +45,90 @@ static char abi_err[320] = "";
 static int abi_fail(int code, const char *what) {
   snprintf(abi_err, sizeof(abi_err), "%s", what);
   return code;
+}
+
+/* ---- call recording ---------------------------------------------------- */
+enum { REC_EP = 0, REC_MHD = 1, REC_MOVE = 2, REC_MAS_MOVE = 3 };
+static long rec_index = 0;
+
+static void rec_put(FILE *fp, const char *name, int type, const void *data, int64_t count) {
+  static const int size[4] = {8, 4, 4, 1};
+  const int32_t nl = (int32_t)strlen(name), t = type;
+  fwrite(&nl, 4, 1, fp);
+  fwrite(name, 1, (size_t)nl, fp);
+  fwrite(&t, 4, 1, fp);
+  fwrite(&count, 8, 1, fp);
+  if (count > 0) fwrite(data, (size_t)size[type], (size_t)count, fp);
+}
+
+static int rec_wanted(long idx) {
+  const char *at = getenv("EPREM_ORACLE_RECORD_AT");
+  if (!at) return 0;
+  const char *p = at;
+  while (*p) {
+    char *end;
+    const long v = strtol(p, &end, 10);
+    if (end == p) break;
+    if (v == idx) return 1;
+    p = (*end == ',') ? end + 1 : end;
+  }
+  return 0;
+}
+
+static void rec_call(const eprem_gpu_run *r, int kind, double arg) {
+  const char *dir = getenv("EPREM_ORACLE_RECORD");
+  const long idx = rec_index++;
+  if (!dir) return;
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/calls.txt", dir);
+  FILE *fp = fopen(path, "a");
+  if (fp) {
+    fprintf(fp, "%ld %d %.17g\n", idx, kind, arg);
+    fclose(fp);
+  }
+  if (!rec_wanted(idx)) return;
+  snprintf(path, sizeof(path), "%s/call_%ld.rec", dir, idx);
+  fp = fopen(path, "wb");
+  if (!fp) return;
+  const int32_t k = kind, mas_on = r->mas_on;
+  const eprem_dims_t *d = &r->d;
+  const int64_t E = d->num_energies, M = d->num_mu;
+  const int64_t sn = (int64_t)d->num_streams * d->num_nodes;
+  rec_put(fp, "kind", 2, &k, 1);
+  rec_put(fp, "arg", 0, &arg, 1);
+  rec_put(fp, "dims", 3, d, (int64_t)sizeof(*d));
+  rec_put(fp, "params", 3, &r->p, (int64_t)sizeof(r->p));
+  rec_put(fp, "egrid", 0, r->g.egrid, E);
+  rec_put(fp, "vgrid", 0, r->g.vgrid, E);
+  rec_put(fp, "vgrid_i", 0, r->g.vgrid_i, E);
+  rec_put(fp, "rigidity", 0, r->g.rigidity, E);
+  rec_put(fp, "mugrid", 0, r->g.mugrid, M);
+  rec_put(fp, "dlnp", 0, &r->g.dlnp, 1);
+  rec_put(fp, "dmu", 0, &r->g.dmu, 1);
+  if (kind == REC_EP) rec_put(fp, "f", 0, r->f, sn * E * M);
+  rec_put(fp, "nodes", 0, r->nodes, sn * EPREM_NODE_NFIELDS);
+  rec_put(fp, "mas_on", 2, &mas_on, 1);
+  if (r->mas_ready) {
+    rec_put(fp, "mas_params", 3, &r->mas.p, (int64_t)sizeof(r->mas.p));
+    rec_put(fp, "s_cor", 0, &r->mas.s_cor, 1);
+    rec_put(fp, "phi_offset", 0, &r->mas.phi_offset, 1);
+    const eprem_mas_slice_t *sl[2] = {r->mas.slot0, r->mas.slot1};
+    for (int s = 0; s < 2; s++) {
+      char nm[64];
+      snprintf(nm, sizeof(nm), "slot%d_dims", s);
+      rec_put(fp, nm, 2, sl[s]->dims, 3 * EPREM_MAS_NFIELDS);
+      for (int fld = 0; fld < EPREM_MAS_NFIELDS; fld++) {
+        const int64_t nr = sl[s]->dims[fld][0], nt = sl[s]->dims[fld][1], np = sl[s]->dims[fld][2];
+        for (int a = 0; a < 3; a++) {
+          snprintf(nm, sizeof(nm), "slot%d_mesh%d_%d", s, fld, a);
+          rec_put(fp, nm, 1, sl[s]->mesh[fld][a], sl[s]->dims[fld][a]);
+        }
+        snprintf(nm, sizeof(nm), "slot%d_data%d", s, fld);
+        rec_put(fp, nm, 1, sl[s]->data[fld], nr * nt * np);
+      }
+    }
+  }
+  fclose(fp);
 }
 
 static void stats_reset(eprem_ep_stats_t *s) {
@@ -87,7 +181,7 @@ int eprem_gpu_download_nodes(eprem_gpu_run *r, double *nodes, uint64_t mask) {
  * (independent when drift and shell diffusion are off); results do not
  * depend on it. */
 int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
-  (void)t_global;
+  rec_call(r, REC_EP, t_global);
   char err[256] = "";
   const char *env = getenv("EPREM_ORACLE_THREADS");
   const int nt = env ? atoi(env) : 1;
@@ -102,11 +196,13 @@ int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *s) {
 }
 
 int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
+  rec_call(r, REC_MHD, t_global);
   const int rc = r->mas_on ? orc_mas_update_mhd(&r->d, &r->p, r->nodes, &r->mas, t_global)
                            : orc_update_mhd(&r->d, &r->p, r->nodes, t_global);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, "updateMhd");
 }
 int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
+  rec_call(r, REC_MOVE, dt);
   const int rc = orc_move_nodes(&r->d, &r->p, r->nodes, dt);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, "moveNodes");
 }
@@ -146,6 +242,7 @@ int eprem_gpu_mas_use(eprem_gpu_run *r, int use_mas) {
 }
 int eprem_gpu_mas_move_nodes(eprem_gpu_run *r, double dt) {
   if (!r->mas_ready) return abi_fail(EPREM_GPU_ERR_ARG, "MAS not initialised");
+  rec_call(r, REC_MAS_MOVE, dt);
   const int rc = orc_mas_move_nodes(&r->d, &r->p, r->nodes, &r->mas, dt);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, "masMoveNodes");
 }
