@@ -78,6 +78,8 @@ struct RunView {
   // parameters
   double r_scale, dt, dt_full, dmu, dlnp;
   double norm_j0, bf_xi, dsh_min, damp_cooling;
+  double f_scale, f_unscale;  // device f = f * f_scale (2^kF32Shift in the FP32 form, else 1)
+  double ln_f_shift;          // ln f_scale (0 in FP64): the change operator works on ln f itself
   int num_ep_steps, max_subcycles;
   int check_seed, use_bc, use_stream, use_focus, use_change;
   int focus_alg, change_alg;
@@ -107,6 +109,20 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double 
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// The FP32 form holds f multiplied by 2^kF32Shift.  Streaming,
+// isotropisation and focusing are linear in f, so the shift changes none of
+// their results beyond rounding.  Adiabatic change advects ln f in flux form
+// with a velocity that varies along ln p, which is not invariant under
+// ln f -> ln f + const: its kernels take ln f_scale off on load (and off the
+// seed boundary values) and put it back before the exponential.  The shift
+// moves the float window from [1.2e-38, 3.4e38]
+// to [6.4e-58, 1.8e19] in EPREM's normalised units, where the distributions
+// of real runs live: their far tails (f down to 1e-240 in the MAS testsuite
+// runs) then floor 20 decades lower, so floored cells stop feeding the
+// fluxes within 30 decades of the peak.  Conversions, seeds and the flux
+// apply the shift; FP64 runs use a scale of 1.
+constexpr int kF32Shift = 64;
+
 // sepSeedFunction (src/energeticParticlesBoundary.c:67-116) with the
 // node-only factor (radial term) and the energy-only factors precomputed:
 // normJHe = normJ0 * radial * power * exp, then /xi, /(2E), floor DBL_MIN.
@@ -116,7 +132,7 @@ __device__ __forceinline__ double seed_value(const RunView &r, const EnergyConst
   double normJ = normJHe / r.bf_xi;
   double normf = normJ / (2.0 * ec.egrid);
   if (normf < DBL_MIN) normf = DBL_MIN;
-  return normf;
+  return normf * r.f_scale;  // in the device's units of f (exact: a power of two)
 }
 
 // Floor value below which the reference resets f (DBL_MIN); the FP32 form

@@ -232,6 +232,10 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.r_scale = p.r_scale;
   v.dt = p.t_del / (1.0 * p.num_ep_steps);  // src/energeticParticles.c:99
   v.dt_full = v.dt * p.num_ep_steps;        // :861, :1582
+  const bool fp32 = dims->precision == EPREM_FP32;
+  v.f_scale = fp32 ? ldexp(1.0, kF32Shift) : 1.0;
+  v.f_unscale = fp32 ? ldexp(1.0, -kF32Shift) : 1.0;
+  v.ln_f_shift = fp32 ? kF32Shift * 0.69314718055994530942 : 0.0;  // ln 2^K
   v.dmu = grids->dmu;
   v.dlnp = grids->dlnp;
   v.norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);

@@ -141,22 +141,23 @@ __global__ void k_omni_flux(RunView r, double *out) {
     double iso = 0.0;
     for (int m = 0; m < r.M; ++m) iso += (double)fp[m];
     iso /= r.M;
-    out[it] = 2.0 * r.ec[it % r.E].egrid * iso;
+    out[it] = 2.0 * r.ec[it % r.E].egrid * iso * r.f_unscale;
   }
 }
 
-// double staging buffer <-> device f (float in the FP32 form)
-__global__ void k_f64_to_f32(const double *src, float *dst, size_t n) {
+// double staging buffer <-> device f (float in the FP32 form, shifted by a
+// power of two: scaling is exact, the float rounding is the same)
+__global__ void k_f64_to_f32(const double *src, float *dst, size_t n, double scale) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    float v = (float)src[i];
+    float v = (float)(src[i] * scale);
     dst[i] = v < FLT_MIN ? FLT_MIN : v;
   }
 }
-__global__ void k_f32_to_f64(const float *src, double *dst, size_t n) {
+__global__ void k_f32_to_f64(const float *src, double *dst, size_t n, double unscale) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = (double)src[i];
+    dst[i] = (double)src[i] * unscale;
 }
 
 static int grid_for(size_t n) {
@@ -200,12 +201,12 @@ int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *l
 // to_device_real: staging (double) -> f (float); else f (float) -> staging.
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
                      size_t count, cudaStream_t st, uint64_t *launches) {
-  (void)r;
   if (to_device_real)
-    k_f64_to_f32<<<grid_for(count), 256, 0, st>>>(src64, reinterpret_cast<float *>(dst64), count);
+    k_f64_to_f32<<<grid_for(count), 256, 0, st>>>(src64, reinterpret_cast<float *>(dst64), count,
+                                                  r.f_scale);
   else
     k_f32_to_f64<<<grid_for(count), 256, 0, st>>>(reinterpret_cast<const float *>(src64), dst64,
-                                                  count);
+                                                  count, r.f_unscale);
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

@@ -319,8 +319,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       n_c[tid] = dlnndt;
       n_d[tid] = (dlnndt < 0) ? 1.0 - r.damp_cooling : 1.0;
       const double radial = r.seed_radial[g];
-      n_bc0[tid] = log(seed_value(r, r.ec[0], radial));
-      n_bc1[tid] = log(seed_value(r, r.ec[E - 1], radial));
+      // ln of the seeds in f's own units (ln f itself in the FP32 form)
+      n_bc0[tid] = log(seed_value(r, r.ec[0], radial)) - r.ln_f_shift;
+      n_bc1[tid] = log(seed_value(r, r.ec[E - 1], radial)) - r.ln_f_shift;
       vmax_bits[tid] = 0ull;
     }
     __syncthreads();
@@ -385,10 +386,11 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       Real *col = slab + (size_t)g * EM + m;  // stride M
       const double *vcol = vf + (size_t)g * F + m;  // face e at vcol[e*M]
       const Real bc0 = (Real)n_bc0[g], bc1 = (Real)n_bc1[g];
+      const Real lns = (Real)r.ln_f_shift;  // 0 in FP64
       Real fc[P];
 #pragma unroll
       for (int e = 0; e < P; ++e)
-        if (e < E) fc[e] = log_r<Real>(col[e * M]);
+        if (e < E) fc[e] = log_r<Real>(col[e * M]) - lns;
       if (ns > 0 && alg == 1) {
         // Euler upwind in ln p, faces pre-scaled by dt_sub/dlnp; the end cells
         // use the reference's one-sided forms with the seed on inflow.
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
 #pragma unroll
       for (int e = 0; e < P; ++e) {
         if (e < E) {
-          Real v = exp_r<Real>(fc[e]);
+          Real v = exp_r<Real>(fc[e] + lns);
           if (bad_value(v, &code)) {
             const size_t gg = g0 + g;
             set_error(r.status, code, 3, (int)(gg / N), (int)(gg % N), e, m);

@@ -147,7 +147,9 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
       c.scale_c = (float)((dt / ns_c) / r.dlnp);
       if (lane < 2) {
         const double radial = r.seed_radial[g];
-        const float lbc = (float)log(seed_value(r, r.ec[lane ? E - 1 : 0], radial));
+        // ln of the seed itself (f is held shifted; see kF32Shift)
+        const float lbc =
+            (float)(log(seed_value(r, r.ec[lane ? E - 1 : 0], radial)) - r.ln_f_shift);
         const float other = __shfl_down_sync(0x3u, lbc, 1);
         c.bc0 = lbc;
         c.bc1 = other;
@@ -298,7 +300,8 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
   float *col = reinterpret_cast<float *>(r.f) + g * E * M + m;  // stride M
   float *fc = lnf + tid;                                       // stride kChangeThreads
   constexpr int T = kChangeThreads;
-  for (int e = 0; e < E; ++e) fc[e * T] = logf(col[e * M]);
+  const float lns = (float)r.ln_f_shift;  // the shift of the FP32 store, off ln f
+  for (int e = 0; e < E; ++e) fc[e * T] = logf(col[e * M]) - lns;
   if (c.ns_c > 0) {
     const float mu = r.mugrid32[m];
     const float am = -mu * c.dupar;
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
   }
   int code = 0;
   for (int e = 0; e < E; ++e) {
-    const float v = expf(fc[e * T]);
+    const float v = expf(fc[e * T] + lns);
     if (bad_value(v, &code)) set_error(r.status, code, 3, (int)(g / N), (int)(g % N), e, m);
     col[e * M] = v < FLT_MIN ? FLT_MIN : v;
   }

@@ -63,7 +63,10 @@ extern "C" {
 #define EPREM_FP64 0  /* plain form: every operation in IEEE double          */
 #define EPREM_FP32 1  /* f and the stencil/scattering arithmetic in float;
                          positions, distances, dt/CFL reductions and
-                         conservation sums in double                         */
+                         conservation sums in double.  The device holds
+                         f * 2^64 (uploads, downloads and fluxes convert), so
+                         f values between 6.4e-58 and 1.8e19 are held as
+                         normal floats; smaller ones floor at 6.4e-58       */
 
 /* ---- sizes -------------------------------------------------------------- */
 typedef struct {
