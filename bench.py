@@ -610,55 +610,76 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     sizes and parameters (24-1536 streams, 400-2000 nodes, 20-50 E, 20-40 mu,
     seed index, mean free path and shock speed drawn from a fixed seed) in
     the FP32 form, streaming shapes autotuned per size class, one CUDA-graph
-    launch per step for all runs; beside it the same runs stepped one after
-    another through the per-run entry points."""
+    launch per step for all runs.  Beside it, the same runs from the same
+    state stepped one after another through the per-run entry points (each
+    run's step completes before the next run's starts): both legs re-create
+    the state (nodes, background, seed population), take one untimed step and
+    time the same K steps, so both do the same sub-cycles."""
     import torch
     members = W.ensemble_members(64)[: args.ensemble_runs]
-    runs = []
-    for w in members:
-        run = EpremRun(w.dims(abi.EPREM_FP32), w.params, W.build_grids(w))
-        run.upload_nodes(W.initial_nodes(w))
-        run.update_mhd(0.0)
-        run.move_nodes(w.params.t_del)
-        run.update_mhd(w.params.t_del)
-        run.init_seed_population(w.seed, w.perturb)
-        runs.append(run)
+    runs = [EpremRun(w.dims(abi.EPREM_FP32), w.params, W.build_grids(w)) for w in members]
+
+    def initial_state():
+        for run, w in zip(runs, members):
+            run.upload_nodes(W.initial_nodes(w))
+            run.update_mhd(0.0)
+            run.move_nodes(w.params.t_del)
+            run.update_mhd(w.params.t_del)
+            run.init_seed_population(w.seed, w.perturb)
+        torch.cuda.synchronize()
+
     cells = sum(w.cells * w.params.num_ep_steps for w in members)
+    initial_state()
     t_tune = time.perf_counter()
     ens = Ensemble(runs)
     chosen = ens.autotune()
     t_tune = time.perf_counter() - t_tune
-    # one after another, per-run entry points (host-timed around device syncs)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for run, w in zip(runs, members):
-        t = w.params.t_del
-        run.move_nodes(w.params.t_del)
-        run.update_mhd(t + w.params.t_del)
-        run.update_energetic_particles(t)
-        run.synchronize()
-    seq_s = time.perf_counter() - t0
-    ens.set_time([2 * w.params.t_del for w in members])
-    ens.step()  # capture + first replay
-    ens.synchronize()
-    s, e0, e1 = event_pair(ens.stream)
-    n0 = sum(r.kernel_launches for r in runs)
-    e0.record(s)
-    for _ in range(args.ensemble_steps):
-        ens.step()
-    e1.record(s)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    ens.synchronize()
-    launches = sum(r.kernel_launches for r in runs) - n0
+    K = args.ensemble_steps
+
+    # one after another, per-run entry points, host-timed around device syncs
+    initial_state()
+    seq_s = 0.0
+    for k in range(1 + K):
+        t0 = time.perf_counter()
+        for run, w in zip(runs, members):
+            t = (1 + k) * w.params.t_del
+            run.move_nodes(w.params.t_del)
+            run.update_mhd(t + w.params.t_del)
+            run.update_energetic_particles(t)
+            run.synchronize()
+        if k:
+            seq_s += time.perf_counter() - t0
+
+    # the same steps from the same state, one graph launch per step, for two
+    # graph schedules: one branch per run side by side, and the runs in one
+    # serial chain (the default); `value` is the default's
+    by_chains = {}
+    for chains in (0, 1):
+        initial_state()
+        ens.set_chains(chains)
+        ens.set_time([w.params.t_del for w in members])
+        ens.step()  # capture + the untimed step
+        ens.synchronize()
+        s, e0, e1 = event_pair(ens.stream)
+        n0 = sum(r.kernel_launches for r in runs)
+        e0.record(s)
+        for _ in range(K):
+            ens.step()
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        ens.synchronize()
+        launches = sum(r.kernel_launches for r in runs) - n0
+        by_chains[chains] = cells * K / (ms * 1e-3)
     out = {
-        "value": cells * args.ensemble_steps / (ms * 1e-3), "unit": UNIT,
+        "value": cells * K / (ms * 1e-3), "unit": UNIT,
+        "value_by_schedule": {"branch_per_run": by_chains[0], "one_chain": by_chains[1]},
         "runs": len(members), "of_runs": 64, "total_cells": sum(w.cells for w in members),
         "sizes": [w.name.split(": ")[1] for w in members],
-        "steps": args.ensemble_steps, "warmup": 1, "ms_per_step": ms / args.ensemble_steps,
-        "graph_launches_per_step": 1, "kernel_launches_per_step": launches // args.ensemble_steps,
-        "one_by_one_value": cells / seq_s,
-        "speedup_vs_one_by_one": (cells * args.ensemble_steps / (ms * 1e-3)) / (cells / seq_s),
+        "steps": K, "warmup": 1, "ms_per_step": ms / K,
+        "graph_launches_per_step": 1, "kernel_launches_per_step": launches // K,
+        "one_by_one_value": cells * K / seq_s,
+        "speedup_vs_one_by_one": (cells * K / (ms * 1e-3)) / (cells * K / seq_s),
         "autotuned_stream_variants": chosen, "autotune_s": round(t_tune, 3), "dtype": "f32",
     }
     ens.close()

@@ -105,8 +105,9 @@ extern "C" int eprem_gpu_set_stream_variant(eprem_gpu_run *r, int variant) {
 // ---- ensembles -------------------------------------------------------------
 // Independent runs stepped together.  The first eprem_gpu_ensemble_step
 // captures one driver step of every run (moveNodes, updateMhd at t + tDel,
-// updateEnergeticParticles, t += tDel) into one CUDA graph, each run on its
-// own branch between a fork and a join on the ensemble's stream; every step
+// updateEnergeticParticles, t += tDel) into one CUDA graph, the runs on
+// serial chains (one by default, or one branch per run) between a fork and a
+// join on the ensemble's stream; every step
 // after that is one graph launch.  Each run's time lives on the device so
 // the replayed graph advances it.
 struct eprem_gpu_ensemble {
@@ -119,6 +120,7 @@ struct eprem_gpu_ensemble {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> launches_per_step;
+  int chains = 1;  // serial chains side by side; 0: one branch per run
 };
 
 static void ensemble_drop_graph(eprem_gpu_ensemble *e) {
@@ -229,12 +231,28 @@ static int ensemble_capture(eprem_gpu_ensemble *e) {
   CK(cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeRelaxed));
   int rc = EPREM_GPU_OK;
   cudaError_t err = cudaEventRecord(e->fork, e->origin);
-  for (int i = 0; i < n && err == cudaSuccess && rc == EPREM_GPU_OK; i++) {
+  // chain of each run: largest run first onto the chain with the fewest cells
+  const int nch = (e->chains <= 0 || e->chains > n) ? n : e->chains;
+  std::vector<int> order(n), chain_of(n, 0);
+  for (int i = 0; i < n; i++) order[i] = i;
+  auto cells = [&](int i) { return (double)e->runs[i]->cells(); };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
+  std::vector<double> load(nch, 0.0);
+  std::vector<int> last(nch, -1);  // last run on each chain so far
+  for (int i : order) {
+    const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    chain_of[i] = c;
+    load[c] += cells(i);
+  }
+  for (int k = 0; k < n && err == cudaSuccess && rc == EPREM_GPU_OK; k++) {
+    const int i = order[k];
     eprem_gpu_run *r = e->runs[i];
     r->timing = false;  // no event bookkeeping inside a graph
     const uint64_t l0 = r->launches;
-    err = cudaStreamWaitEvent(r->stream, e->fork, 0);
+    const int prev = last[chain_of[i]];
+    err = cudaStreamWaitEvent(r->stream, prev < 0 ? e->fork : e->joins[prev], 0);
     if (err != cudaSuccess) break;
+    last[chain_of[i]] = i;
     const double td = r->params.t_del;
     if (launch_move_nodes(r->v, td, r->stream, &r->launches) ||
         launch_update_mhd(r->v, r->mhd, td, r->stream, &r->launches, e->d_time + i)) {
@@ -250,8 +268,9 @@ static int ensemble_capture(eprem_gpu_ensemble *e) {
     e->launches_per_step[i] = r->launches - l0;
     r->launches = l0;  // counted again at every replay
     err = cudaEventRecord(e->joins[i], r->stream);
-    if (err == cudaSuccess) err = cudaStreamWaitEvent(e->origin, e->joins[i], 0);
   }
+  for (int c = 0; c < nch && err == cudaSuccess; c++)
+    if (last[c] >= 0) err = cudaStreamWaitEvent(e->origin, e->joins[last[c]], 0);
   for (int i = 0; i < n; i++) e->runs[i]->timing = saved[i];
   cudaGraph_t g = nullptr;
   const cudaError_t end = cudaStreamEndCapture(e->origin, &g);
@@ -267,6 +286,17 @@ static int ensemble_capture(eprem_gpu_ensemble *e) {
     return cuda_fail(err, "ensemble step capture");
   }
   e->graph = g;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *e, int chains) {
+  if (!e) return fail(EPREM_GPU_ERR_ARG, "null ensemble");
+  if (chains < 0) return fail(EPREM_GPU_ERR_ARG, "chains must be >= 0");
+  if (chains != e->chains) {
+    if (e->origin) CK(cudaStreamSynchronize(e->origin));
+    ensemble_drop_graph(e);
+    e->chains = chains;
+  }
   return EPREM_GPU_OK;
 }
 

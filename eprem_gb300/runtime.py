@@ -59,6 +59,7 @@ EXPORTS = [
     ("eprem_gpu_ensemble_set_time", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_ensemble_get_time", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_ensemble_autotune", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("eprem_gpu_ensemble_set_chains", C.c_int, [C.c_void_p, C.c_int]),
     ("eprem_gpu_ensemble_step", C.c_int, [C.c_void_p]),
     ("eprem_gpu_ensemble_synchronize", C.c_int, [C.c_void_p]),
     ("eprem_gpu_ensemble_stream", C.c_void_p, [C.c_void_p]),
@@ -314,6 +315,11 @@ class Ensemble:
         out = (C.c_int * len(self.runs))()
         self._check(self.lib.eprem_gpu_ensemble_autotune(self.handle, out))
         return list(out)
+
+    def set_chains(self, chains: int):
+        """Graph schedule: `chains` serial chains side by side (1, the
+        default: all runs in sequence; 0: one branch per run)."""
+        self._check(self.lib.eprem_gpu_ensemble_set_chains(self.handle, chains))
 
     def step(self):
         self._check(self.lib.eprem_gpu_ensemble_step(self.handle))

@@ -392,8 +392,9 @@ int eprem_gpu_set_stream_variant(eprem_gpu_run *run, int variant);
  * the current device, analytic background) stepped together.  The first
  * eprem_gpu_ensemble_step captures one driver step of every run --
  * moveNodes(tDel), updateMhd(t + tDel), updateEnergeticParticles, t += tDel,
- * the order of src/eprem.c:620-671 -- into one CUDA graph with one branch per
- * run; each later step is one launch of that graph.  Each run's time t lives
+ * the order of src/eprem.c:620-671 -- into one CUDA graph (the runs in
+ * sequence, or the chains of eprem_gpu_ensemble_set_chains); each later step
+ * is one launch of that graph.  Each run's time t lives
  * on the device (set_time / get_time, zero at creation).  Until
  * eprem_gpu_ensemble_synchronize returns, the member runs must not be used
  * on their own.  Failures inside a step are reported by synchronize, with the
@@ -408,6 +409,14 @@ int eprem_gpu_ensemble_get_time(eprem_gpu_ensemble *ens, double *t_global);
  * its choice to the others of the class; chosen_variants (may be NULL)
  * receives one variant per run.  The next step captures a new graph. */
 int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *ens, int *chosen_variants);
+/* How the graph orders the runs: `chains` serial chains that run side by
+ * side, the runs spread over them largest first onto the chain with the
+ * fewest cells (1, the default: every run after the previous one; 0: one
+ * branch per run, all side by side).  Runs that each fill the GPU step
+ * fastest in one chain (8 runs of 0.1-2.6 G cells: one chain 8.55e9
+ * cell-updates/s, one branch per run 8.14e9); side-by-side branches are for
+ * runs too small to fill it.  The next step captures a new graph. */
+int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *ens, int chains);
 int eprem_gpu_ensemble_step(eprem_gpu_ensemble *ens);
 int eprem_gpu_ensemble_synchronize(eprem_gpu_ensemble *ens);
 /* The cudaStream_t the graph launches on (as void*). */

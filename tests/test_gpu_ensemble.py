@@ -28,8 +28,11 @@ def _start(w, orc, precision):
     return run
 
 
+@pytest.mark.parametrize("chains", [0, 1, 2])
 @pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
-def test_ensemble_step_equals_individual_steps(oracle_lib, precision):
+def test_ensemble_step_equals_individual_steps(oracle_lib, precision, chains):
+    """Every graph schedule (one branch per run, one serial chain, two
+    chains) replays the runs' own kernels: bit-equal to stepping them."""
     ws = _members()
     td = ws[0].params.t_del
     t0 = [td, 2 * td, 3 * td]
@@ -43,6 +46,7 @@ def test_ensemble_step_equals_individual_steps(oracle_lib, precision):
             t += w.params.t_del
         run.synchronize()
     ens = Ensemble(batched)
+    ens.set_chains(chains)
     ens.set_time(t0)
     n0 = [r.kernel_launches for r in batched]
     for _ in range(3):
