@@ -15,7 +15,9 @@
 //   * warp-edge lanes publish only the half their neighbour needs (lane 31's
 //     last node for mu >= 0, lane 0's first node for mu < 0).
 // A CTA of T threads holds NPT*T >= 1024 nodes for mu bins up to 48, so a
-// 1000-node stream fits one CTA.
+// 1000-node stream fits one CTA.  Two kernels: k_stream2, the scalar shape
+// (any M and split), and k_stream2_pairs, the packed fp32x2 shapes for even
+// halves, with f held as float2 pairs.
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -42,12 +44,8 @@ constexpr size_t stream2_smem_bytes() {
   return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
 }
 
-// PACK: the upwind and relaxation arithmetic on pairs of mu cells with the
-// packed fp32x2 instructions (two cells per instruction, the same roundings as
-// the scalar fused multiply-adds); needs an even number of cells per half.
-// FILLED: both mu halves fill their MMAX/2 register slots (M = MMAX, m0 = M/2),
-// so every cell guard is known at compile time.
-template <int MMAX, bool PACK, bool FILLED>
+// The scalar shape: any M up to MMAX and any split m0 (odd halves included).
+template <int MMAX>
 __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr int NPT = Stream2Shape<MMAX>::NPT;
@@ -66,7 +64,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int M = r.M, N = r.N;
   // cells moving toward the inner / outer end
-  const int nL = FILLED ? H : m0, nR = FILLED ? H : M - m0;
+  const int nL = m0, nR = M - m0;
   const int L = r.list_size[s];
   if (L < 3) return;
 
@@ -158,41 +156,22 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
     if (lane == 31) {  // last node's outward half for the next warp's first node
       float *dst = hi(p, warp + 1);
       float *rdst = (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H : nullptr;
-      if constexpr (FILLED && H % 4 == 0) {  // whole half, 16-byte slots (H * 4 B rows)
 #pragma unroll
-        for (int j = 0; j < H; j += 4) {
-          const float4 v = make_float4(Rf[NPT - 1][j], Rf[NPT - 1][j + 1], Rf[NPT - 1][j + 2],
-                                       Rf[NPT - 1][j + 3]);
-          *reinterpret_cast<float4 *>(dst + j) = v;
-          if (rdst) *reinterpret_cast<float4 *>(rdst + j) = v;
+      for (int j = 0; j < H; ++j)
+        if (j < nR) {
+          dst[j] = Rf[NPT - 1][j];
+          if (rdst) rdst[j] = Rf[NPT - 1][j];
         }
-      } else {
-#pragma unroll
-        for (int j = 0; j < H; ++j)
-          if (j < nR) {
-            dst[j] = Rf[NPT - 1][j];
-            if (rdst) rdst[j] = Rf[NPT - 1][j];
-          }
-      }
     }
     if (lane == 0) {  // first node's inward half for the previous warp's last node
       float *dst = lo(p, warp);
       float *rdst = (warp == 0 && prev_loW) ? prev_loW + ((p * 2 + 1) * (W + 1) + W) * H : nullptr;
-      if constexpr (FILLED && H % 4 == 0) {
 #pragma unroll
-        for (int j = 0; j < H; j += 4) {
-          const float4 v = make_float4(Lf[0][j], Lf[0][j + 1], Lf[0][j + 2], Lf[0][j + 3]);
-          *reinterpret_cast<float4 *>(dst + j) = v;
-          if (rdst) *reinterpret_cast<float4 *>(rdst + j) = v;
+      for (int j = 0; j < H; ++j)
+        if (j < nL) {
+          dst[j] = Lf[0][j];
+          if (rdst) rdst[j] = Lf[0][j];
         }
-      } else {
-#pragma unroll
-        for (int j = 0; j < H; ++j)
-          if (j < nL) {
-            dst[j] = Lf[0][j];
-            if (rdst) rdst[j] = Lf[0][j];
-          }
-      }
     }
     if (C > 1)
       cluster.sync();
@@ -200,128 +179,50 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       __syncthreads();
     const float *my_hi = hi(p, warp);
     const float *my_lo = lo(p, warp + 1);
-    if constexpr (PACK) {
-      const float2 neg1 = make_float2(-1.f, -1.f);
-      float2 acc2[NPT];
+    float acc[NPT];
 #pragma unroll
-      for (int q = 0; q < NPT; ++q) acc2[q] = make_float2(0.f, 0.f);
+    for (int q = 0; q < NPT; ++q) acc[q] = 0.f;
+    // mu < 0: upwind from the outer neighbour (list node + 1), old values
 #pragma unroll
-      for (int h = 0; h < H / 2; ++h) {
-        const int j = 2 * h;
-        if (j < nL) {
-          float d0 = dl0 + (float)j * ddel, d1 = dl0 + (float)(j + 1) * ddel;
-          asm volatile("" : "+f"(d0), "+f"(d1));
-          const float2 del2 = make_float2(d0, d1);
-          float nb0 = __shfl_down_sync(FULL, Lf[0][j], 1);
-          float nb1 = __shfl_down_sync(FULL, Lf[0][j + 1], 1);
-          if (lane == 31) {
-            const float2 h2 = *reinterpret_cast<const float2 *>(my_lo + j);
-            nb0 = h2.x;
-            nb1 = h2.y;
-          }
+    for (int j = 0; j < H; ++j) {
+      if (j < nL) {
+        float del = dl0 + (float)j * ddel;
+        // opaque to loop-invariant code motion: otherwise the compiler hoists
+        // every mult*del product out of the sub-cycle loop into registers
+        asm volatile("" : "+f"(del));
+        float nb = __shfl_down_sync(FULL, Lf[0][j], 1);
+        if (lane == 31) nb = my_lo[j];
 #pragma unroll
-          for (int q = 0; q < NPT; ++q) {
-            const int qn = q + 1 < NPT ? q + 1 : q;
-            const float2 cur = make_float2(Lf[q][j], Lf[q][j + 1]);
-            const float2 right =
-                (q + 1 < NPT) ? make_float2(Lf[qn][j], Lf[qn][j + 1]) : make_float2(nb0, nb1);
-            const float2 c2 = __fmul2_rn(make_float2(mlo[q], mlo[q]), del2);
-            const float2 nw = __ffma2_rn(c2, __ffma2_rn(right, neg1, cur), cur);
-            Lf[q][j] = nw.x;
-            Lf[q][j + 1] = nw.y;
-            acc2[q] = __fadd2_rn(acc2[q], nw);
-          }
+        for (int q = 0; q < NPT; ++q) {
+          const float right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][j] : nb;
+          Lf[q][j] = Lf[q][j] + (mlo[q] * del) * (Lf[q][j] - right);
+          acc[q] += Lf[q][j];
         }
       }
+    }
+    // mu >= 0: upwind from the inner neighbour (list node - 1), old values
 #pragma unroll
-      for (int h = 0; h < H / 2; ++h) {
-        const int j = 2 * h;
-        if (j < nR) {
-          float d0 = dr0 + (float)j * ddel, d1 = dr0 + (float)(j + 1) * ddel;
-          asm volatile("" : "+f"(d0), "+f"(d1));
-          const float2 del2 = make_float2(d0, d1);
-          float nb0 = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
-          float nb1 = __shfl_up_sync(FULL, Rf[NPT - 1][j + 1], 1);
-          if (lane == 0) {
-            const float2 h2 = *reinterpret_cast<const float2 *>(my_hi + j);
-            nb0 = h2.x;
-            nb1 = h2.y;
-          }
+    for (int j = 0; j < H; ++j) {
+      if (j < nR) {
+        float del = dr0 + (float)j * ddel;
+        asm volatile("" : "+f"(del));
+        float nb = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
+        if (lane == 0) nb = my_hi[j];
 #pragma unroll
-          for (int q = NPT - 1; q >= 0; --q) {
-            const int qp = q > 0 ? q - 1 : 0;
-            const float2 cur = make_float2(Rf[q][j], Rf[q][j + 1]);
-            const float2 left =
-                (q > 0) ? make_float2(Rf[qp][j], Rf[qp][j + 1]) : make_float2(nb0, nb1);
-            const float2 c2 = __fmul2_rn(make_float2(mhi[q], mhi[q]), del2);
-            const float2 nw = __ffma2_rn(c2, __ffma2_rn(cur, neg1, left), cur);
-            Rf[q][j] = nw.x;
-            Rf[q][j + 1] = nw.y;
-            acc2[q] = __fadd2_rn(acc2[q], nw);
-          }
+        for (int q = NPT - 1; q >= 0; --q) {
+          const float left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][j] : nb;
+          Rf[q][j] = Rf[q][j] + (mhi[q] * del) * (left - Rf[q][j]);
+          acc[q] += Rf[q][j];
         }
       }
+    }
 #pragma unroll
-      for (int q = 0; q < NPT; ++q) {
-        const float iso = (inv_m * (acc2[q].x + acc2[q].y)) * om[q];
-        const float2 iso2 = make_float2(iso, iso), em2 = make_float2(em[q], em[q]);
+    for (int q = 0; q < NPT; ++q) {
+      const float iso = (inv_m * acc[q]) * om[q];
 #pragma unroll
-        for (int h = 0; h < H / 2; ++h) {
-          const int j = 2 * h;
-          const float2 a = __ffma2_rn(make_float2(Lf[q][j], Lf[q][j + 1]), em2, iso2);
-          const float2 b = __ffma2_rn(make_float2(Rf[q][j], Rf[q][j + 1]), em2, iso2);
-          Lf[q][j] = a.x;
-          Lf[q][j + 1] = a.y;
-          Rf[q][j] = b.x;
-          Rf[q][j + 1] = b.y;
-        }
-      }
-    } else {
-      float acc[NPT];
-  #pragma unroll
-      for (int q = 0; q < NPT; ++q) acc[q] = 0.f;
-      // mu < 0: upwind from the outer neighbour (list node + 1), old values
-  #pragma unroll
       for (int j = 0; j < H; ++j) {
-        if (j < nL) {
-          float del = dl0 + (float)j * ddel;
-          // opaque to loop-invariant code motion: otherwise the compiler hoists
-          // every mult*del product out of the sub-cycle loop into registers
-          asm volatile("" : "+f"(del));
-          float nb = __shfl_down_sync(FULL, Lf[0][j], 1);
-          if (lane == 31) nb = my_lo[j];
-  #pragma unroll
-          for (int q = 0; q < NPT; ++q) {
-            const float right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][j] : nb;
-            Lf[q][j] = Lf[q][j] + (mlo[q] * del) * (Lf[q][j] - right);
-            acc[q] += Lf[q][j];
-          }
-        }
-      }
-      // mu >= 0: upwind from the inner neighbour (list node - 1), old values
-  #pragma unroll
-      for (int j = 0; j < H; ++j) {
-        if (j < nR) {
-          float del = dr0 + (float)j * ddel;
-          asm volatile("" : "+f"(del));
-          float nb = __shfl_up_sync(FULL, Rf[NPT - 1][j], 1);
-          if (lane == 0) nb = my_hi[j];
-  #pragma unroll
-          for (int q = NPT - 1; q >= 0; --q) {
-            const float left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][j] : nb;
-            Rf[q][j] = Rf[q][j] + (mhi[q] * del) * (left - Rf[q][j]);
-            acc[q] += Rf[q][j];
-          }
-        }
-      }
-  #pragma unroll
-      for (int q = 0; q < NPT; ++q) {
-        const float iso = (inv_m * acc[q]) * om[q];
-  #pragma unroll
-        for (int j = 0; j < H; ++j) {
-          Lf[q][j] = Lf[q][j] * em[q] + iso;
-          Rf[q][j] = Rf[q][j] * em[q] + iso;
-        }
+        Lf[q][j] = Lf[q][j] * em[q] + iso;
+        Rf[q][j] = Rf[q][j] * em[q] + iso;
       }
     }
   }
@@ -353,6 +254,296 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
         for (int j = 0; j < H; ++j) {
           if (j < nL) op[j] = Lf[q][j];
           if (j < nR) op[m0 + j] = Rf[q][j];
+        }
+      }
+    }
+  }
+  if (C > 1) cluster.sync();
+}
+
+// The packed shapes: the upwind and relaxation arithmetic on pairs of mu
+// cells with the packed fp32x2 instructions (two cells per instruction, the
+// same roundings as the scalar fused multiply-adds of k_stream2), for even
+// halves (m0 and M - m0 even).  f is held as pairs (float2) from load to
+// store, so every pair sits in an aligned register pair.  FILLED: both halves
+// fill their MMAX/2 slots (M = MMAX, m0 = M/2), every cell guard is known at
+// compile time and rows move as float4 (MMAX is a multiple of 8: 16-byte
+// aligned rows); otherwise rows move as float2 under run-time guards.
+template <int MMAX, bool FILLED>
+__global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(RunView r, int m0) {
+  constexpr int T = Stream2Shape<MMAX>::T;
+  constexpr int NPT = Stream2Shape<MMAX>::NPT;
+  constexpr int W = T / 32;
+  constexpr int H = MMAX / 2;  // cells per direction
+  constexpr int P = H / 2;     // pairs per direction
+  static_assert(H % 4 == 0, "rows move as float4");
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) float halo[];  // [p][hi/lo][W+1][H]
+  auto hi = [&](int p, int w) { return halo + ((p * 2 + 0) * (W + 1) + w) * H; };
+  auto lo = [&](int p, int w) { return halo + ((p * 2 + 1) * (W + 1) + w) * H; };
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int crank = (int)cluster.block_rank();
+  const int s = blockIdx.y;
+  const int e = r.E - 1 - (int)blockIdx.z;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int N = r.N;
+  const int M = FILLED ? MMAX : r.M;
+  if (FILLED) m0 = H;
+  const int nPL = FILLED ? P : m0 / 2, nPR = FILLED ? P : (M - m0) / 2;  // pairs per half
+  const int L = r.list_size[s];
+  if (L < 3) return;
+
+  const EnergyConsts ec = r.ec[e];
+  const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
+  const double nst = floor(r.dt / dtMin + 1.0);
+  if (!(nst <= (double)r.max_subcycles)) {
+    if (crank == 0 && tid == 0) set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    return;
+  }
+  const int nsteps = (int)nst;
+  const double dtProp = r.dt / (1.0 * nsteps);
+  if (crank == 0 && tid == 0) {
+    atomicMax(&r.status->max_stream, nsteps);
+    atomicAdd(&r.status->stream_cs, (unsigned long long)nsteps * L * M);
+  }
+  for (int j = tid; j < 2 * 2 * (W + 1) * H; j += T) halo[j] = 0.f;
+
+  const int i0 = NPT * (crank * T + tid);
+  const size_t sN = (size_t)s * N;
+  float2 Lf[NPT][P], Rf[NPT][P];  // mu = 2p, 2p+1 and m0 + 2p, m0 + 2p + 1
+  float2 mhi[NPT], mlo[NPT], em[NPT];
+  float om[NPT];
+  __shared__ float s_bcv[3];
+  const double vdt = ec.vgrid * dtProp;
+  const float4 *cf = r.scoef + ((size_t)s * r.E + e) * N;
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    mhi[q] = mlo[q] = em[q] = make_float2(0.f, 0.f);
+    om[q] = 0.f;
+#pragma unroll
+    for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(0.f, 0.f);
+    const int il = i0 + q;
+    if (il < L) {
+      const int k = r.list[sN + il];
+      const float4 c = cf[il];
+      const float seedf = c.w;
+      const float *row = reinterpret_cast<const float *>(r.f) + ((sN + k) * r.E + e) * M;
+      if constexpr (FILLED) {
+        const float4 *fp = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int t = 0; t < P / 2; ++t) {
+          const float4 a = fp[t], b = fp[H / 4 + t];
+          Lf[q][2 * t] = make_float2(a.x, a.y);
+          Lf[q][2 * t + 1] = make_float2(a.z, a.w);
+          Rf[q][2 * t] = make_float2(b.x, b.y);
+          Rf[q][2 * t + 1] = make_float2(b.z, b.w);
+        }
+      } else {
+        const float2 *fp = reinterpret_cast<const float2 *>(row);
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+          if (t < nPL) Lf[q][t] = fp[t];
+          if (t < nPR) Rf[q][t] = fp[m0 / 2 + t];
+        }
+      }
+      if (r.check_seed) {  // as (double)v < seed: no float between
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+          if (FILLED || t < nPL) {
+            Lf[q][t].x = Lf[q][t].x < seedf ? seedf : Lf[q][t].x;
+            Lf[q][t].y = Lf[q][t].y < seedf ? seedf : Lf[q][t].y;
+          }
+          if (FILLED || t < nPR) {
+            Rf[q][t].x = Rf[q][t].x < seedf ? seedf : Rf[q][t].x;
+            Rf[q][t].y = Rf[q][t].y < seedf ? seedf : Rf[q][t].y;
+          }
+        }
+      }
+      const float mh = (il == 0) ? 0.f : c.x, ml = (il == L - 1) ? 0.f : c.x;
+      mhi[q] = make_float2(mh, mh);
+      mlo[q] = make_float2(ml, ml);
+      em[q] = make_float2(c.y, c.y);
+      om[q] = c.z;
+      if (il < 3) s_bcv[il] = seedf;
+    }
+  }
+  const float dl0 = (float)(vdt * r.mugrid[0]);
+  const float dr0 = (float)(vdt * r.mugrid[m0 < M ? m0 : M - 1]);
+  const float ddel = (float)(vdt * r.dmu);
+  const float inv_m = (float)(1.0 / M);
+  float *next_hi0 = (C > 1 && crank < C - 1) ? cluster.map_shared_rank(halo, crank + 1) : nullptr;
+  float *prev_loW = (C > 1 && crank > 0) ? cluster.map_shared_rank(halo, crank - 1) : nullptr;
+  if (C > 1)
+    cluster.sync();
+  else
+    __syncthreads();
+
+  const float2 neg1 = make_float2(-1.f, -1.f);
+  for (int step = 0; step < nsteps; ++step) {
+    const int ph = step & 1;
+    if (r.use_bc && crank == 0 && warp == 0) {  // list nodes 0..2 live in warp 0
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        if (i0 + q < 3) {
+          const float b = s_bcv[i0 + q];
+#pragma unroll
+          for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(b, b);
+        }
+      }
+    }
+    if (lane == 31) {  // last node's outward half for the next warp's first node
+      float4 *dst = reinterpret_cast<float4 *>(hi(ph, warp + 1));
+      float4 *rdst = (warp == W - 1 && next_hi0)
+                         ? reinterpret_cast<float4 *>(next_hi0 + ((ph * 2 + 0) * (W + 1)) * H)
+                         : nullptr;
+      if constexpr (FILLED) {
+#pragma unroll
+        for (int t = 0; t < P / 2; ++t) {
+          const float4 v = make_float4(Rf[NPT - 1][2 * t].x, Rf[NPT - 1][2 * t].y,
+                                       Rf[NPT - 1][2 * t + 1].x, Rf[NPT - 1][2 * t + 1].y);
+          dst[t] = v;
+          if (rdst) rdst[t] = v;
+        }
+      } else {
+        float2 *d2 = reinterpret_cast<float2 *>(dst), *r2 = reinterpret_cast<float2 *>(rdst);
+#pragma unroll
+        for (int t = 0; t < P; ++t)
+          if (t < nPR) {
+            d2[t] = Rf[NPT - 1][t];
+            if (r2) r2[t] = Rf[NPT - 1][t];
+          }
+      }
+    }
+    if (lane == 0) {  // first node's inward half for the previous warp's last node
+      float4 *dst = reinterpret_cast<float4 *>(lo(ph, warp));
+      float4 *rdst = (warp == 0 && prev_loW)
+                         ? reinterpret_cast<float4 *>(prev_loW + ((ph * 2 + 1) * (W + 1) + W) * H)
+                         : nullptr;
+      if constexpr (FILLED) {
+#pragma unroll
+        for (int t = 0; t < P / 2; ++t) {
+          const float4 v = make_float4(Lf[0][2 * t].x, Lf[0][2 * t].y, Lf[0][2 * t + 1].x,
+                                       Lf[0][2 * t + 1].y);
+          dst[t] = v;
+          if (rdst) rdst[t] = v;
+        }
+      } else {
+        float2 *d2 = reinterpret_cast<float2 *>(dst), *r2 = reinterpret_cast<float2 *>(rdst);
+#pragma unroll
+        for (int t = 0; t < P; ++t)
+          if (t < nPL) {
+            d2[t] = Lf[0][t];
+            if (r2) r2[t] = Lf[0][t];
+          }
+      }
+    }
+    if (C > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+    const float2 *my_hi = reinterpret_cast<const float2 *>(hi(ph, warp));
+    const float2 *my_lo = reinterpret_cast<const float2 *>(lo(ph, warp + 1));
+    float2 acc[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) acc[q] = make_float2(0.f, 0.f);
+    // mu < 0: upwind from the outer neighbour (list node + 1), old values
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      if (!FILLED && p >= nPL) continue;
+      float d0 = dl0 + (float)(2 * p) * ddel, d1 = dl0 + (float)(2 * p + 1) * ddel;
+      // opaque to loop-invariant code motion: otherwise every mult*del product
+      // is hoisted out of the sub-cycle loop into registers
+      asm volatile("" : "+f"(d0), "+f"(d1));
+      const float2 del2 = make_float2(d0, d1);
+      float2 nb;
+      nb.x = __shfl_down_sync(FULL, Lf[0][p].x, 1);
+      nb.y = __shfl_down_sync(FULL, Lf[0][p].y, 1);
+      if (lane == 31) nb = my_lo[p];
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const float2 cur = Lf[q][p];
+        const float2 right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][p] : nb;
+        const float2 nw = __ffma2_rn(__fmul2_rn(mlo[q], del2), __ffma2_rn(right, neg1, cur), cur);
+        Lf[q][p] = nw;
+        acc[q] = __fadd2_rn(acc[q], nw);
+      }
+    }
+    // mu >= 0: upwind from the inner neighbour (list node - 1), old values
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      if (!FILLED && p >= nPR) continue;
+      float d0 = dr0 + (float)(2 * p) * ddel, d1 = dr0 + (float)(2 * p + 1) * ddel;
+      asm volatile("" : "+f"(d0), "+f"(d1));
+      const float2 del2 = make_float2(d0, d1);
+      float2 nb;
+      nb.x = __shfl_up_sync(FULL, Rf[NPT - 1][p].x, 1);
+      nb.y = __shfl_up_sync(FULL, Rf[NPT - 1][p].y, 1);
+      if (lane == 0) nb = my_hi[p];
+#pragma unroll
+      for (int q = NPT - 1; q >= 0; --q) {
+        const float2 cur = Rf[q][p];
+        const float2 left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][p] : nb;
+        const float2 nw = __ffma2_rn(__fmul2_rn(mhi[q], del2), __ffma2_rn(cur, neg1, left), cur);
+        Rf[q][p] = nw;
+        acc[q] = __fadd2_rn(acc[q], nw);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const float iso = (inv_m * (acc[q].x + acc[q].y)) * om[q];
+      const float2 iso2 = make_float2(iso, iso);
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        Lf[q][p] = __ffma2_rn(Lf[q][p], em[q], iso2);
+        Rf[q][p] = __ffma2_rn(Rf[q][p], em[q], iso2);
+      }
+    }
+  }
+
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il < L) {
+      const int k = r.list[sN + il];
+      int code = 0;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        float2 a = Lf[q][p], b = Rf[q][p];
+        if (FILLED || p < nPL) {
+          if (bad_value(a.x, &code)) set_error(r.status, code, 1, s, k, e, 2 * p);
+          if (bad_value(a.y, &code)) set_error(r.status, code, 1, s, k, e, 2 * p + 1);
+        }
+        if (FILLED || p < nPR) {
+          if (bad_value(b.x, &code)) set_error(r.status, code, 1, s, k, e, m0 + 2 * p);
+          if (bad_value(b.y, &code)) set_error(r.status, code, 1, s, k, e, m0 + 2 * p + 1);
+        }
+        a.x = a.x < FLT_MIN ? FLT_MIN : a.x; a.y = a.y < FLT_MIN ? FLT_MIN : a.y;
+        b.x = b.x < FLT_MIN ? FLT_MIN : b.x; b.y = b.y < FLT_MIN ? FLT_MIN : b.y;
+        Lf[q][p] = a;
+        Rf[q][p] = b;
+      }
+      // node k and the thinned nodes that reference it (previous list node + 1 .. k)
+      const int kfirst = (il == 0) ? 0 : r.list[sN + il - 1] + 1;
+      for (int kk = kfirst; kk <= k; ++kk) {
+        float *row = reinterpret_cast<float *>(r.f) + ((sN + kk) * r.E + e) * M;
+        if constexpr (FILLED) {
+          float4 *op = reinterpret_cast<float4 *>(row);
+#pragma unroll
+          for (int t = 0; t < P / 2; ++t) {
+            op[t] = make_float4(Lf[q][2 * t].x, Lf[q][2 * t].y, Lf[q][2 * t + 1].x,
+                                Lf[q][2 * t + 1].y);
+            op[H / 4 + t] = make_float4(Rf[q][2 * t].x, Rf[q][2 * t].y, Rf[q][2 * t + 1].x,
+                                        Rf[q][2 * t + 1].y);
+          }
+        } else {
+          float2 *op = reinterpret_cast<float2 *>(row);
+#pragma unroll
+          for (int t = 0; t < P; ++t) {
+            if (t < nPL) op[t] = Lf[q][t];
+            if (t < nPR) op[m0 / 2 + t] = Rf[q][t];
+          }
         }
       }
     }
@@ -431,20 +622,22 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *pla
   return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
 }
 
-template <int MMAX, bool PACK>
-static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, bool full,
+template <int MMAX>
+static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int m0,
                                     cudaStream_t st) {
   constexpr int T = Stream2Shape<MMAX>::T;
   constexpr size_t dyn = stream2_smem_bytes<MMAX>();
-  auto kern = full ? k_stream2<MMAX, PACK, true> : k_stream2<MMAX, PACK, false>;
+  void (*kern)(RunView, int) = !pl.packed  ? k_stream2<MMAX>
+                               : pl.filled ? k_stream2_pairs<MMAX, true>
+                                           : k_stream2_pairs<MMAX, false>;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cluster, r.S, r.E);
+  cfg.gridDim = dim3(pl.cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
   cfg.dynamicSmemBytes = dyn;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.x = pl.cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -452,23 +645,18 @@ static cudaError_t launch_stream2_t(const RunView &r, int cluster, int m0, bool 
   return cudaLaunchKernelEx(&cfg, kern, r, m0);
 }
 
-template <bool PACK>
-static cudaError_t launch_mmax(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st) {
-  switch (pl.mmax) {
-    case 8: return launch_stream2_t<8, PACK>(r, pl.cluster, m0, pl.filled, st);
-    case 16: return launch_stream2_t<16, PACK>(r, pl.cluster, m0, pl.filled, st);
-    case 24: return launch_stream2_t<24, PACK>(r, pl.cluster, m0, pl.filled, st);
-    case 32: return launch_stream2_t<32, PACK>(r, pl.cluster, m0, pl.filled, st);
-    case 40: return launch_stream2_t<40, PACK>(r, pl.cluster, m0, pl.filled, st);
-    case 48: return launch_stream2_t<48, PACK>(r, pl.cluster, m0, pl.filled, st);
-    default: return launch_stream2_t<64, PACK>(r, pl.cluster, m0, pl.filled, st);
-  }
-}
-
 int launch_stream2(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st,
                    uint64_t *launches) {
-  const cudaError_t err = pl.packed ? launch_mmax<true>(r, pl, m0, st)
-                                    : launch_mmax<false>(r, pl, m0, st);
+  cudaError_t err;
+  switch (pl.mmax) {
+    case 8: err = launch_stream2_t<8>(r, pl, m0, st); break;
+    case 16: err = launch_stream2_t<16>(r, pl, m0, st); break;
+    case 24: err = launch_stream2_t<24>(r, pl, m0, st); break;
+    case 32: err = launch_stream2_t<32>(r, pl, m0, st); break;
+    case 40: err = launch_stream2_t<40>(r, pl, m0, st); break;
+    case 48: err = launch_stream2_t<48>(r, pl, m0, st); break;
+    default: err = launch_stream2_t<64>(r, pl, m0, st); break;
+  }
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
