@@ -249,7 +249,7 @@ def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
     # algorithmic HBM bytes: one read + one write of f per operator pass
     bytes_per_launch = cells * BYTES_PER_CELL_UPDATE[form] / 2.0
     return {
-        "kernel": ({"fp32": "k_stream2", "fp64": "k_stream"}[form] if kind == "stream"
+        "kernel": ({"fp32": "k_stream2_pairs", "fp64": "k_stream"}[form] if kind == "stream"
                    else {"fp32": "k_focus32+k_change32", "fp64": "k_node"}[form]),
         "bound": "fp64" if form == "fp64" else "fp32",
         "achieved": round(achieved, 3), "peak": round(peak_tflops, 3), "unit": "TFLOP/s",
@@ -395,10 +395,13 @@ def ours(args, rank, ws, dist):
     torch.cuda.synchronize()
     e0.record(s)
     for _ in range(args.e2e_steps):
-        run.upload_f(f_host)
+        # the step with every input copied in and every output copied out:
+        # node fields around it, f through the pipelined host-buffer update
         run.upload_nodes(nodes_host)
-        t = step(run, t, w)
-        run.download_f(f_host)
+        run.move_nodes(w.params.t_del)
+        run.update_mhd(t + w.params.t_del)
+        run.update_energetic_particles_host(f_host, f_host, t)
+        t += w.params.t_del
         run.download_nodes(nodes_host)
     e1.record(s)
     e1.synchronize()

@@ -80,6 +80,10 @@ struct RunView {
   double norm_j0, bf_xi, dsh_min, damp_cooling;
   double f_scale, f_unscale;  // device f = f * f_scale (2^kF32Shift in the FP32 form, else 1)
   double ln_f_shift;          // ln f_scale (0 in FP64): the change operator works on ln f itself
+  // A view of streams [s_base, s_base + S) of the run (stream_range_view):
+  // node field k of node g is nodes[k * node_stride + g]
+  size_t node_stride;
+  int s_base;
   int num_ep_steps, max_subcycles;
   int check_seed, use_bc, use_stream, use_focus, use_change;
   int focus_alg, change_alg;
@@ -87,7 +91,7 @@ struct RunView {
 };
 
 __device__ __forceinline__ double *node_field(const RunView &r, int field) {
-  return r.nodes + (size_t)field * ((size_t)r.S * r.N);
+  return r.nodes + (size_t)field * r.node_stride;
 }
 
 __device__ __forceinline__ void set_error(DevStatus *st, int code, int where, int s, int k, int e,
@@ -99,6 +103,12 @@ __device__ __forceinline__ void set_error(DevStatus *st, int code, int where, in
     st->energy = e;
     st->mu = m;
   }
+}
+
+// The same, for a stream index s of the view r (reported as the run's stream).
+__device__ __forceinline__ void set_error(const RunView &r, int code, int where, int s, int k,
+                                          int e, int m) {
+  set_error(r.status, code, where, s < 0 ? s : s + r.s_base, k, e, m);
 }
 
 // Non-negative doubles order like their bit patterns.

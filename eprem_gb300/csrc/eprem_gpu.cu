@@ -229,6 +229,8 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.seed_radial = r->d_seed_radial;
   v.mfp_node = r->d_mfp_node;
   v.status = r->d_status;
+  v.node_stride = (size_t)S * N;
+  v.s_base = 0;
   v.r_scale = p.r_scale;
   v.dt = p.t_del / (1.0 * p.num_ep_steps);  // src/energeticParticles.c:99
   v.dt_full = v.dt * p.num_ep_steps;        // :861, :1582
@@ -402,46 +404,161 @@ extern "C" int eprem_gpu_download_nodes(eprem_gpu_run *r, double *nodes, uint64_
   return check_status(r, false, nullptr);
 }
 
-extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
-  (void)t_global;
-  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+// The run's view restricted to streams [s0, s1): every per-stream and
+// per-node array starts at stream s0; node fields keep the run's stride and
+// errors report the run's stream numbers.  Streams are independent on this
+// path (no drift, no shell diffusion), so updating the views of a partition
+// of the streams one after another is the update of the whole run.
+static RunView stream_range_view(const eprem_gpu_run *r, int s0, int s1) {
+  const RunView &v = r->v;
+  RunView u = v;
+  const size_t n0 = (size_t)s0 * v.N;
+  const size_t c0 = n0 * v.E * v.M;
+  u.S = s1 - s0;
+  u.s_base = v.s_base + s0;
+  u.f = v.precision == EPREM_FP32 ? static_cast<void *>(static_cast<float *>(v.f) + c0)
+                                  : static_cast<void *>(static_cast<double *>(v.f) + c0);
+  u.nodes = v.nodes + n0;
+  u.list = v.list + n0;
+  u.list_size = v.list_size + s0;
+  u.ds_i = v.ds_i + n0;
+  u.ds_min = v.ds_min + s0;
+  u.seed_radial = v.seed_radial + n0;
+  u.mfp_node = v.mfp_node + n0;
+  if (u.coef32) u.coef32 = v.coef32 + n0;
+  if (u.scoef) u.scoef = v.scoef + (size_t)s0 * v.E * v.N;
+  return u;
+}
+
+// updateEnergeticParticles on the streams of view v, on the run's stream.
+static int ep_update(eprem_gpu_run *r, const RunView &v) {
   const eprem_params_t &p = r->params;
   int rc = timed(r, EPREM_KERNEL_GEOMETRY, [&] {
-    return launch_geometry(r->v, r->stream, r->norm_radius, r->neg_beta, p.mfp_type,
+    return launch_geometry(v, r->stream, r->norm_radius, r->neg_beta, p.mfp_type,
                            p.mfp_type == 2 ? p.mfp_b_power : p.mfp_radial_power, p.mhd_bs_au,
                            &r->launches);
   });
   if (rc) return cuda_fail(cudaGetLastError(), "geometry launch");
-  if (r->v.use_stream && r->splan.reg_coef == 2) {
+  if (v.use_stream && r->splan.reg_coef == 2) {
     rc = timed(r, EPREM_KERNEL_GEOMETRY,
-               [&] { return launch_stream2_coef(r->v, r->stream, &r->launches); });
+               [&] { return launch_stream2_coef(v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "streaming coefficient launch");
   }
-  if (r->nplan.fast32 && (r->v.use_focus || r->v.use_change)) {
+  if (r->nplan.fast32 && (v.use_focus || v.use_change)) {
     rc = timed(r, EPREM_KERNEL_NODE,
-               [&] { return launch_node32_setup(r->v, r->stream, &r->launches); });
+               [&] { return launch_node32_setup(v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "focusing/change set-up launch");
   }
   for (int step = 0; step < p.num_ep_steps; step++) {
-    if (r->v.use_stream)
+    if (v.use_stream)
       rc = timed(r, EPREM_KERNEL_STREAM,
-                 [&] { return launch_stream(r->v, r->splan, r->m0, r->stream, &r->launches); });
-    else if (r->v.check_seed)
+                 [&] { return launch_stream(v, r->splan, r->m0, r->stream, &r->launches); });
+    else if (v.check_seed)
       rc = timed(r, EPREM_KERNEL_SEED_CHECK,
-                 [&] { return launch_seed_check(r->v, r->stream, &r->launches); });
+                 [&] { return launch_seed_check(v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "streaming launch");
     if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {
       rc = timed(r, EPREM_KERNEL_NODE, [&] { return split_node_phase(r); });
       if (rc) return rc == EPREM_GPU_ERR_CUDA ? cuda_fail(cudaGetLastError(), "split node phase") : rc;
-    } else if (r->v.use_focus || r->v.use_change) {
+    } else if (v.use_focus || v.use_change) {
       rc = timed(r, EPREM_KERNEL_NODE, [&] {
-        return r->nplan.fast32 ? launch_node32(r->v, r->nplan, r->stream, &r->launches)
-                               : launch_node(r->v, r->nplan, r->stream, &r->launches);
+        return r->nplan.fast32 ? launch_node32(v, r->nplan, r->stream, &r->launches)
+                               : launch_node(v, r->nplan, r->stream, &r->launches);
       });
       if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
     }
   }
   return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
+  (void)t_global;
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  return ep_update(r, r->v);
+}
+
+// The same update with f in host memory, pipelined: the streams go through in
+// chunks; chunk c's host-to-device copy runs on the copy stream while chunk
+// c-1 is updated on the run's stream, and its device-to-host copy while chunk
+// c+1 is updated.  The FP32 form converts each chunk in one of two staging
+// buffers (chunk c in buffer c % 2, reused once chunk c-2's copy back has
+// left it).  Synchronous: f_out holds the result on return.
+extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_in,
+                                                         double *f_out, double t_global) {
+  (void)t_global;
+  if (!r || !f_in || !f_out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {  // those phases work on the whole run
+    int rc = eprem_gpu_upload_f(r, f_in);
+    if (!rc) rc = ep_update(r, r->v);
+    if (!rc) rc = eprem_gpu_download_f(r, f_out);
+    return rc;
+  }
+  const int S = r->dims.num_streams;
+  const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
+  // about eight chunks: each copy is short beside an update, and the first
+  // upload and last download, the only ones not hidden, stay small
+  const int cs = (S + 7) / 8;
+  const int nch = (S + cs - 1) / cs;
+  const bool fp32 = r->dims.precision == EPREM_FP32;
+  int rc = ensure_stage(r, fp32 ? (size_t)cs * per_stream : 1);
+  if (rc) return rc;
+  cudaEvent_t *arrived = r->stage_ev, *updated = r->stage_ev + 2;
+  // the run's earlier work on f and the staging buffers comes first
+  CK(cudaEventRecord(updated[0], r->stream));
+  CK(cudaStreamWaitEvent(r->copy_stream, updated[0], 0));
+  auto dev64 = [&](int c) {  // chunk c on the device as FP64: staging or f itself
+    return fp32 ? r->d_stage + (size_t)(c & 1) * r->stage_elems
+                : static_cast<double *>(r->d_f) + (size_t)c * cs * per_stream;
+  };
+  auto h2d = [&](int c) -> int {
+    const int s0 = c * cs, s1 = s0 + cs < S ? s0 + cs : S;
+    const size_t n = (size_t)(s1 - s0) * per_stream;
+    CK(cudaMemcpyAsync(dev64(c), f_in + (size_t)s0 * per_stream, n * sizeof(double),
+                       cudaMemcpyHostToDevice, r->copy_stream));
+    CK(cudaEventRecord(arrived[c & 1], r->copy_stream));
+    return EPREM_GPU_OK;
+  };
+  rc = h2d(0);
+  for (int c = 0; c < nch && !rc; c++) {
+    if (c + 1 < nch) rc = h2d(c + 1);  // copy stream: after chunk c-1's download
+    if (rc) break;
+    const int s0 = c * cs, s1 = s0 + cs < S ? s0 + cs : S;
+    const size_t n = (size_t)(s1 - s0) * per_stream;
+    const RunView v = stream_range_view(r, s0, s1);
+    CK(cudaStreamWaitEvent(r->stream, arrived[c & 1], 0));
+    if (fp32) {
+      rc = launch_convert_f(v, dev64(c), static_cast<double *>(v.f), 1, n, r->stream,
+                            &r->launches);
+      if (rc) return fail(rc, "conversion kernel launch failed");
+    }
+    rc = ep_update(r, v);
+    if (rc) break;
+    if (fp32) {
+      rc = launch_convert_f(v, static_cast<const double *>(v.f), dev64(c), 0, n, r->stream,
+                            &r->launches);
+      if (rc) return fail(rc, "conversion kernel launch failed");
+    }
+    CK(cudaEventRecord(updated[c & 1], r->stream));
+    CK(cudaStreamWaitEvent(r->copy_stream, updated[c & 1], 0));
+    CK(cudaMemcpyAsync(f_out + (size_t)s0 * per_stream, dev64(c), n * sizeof(double),
+                       cudaMemcpyDeviceToHost, r->copy_stream));
+  }
+  CK(cudaStreamSynchronize(r->copy_stream));
+  if (rc) return rc;
+  return check_status(r, false, nullptr);
+}
+
+extern "C" void *eprem_gpu_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+    fail(EPREM_GPU_ERR_CUDA, "page-locked host allocation failed");
+    return nullptr;
+  }
+  return p;
+}
+
+extern "C" void eprem_gpu_host_free(void *p) {
+  if (p) cudaFreeHost(p);
 }
 
 extern "C" int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *stats) {

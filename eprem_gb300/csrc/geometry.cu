@@ -116,7 +116,7 @@ __global__ void k_stream_list(RunView r) {
   const int L = Lsh;
   if (L < 3) {
     if (lane == 0) {
-      set_error(r.status, EPREM_GPU_ERR_STATE, 4, s, L, -1, -1);
+      set_error(r, EPREM_GPU_ERR_STATE, 4, s, L, -1, -1);
       r.list_size[s] = L;
     }
     return;
@@ -147,7 +147,7 @@ __global__ void k_stream_list(RunView r) {
   if (lane == 0) {
     r.list_size[s] = L;
     r.ds_min[s] = dmin;
-    if (!(dmin > 0.0)) set_error(r.status, EPREM_GPU_ERR_DS, 4, s, -1, -1, -1);
+    if (!(dmin > 0.0)) set_error(r, EPREM_GPU_ERR_DS, 4, s, -1, -1, -1);
   }
 }
 

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       if (!(nsub <= (double)r.max_subcycles)) {
         if (n_ok[tid]) {
           const size_t g = g0 + tid;
-          set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 2, (int)(g / N), (int)(g % N), -1, -1);
+          set_error(r, EPREM_GPU_ERR_SUBCYCLES, 2, (int)(g / N), (int)(g % N), -1, -1);
         }
       } else {
         ns = (int)nsub;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
           Real v = row[m];
           if (bad_value(v, &code)) {
             const size_t gg = g0 + g;
-            set_error(r.status, code, 2, (int)(gg / N), (int)(gg % N), e, m);
+            set_error(r, code, 2, (int)(gg / N), (int)(gg % N), e, m);
           }
           row[m] = v < fl_min ? fl_min : v;
         }
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       if (!(nsub <= (double)r.max_subcycles)) {
         if (n_ok[tid]) {
           const size_t g = g0 + tid;
-          set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 3, (int)(g / N), (int)(g % N), -1, -1);
+          set_error(r, EPREM_GPU_ERR_SUBCYCLES, 3, (int)(g / N), (int)(g % N), -1, -1);
         }
       } else {
         ns = (int)nsub;
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
           Real v = exp_r<Real>(fc[e] + lns);
           if (bad_value(v, &code)) {
             const size_t gg = g0 + g;
-            set_error(r.status, code, 3, (int)(gg / N), (int)(gg % N), e, m);
+            set_error(r, code, 3, (int)(gg / N), (int)(gg % N), e, m);
           }
           col[e * M] = v < fl_min ? fl_min : v;
         }

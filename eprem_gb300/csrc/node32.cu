@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
       const double nsub = ceil(dt / (m_(0.9, r.dmu) / vmax));
       if (!(nsub <= (double)r.max_subcycles)) {
         if (ok && lane == 0)
-          set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 2, (int)(g / N), (int)(g % N), -1, -1);
+          set_error(r, EPREM_GPU_ERR_SUBCYCLES, 2, (int)(g / N), (int)(g % N), -1, -1);
       } else {
         ns_f = (int)nsub;
       }
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
       const double nsub = ceil(dt / (m_(0.9, r.dlnp) / vmax));
       if (!(nsub <= (double)r.max_subcycles)) {
         if (ok && lane == 0)
-          set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 3, (int)(g / N), (int)(g % N), -1, -1);
+          set_error(r, EPREM_GPU_ERR_SUBCYCLES, 3, (int)(g / N), (int)(g % N), -1, -1);
       } else {
         ns_c = (int)nsub;
       }
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
       for (int m = 0; m < P; ++m) {
         if (m < M) {
           const float v = fr[m];
-          if (bad_value(v, &code)) set_error(r.status, code, 2, (int)(g / N), (int)(g % N), e, m);
+          if (bad_value(v, &code)) set_error(r, code, 2, (int)(g / N), (int)(g % N), e, m);
           row[m] = v < FLT_MIN ? FLT_MIN : v;
         }
       }
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
   int code = 0;
   for (int e = 0; e < E; ++e) {
     const float v = expf(fc[e * T] + lns);
-    if (bad_value(v, &code)) set_error(r.status, code, 3, (int)(g / N), (int)(g % N), e, m);
+    if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / N), (int)(g % N), e, m);
     col[e * M] = v < FLT_MIN ? FLT_MIN : v;
   }
 }

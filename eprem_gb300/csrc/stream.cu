@@ -96,7 +96,7 @@ __global__ void __launch_bounds__((StreamShape<Real, MMAX, RegCoef>::T), 1)
   const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
   const double nst = floor(r.dt / dtMin + 1.0);
   if (!(nst <= (double)r.max_subcycles)) {
-    if (crank == 0 && tid == 0) set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    if (crank == 0 && tid == 0) set_error(r, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
     return;  // uniform over the cluster
   }
   const int nsteps = (int)nst;
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__((StreamShape<Real, MMAX, RegCoef>::T), 1)
     for (int mu = 0; mu < MMAX; ++mu) {
       if (mu < M) {
         Real v = fr[mu];
-        if (bad_value(v, &code)) set_error(r.status, code, 1, s, k, e, mu);
+        if (bad_value(v, &code)) set_error(r, code, 1, s, k, e, mu);
         fr[mu] = v < fl ? fl : v;
       }
     }

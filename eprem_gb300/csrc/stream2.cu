@@ -72,7 +72,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
   const double nst = floor(r.dt / dtMin + 1.0);
   if (!(nst <= (double)r.max_subcycles)) {
-    if (crank == 0 && tid == 0) set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    if (crank == 0 && tid == 0) set_error(r, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
     return;
   }
   const int nsteps = (int)nst;
@@ -237,12 +237,12 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       for (int j = 0; j < H; ++j) {
         if (j < nL) {
           const float v = Lf[q][j];
-          if (bad_value(v, &code)) set_error(r.status, code, 1, s, k, e, j);
+          if (bad_value(v, &code)) set_error(r, code, 1, s, k, e, j);
           Lf[q][j] = v < FLT_MIN ? FLT_MIN : v;
         }
         if (j < nR) {
           const float v = Rf[q][j];
-          if (bad_value(v, &code)) set_error(r.status, code, 1, s, k, e, m0 + j);
+          if (bad_value(v, &code)) set_error(r, code, 1, s, k, e, m0 + j);
           Rf[q][j] = v < FLT_MIN ? FLT_MIN : v;
         }
       }
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
   const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
   const double nst = floor(r.dt / dtMin + 1.0);
   if (!(nst <= (double)r.max_subcycles)) {
-    if (crank == 0 && tid == 0) set_error(r.status, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    if (crank == 0 && tid == 0) set_error(r, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
     return;
   }
   const int nsteps = (int)nst;
@@ -512,12 +512,12 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
       for (int p = 0; p < P; ++p) {
         float2 a = Lf[q][p], b = Rf[q][p];
         if (FILLED || p < nPL) {
-          if (bad_value(a.x, &code)) set_error(r.status, code, 1, s, k, e, 2 * p);
-          if (bad_value(a.y, &code)) set_error(r.status, code, 1, s, k, e, 2 * p + 1);
+          if (bad_value(a.x, &code)) set_error(r, code, 1, s, k, e, 2 * p);
+          if (bad_value(a.y, &code)) set_error(r, code, 1, s, k, e, 2 * p + 1);
         }
         if (FILLED || p < nPR) {
-          if (bad_value(b.x, &code)) set_error(r.status, code, 1, s, k, e, m0 + 2 * p);
-          if (bad_value(b.y, &code)) set_error(r.status, code, 1, s, k, e, m0 + 2 * p + 1);
+          if (bad_value(b.x, &code)) set_error(r, code, 1, s, k, e, m0 + 2 * p);
+          if (bad_value(b.y, &code)) set_error(r, code, 1, s, k, e, m0 + 2 * p + 1);
         }
         a.x = a.x < FLT_MIN ? FLT_MIN : a.x; a.y = a.y < FLT_MIN ? FLT_MIN : a.y;
         b.x = b.x < FLT_MIN ? FLT_MIN : b.x; b.y = b.y < FLT_MIN ? FLT_MIN : b.y;

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kRowThreads)
 #pragma unroll
   for (int m = 0; m < kSurM; ++m) {
     const float v = fr[m];
-    if (bad_value(v, &code)) set_error(r.status, code, 2, (int)(g / r.N), (int)(g % r.N), e, m);
+    if (bad_value(v, &code)) set_error(r, code, 2, (int)(g / r.N), (int)(g % r.N), e, m);
     row[m] = v < FLT_MIN ? FLT_MIN : v;
   }
 }

@@ -173,8 +173,9 @@ static void dropin_init(void) {
   dropin_t_del = config.tDel;
   dropin_sn = (size_t)d.num_streams * d.num_nodes;
   dropin_cells = dropin_sn * d.num_energies * d.num_mu;
-  dropin_f = (double *)malloc(sizeof(double) * dropin_cells);
-  dropin_nodes = (double *)malloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
+  /* page-locked, so the chunked copies of the EP update overlap it */
+  dropin_f = (double *)eprem_gpu_host_alloc(sizeof(double) * dropin_cells);
+  dropin_nodes = (double *)eprem_gpu_host_alloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
   if (!dropin_f || !dropin_nodes) panic("GPU path: host staging allocation failed");
 }
 
@@ -238,13 +239,12 @@ void updateEnergeticParticles(void) {
   double t0 = MPI_Wtime();
   dropin_pack_f();
   dropin_pack_nodes(DROPIN_EP_IN);
-  dropin_check(eprem_gpu_upload_f(dropin_run, dropin_f), "upload f");
   dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, DROPIN_EP_IN), "upload nodes");
-  dropin_check(eprem_gpu_update_energetic_particles(dropin_run, t_global),
+  /* f goes up, through the update and back in overlapped chunks */
+  dropin_check(eprem_gpu_update_energetic_particles_host(dropin_run, dropin_f, dropin_f, t_global),
                "updateEnergeticParticles");
   eprem_ep_stats_t st;
   dropin_check(eprem_gpu_read_stats(dropin_run, &st), "updateEnergeticParticles");
-  dropin_check(eprem_gpu_download_f(dropin_run, dropin_f), "download f");
   dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, DROPIN_EP_OUT),
                "download nodes");
   dropin_unpack_f();

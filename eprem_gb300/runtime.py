@@ -37,6 +37,10 @@ EXPORTS = [
     ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_set_time_step", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_update_energetic_particles_host", C.c_int,
+     [C.c_void_p, DP, DP, C.c_double]),
+    ("eprem_gpu_host_alloc", C.c_void_p, [C.c_size_t]),
+    ("eprem_gpu_host_free", None, [C.c_void_p]),
     ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_omni_flux_static", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_synchronize", C.c_int, [C.c_void_p]),
@@ -205,6 +209,20 @@ class EpremRun:
     def move_nodes(self, dt: float):
         """moveNodes (src/simCore.c:737-785)."""
         self._check(self.lib.eprem_gpu_move_nodes(self.handle, dt))
+
+    def update_energetic_particles_host(self, f_in: np.ndarray, f_out: np.ndarray = None,
+                                       t_global: float = 0.0) -> np.ndarray:
+        """updateEnergeticParticles with f in host memory, copies overlapped
+        with the update chunk by chunk (f_out may be f_in; pinned memory
+        lets the copies overlap)."""
+        n = self.num_cells
+        assert f_in.dtype == np.float64 and f_in.size == n and f_in.flags["C_CONTIGUOUS"]
+        if f_out is None:
+            f_out = np.empty(n)
+        assert f_out.dtype == np.float64 and f_out.size == n and f_out.flags["C_CONTIGUOUS"]
+        self._check(self.lib.eprem_gpu_update_energetic_particles_host(
+            self.handle, f_in.ctypes.data_as(DP), f_out.ctypes.data_as(DP), t_global))
+        return f_out
 
     def set_time_step(self, t_del: float):
         """A new config.tDel from the next call on, as SetDT

@@ -244,6 +244,27 @@ int eprem_gpu_download_nodes(eprem_gpu_run *run, double *nodes_host,
  * are not supported. */
 int eprem_gpu_update_energetic_particles(eprem_gpu_run *run, double t_global);
 
+/* The same update with f in host memory (f_in and f_out: S*N*E*M doubles,
+ * stream-major as eprem_gpu_upload_f; they may be the same array): what the
+ * drop-in's updateEnergeticParticles does with eParts.  The streams go
+ * through in about eight chunks, and each chunk's host-to-device copy,
+ * update and device-to-host copy overlap the neighbouring chunks' work, so
+ * the copies hide behind the update (with pinned host memory).  Node fields
+ * are not copied: upload and download them as for
+ * eprem_gpu_update_energetic_particles.  Returns when f_out holds the result;
+ * statistics accumulate as for that call.  No reference counterpart beyond
+ * the gather / update / scatter of src/simCore.c:178-318 and
+ * src/energeticParticles.c:70-203. */
+int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *run, const double *f_in,
+                                              double *f_out, double t_global);
+
+/* Page-locked host memory (NULL on failure) for the host arrays of the calls
+ * above: copies from it run asynchronously at the link's rate, which the
+ * overlap of eprem_gpu_update_energetic_particles_host needs.  Replaces the
+ * malloc of the host staging a caller would otherwise use. */
+void *eprem_gpu_host_alloc(size_t bytes);
+void eprem_gpu_host_free(void *ptr);
+
 /* Statistics accumulated since the previous read (then reset), as the driver
  * prints and resets them once per step (src/eprem.c:694-716).  Synchronizes. */
 int eprem_gpu_read_stats(eprem_gpu_run *run, eprem_ep_stats_t *stats);
@@ -413,8 +434,8 @@ int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *ens, int *chosen_variants);
  * side, the runs spread over them largest first onto the chain with the
  * fewest cells (1, the default: every run after the previous one; 0: one
  * branch per run, all side by side).  Runs that each fill the GPU step
- * fastest in one chain (8 runs of 0.1-2.6 G cells: one chain 8.55e9
- * cell-updates/s, one branch per run 8.14e9); side-by-side branches are for
+ * fastest in one chain (8 runs of 0.1-2.6 G cells: one chain 9.30e9
+ * cell-updates/s, one branch per run 9.06e9); side-by-side branches are for
  * runs too small to fill it.  The next step captures a new graph. */
 int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *ens, int chains);
 int eprem_gpu_ensemble_step(eprem_gpu_ensemble *ens);

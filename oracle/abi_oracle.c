@@ -189,6 +189,17 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
                                                 nt > 0 ? nt : 1, err);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, err);
 }
+void *eprem_gpu_host_alloc(size_t bytes) { return malloc(bytes ? bytes : 1); }
+void eprem_gpu_host_free(void *p) { free(p); }
+
+int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_in,
+                                              double *f_out, double t_global) {
+  int rc = eprem_gpu_upload_f(r, f_in);
+  if (rc == EPREM_GPU_OK) rc = eprem_gpu_update_energetic_particles(r, t_global);
+  if (rc == EPREM_GPU_OK) rc = eprem_gpu_download_f(r, f_out);
+  return rc;
+}
+
 int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *s) {
   *s = r->stats;
   stats_reset(&r->stats);

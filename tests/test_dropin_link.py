@@ -31,7 +31,7 @@ def test_driver_links_against_dropin():
                  "masMoveNodes_cpu"):
         assert name in defined
     undefined = {ln.split()[-1] for ln in syms.splitlines() if " U " in ln}
-    assert {"eprem_gpu_create", "eprem_gpu_update_energetic_particles",
+    assert {"eprem_gpu_create", "eprem_gpu_update_energetic_particles_host",
             "eprem_gpu_update_mhd", "eprem_gpu_move_nodes", "eprem_gpu_mas_init",
             "eprem_gpu_mas_load_slice", "eprem_gpu_mas_select", "eprem_gpu_mas_move_nodes",
             "eprem_gpu_mas_use"} <= undefined

@@ -1,0 +1,57 @@
+"""The host-buffer update (eprem_gpu_update_energetic_particles_host): the
+streams go through in chunks whose copies overlap the neighbouring chunks'
+updates.  Streams are independent on this path, so the result must be
+bit-identical to uploading f, updating the whole run and downloading f."""
+import numpy as np
+import pytest
+
+from eprem_gb300 import EpremGpuError, EpremRun, abi, workloads as W
+
+from helpers import primed_state
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+@pytest.mark.parametrize("in_place", [False, True])
+def test_host_update_equals_whole_run_update(oracle_lib, precision, in_place):
+    # 30 streams: chunks of 4, the last one of 2
+    w = W.custom(1, 5, 60, 8, 8, num_ep_steps=2)
+    d, g, f, nodes = primed_state(w, oracle_lib, precision)
+    whole = EpremRun(d, w.params, g)
+    whole.upload_f(f)
+    whole.upload_nodes(nodes)
+    whole.update_energetic_particles(0.0)
+    st_w = whole.read_stats()
+    f_w = whole.download_f()
+    n_w = whole.download_nodes()
+    whole.close()
+    run = EpremRun(d, w.params, g)
+    run.upload_nodes(nodes)
+    f_in = f.copy()
+    f_out = f_in if in_place else np.empty_like(f_in)
+    run.update_energetic_particles_host(f_in, f_out, 0.0)
+    st = run.read_stats()
+    n_h = run.download_nodes()
+    run.close()
+    np.testing.assert_array_equal(f_out, f_w)
+    np.testing.assert_array_equal(n_h, n_w)
+    assert st.as_dict() == st_w.as_dict()
+    if not in_place:
+        np.testing.assert_array_equal(f_in, f)  # input untouched
+
+
+def test_host_update_reports_the_run_stream(oracle_lib):
+    """A NaN in a late chunk is reported at its stream number in the run."""
+    w = W.custom(1, 5, 30, 8, 6, num_ep_steps=2)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    bad = f.copy()
+    s_bad = 27  # chunk 6 of 8
+    bad[((s_bad * 30 + 15) * 8 + 3) * 6 + 2] = np.nan
+    run = EpremRun(d, w.params, g)
+    run.upload_nodes(nodes)
+    with pytest.raises(EpremGpuError) as ei:
+        run.update_energetic_particles_host(bad, np.empty_like(bad), 0.0)
+    assert ei.value.code == abi.EPREM_GPU_ERR_NAN
+    assert f"stream {s_bad}" in str(ei.value), str(ei.value)
+    run.close()
