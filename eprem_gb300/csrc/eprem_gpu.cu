@@ -480,7 +480,8 @@ extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_g
 // The same update with f in host memory, pipelined: the streams go through in
 // chunks; chunk c's host-to-device copy runs on the copy stream while chunk
 // c-1 is updated on the run's stream, and its device-to-host copy while chunk
-// c+1 is updated.  The FP32 form converts each chunk in one of two staging
+// c+1 is updated (measured on a GB300 whose host link moved 31 GB/s back:
+// 0.26-0.30 s of copies left per 4.81 s step with eight equal chunks).  The FP32 form converts each chunk in one of two staging
 // buffers (chunk c in buffer c % 2, reused once chunk c-2's copy back has
 // left it).  Synchronous: f_out holds the result on return.
 extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_in,
@@ -495,12 +496,25 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
   }
   const int S = r->dims.num_streams;
   const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
-  // about eight chunks: each copy is short beside an update, and the first
-  // upload and last download, the only ones not hidden, stay small
-  const int cs = (S + 7) / 8;
-  const int nch = (S + cs - 1) / cs;
+  // Chunks: a short first and last one (1/32 of the streams each: the first
+  // upload and the last download are the copies nothing hides) around six
+  // long ones, whose copies each take less than a neighbour's update.
+  std::vector<int> bounds{0};
+  const int edge = S >= 64 ? (S + 31) / 32 : (S >= 8 ? 1 : 0);
+  if (edge) {
+    const int mid = S - 2 * edge;
+    bounds.push_back(edge);
+    for (int i = 1; i <= 6; i++) {
+      const int b = edge + (int)((long long)mid * i / 6);
+      if (b > bounds.back()) bounds.push_back(b);
+    }
+  }
+  if (bounds.back() < S) bounds.push_back(S);
+  const int nch = (int)bounds.size() - 1;
+  int widest = 0;
+  for (int c = 0; c < nch; c++) widest = std::max(widest, bounds[c + 1] - bounds[c]);
   const bool fp32 = r->dims.precision == EPREM_FP32;
-  int rc = ensure_stage(r, fp32 ? (size_t)cs * per_stream : 1);
+  int rc = ensure_stage(r, fp32 ? (size_t)widest * per_stream : 1);
   if (rc) return rc;
   cudaEvent_t *arrived = r->stage_ev, *updated = r->stage_ev + 2;
   // the run's earlier work on f and the staging buffers comes first
@@ -508,21 +522,21 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
   CK(cudaStreamWaitEvent(r->copy_stream, updated[0], 0));
   auto dev64 = [&](int c) {  // chunk c on the device as FP64: staging or f itself
     return fp32 ? r->d_stage + (size_t)(c & 1) * r->stage_elems
-                : static_cast<double *>(r->d_f) + (size_t)c * cs * per_stream;
+                : static_cast<double *>(r->d_f) + (size_t)bounds[c] * per_stream;
   };
   auto h2d = [&](int c) -> int {
-    const int s0 = c * cs, s1 = s0 + cs < S ? s0 + cs : S;
-    const size_t n = (size_t)(s1 - s0) * per_stream;
-    CK(cudaMemcpyAsync(dev64(c), f_in + (size_t)s0 * per_stream, n * sizeof(double),
+    const size_t n = (size_t)(bounds[c + 1] - bounds[c]) * per_stream;
+    CK(cudaMemcpyAsync(dev64(c), f_in + (size_t)bounds[c] * per_stream, n * sizeof(double),
                        cudaMemcpyHostToDevice, r->copy_stream));
     CK(cudaEventRecord(arrived[c & 1], r->copy_stream));
     return EPREM_GPU_OK;
   };
+  // Per chunk, the update is queued first, then the next chunk's upload and
+  // this chunk's download: the device has the update to run even while the
+  // host sits in a copy call.
   rc = h2d(0);
   for (int c = 0; c < nch && !rc; c++) {
-    if (c + 1 < nch) rc = h2d(c + 1);  // copy stream: after chunk c-1's download
-    if (rc) break;
-    const int s0 = c * cs, s1 = s0 + cs < S ? s0 + cs : S;
+    const int s0 = bounds[c], s1 = bounds[c + 1];
     const size_t n = (size_t)(s1 - s0) * per_stream;
     const RunView v = stream_range_view(r, s0, s1);
     CK(cudaStreamWaitEvent(r->stream, arrived[c & 1], 0));
@@ -539,6 +553,8 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
       if (rc) return fail(rc, "conversion kernel launch failed");
     }
     CK(cudaEventRecord(updated[c & 1], r->stream));
+    if (c + 1 < nch) rc = h2d(c + 1);  // copy stream: after chunk c-1's download
+    if (rc) break;
     CK(cudaStreamWaitEvent(r->copy_stream, updated[c & 1], 0));
     CK(cudaMemcpyAsync(f_out + (size_t)s0 * per_stream, dev64(c), n * sizeof(double),
                        cudaMemcpyDeviceToHost, r->copy_stream));

@@ -247,9 +247,10 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *run, double t_global);
 /* The same update with f in host memory (f_in and f_out: S*N*E*M doubles,
  * stream-major as eprem_gpu_upload_f; they may be the same array): what the
  * drop-in's updateEnergeticParticles does with eParts.  The streams go
- * through in about eight chunks, and each chunk's host-to-device copy,
- * update and device-to-host copy overlap the neighbouring chunks' work, so
- * the copies hide behind the update (with pinned host memory).  Node fields
+ * through in chunks (a short first and last one around six long ones), and
+ * each chunk's host-to-device copy, update and device-to-host copy overlap
+ * the neighbouring chunks' work, so the copies hide behind the update (with
+ * page-locked host memory).  Node fields
  * are not copied: upload and download them as for
  * eprem_gpu_update_energetic_particles.  Returns when f_out holds the result;
  * statistics accumulate as for that call.  No reference counterpart beyond
