@@ -485,17 +485,22 @@ extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_g
 // buffers (chunk c in buffer c % 2, reused once chunk c-2's copy back has
 // left it).  Synchronous: f_out holds the result on return.
 extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_in,
-                                                         double *f_out, double t_global) {
+                                                         double *f_out, size_t stream_pitch,
+                                                         double t_global) {
   (void)t_global;
   if (!r || !f_in || !f_out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const int S = r->dims.num_streams;
+  const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : per_stream;
+  if (pitch < per_stream) return fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
   if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {  // those phases work on the whole run
+    if (pitch != per_stream)
+      return fail(EPREM_GPU_ERR_UNSUPPORTED, "split / surrogate node phases take contiguous f");
     int rc = eprem_gpu_upload_f(r, f_in);
     if (!rc) rc = ep_update(r, r->v);
     if (!rc) rc = eprem_gpu_download_f(r, f_out);
     return rc;
   }
-  const int S = r->dims.num_streams;
-  const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
   // Chunks: a short first and last one (1/32 of the streams each: the first
   // upload and the last download are the copies nothing hides) around six
   // long ones, whose copies each take less than a neighbour's update.
@@ -524,10 +529,16 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
     return fp32 ? r->d_stage + (size_t)(c & 1) * r->stage_elems
                 : static_cast<double *>(r->d_f) + (size_t)bounds[c] * per_stream;
   };
+  const size_t row = per_stream * sizeof(double);
   auto h2d = [&](int c) -> int {
-    const size_t n = (size_t)(bounds[c + 1] - bounds[c]) * per_stream;
-    CK(cudaMemcpyAsync(dev64(c), f_in + (size_t)bounds[c] * per_stream, n * sizeof(double),
-                       cudaMemcpyHostToDevice, r->copy_stream));
+    const size_t rows = (size_t)(bounds[c + 1] - bounds[c]);
+    if (pitch == per_stream)
+      CK(cudaMemcpyAsync(dev64(c), f_in + (size_t)bounds[c] * pitch, rows * row,
+                         cudaMemcpyHostToDevice, r->copy_stream));
+    else
+      CK(cudaMemcpy2DAsync(dev64(c), row, f_in + (size_t)bounds[c] * pitch,
+                           pitch * sizeof(double), row, rows, cudaMemcpyHostToDevice,
+                           r->copy_stream));
     CK(cudaEventRecord(arrived[c & 1], r->copy_stream));
     return EPREM_GPU_OK;
   };
@@ -556,8 +567,12 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
     if (c + 1 < nch) rc = h2d(c + 1);  // copy stream: after chunk c-1's download
     if (rc) break;
     CK(cudaStreamWaitEvent(r->copy_stream, updated[c & 1], 0));
-    CK(cudaMemcpyAsync(f_out + (size_t)s0 * per_stream, dev64(c), n * sizeof(double),
-                       cudaMemcpyDeviceToHost, r->copy_stream));
+    if (pitch == per_stream)
+      CK(cudaMemcpyAsync(f_out + (size_t)s0 * pitch, dev64(c), n * sizeof(double),
+                         cudaMemcpyDeviceToHost, r->copy_stream));
+    else
+      CK(cudaMemcpy2DAsync(f_out + (size_t)s0 * pitch, pitch * sizeof(double), dev64(c), row,
+                           row, (size_t)(s1 - s0), cudaMemcpyDeviceToHost, r->copy_stream));
   }
   CK(cudaStreamSynchronize(r->copy_stream));
   if (rc) return rc;
@@ -575,6 +590,18 @@ extern "C" void *eprem_gpu_host_alloc(size_t bytes) {
 
 extern "C" void eprem_gpu_host_free(void *p) {
   if (p) cudaFreeHost(p);
+}
+
+extern "C" int eprem_gpu_host_register(void *p, size_t bytes) {
+  if (!p || !bytes) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_host_unregister(void *p) {
+  if (!p) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  CK(cudaHostUnregister(p));
+  return EPREM_GPU_OK;
 }
 
 extern "C" int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *stats) {

@@ -49,9 +49,8 @@
 
 static eprem_gpu_run *dropin_run = NULL;
 static double dropin_t_del = 0.0;   /* config.tDel as last passed to the run */
-static double *dropin_f = NULL;     /* [S][N][E][M] host staging of eParts   */
 static double *dropin_nodes = NULL; /* [field][S*N] host staging of grid[]   */
-static size_t dropin_sn = 0, dropin_cells = 0;
+static size_t dropin_sn = 0;
 
 static void dropin_check(int rc, const char *what) {
   if (rc != EPREM_GPU_OK) {
@@ -172,11 +171,15 @@ static void dropin_init(void) {
   dropin_check(eprem_gpu_create(&d, &p, &g, &dropin_run), "eprem_gpu_create");
   dropin_t_del = config.tDel;
   dropin_sn = (size_t)d.num_streams * d.num_nodes;
-  dropin_cells = dropin_sn * d.num_energies * d.num_mu;
-  /* page-locked, so the chunked copies of the EP update overlap it */
-  dropin_f = (double *)eprem_gpu_host_alloc(sizeof(double) * dropin_cells);
   dropin_nodes = (double *)eprem_gpu_host_alloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
-  if (!dropin_f || !dropin_nodes) panic("GPU path: host staging allocation failed");
+  if (!dropin_nodes) panic("GPU path: host staging allocation failed");
+  /* f moves straight between eParts and the device (no host staging); lock
+   * eParts in place so those copies overlap the update -- if it cannot be
+   * locked they stay correct, only slower */
+  if (eprem_gpu_host_register(eParts, sizeof(Scalar_t) * (size_t)NUM_STREAMS * SSPEM) !=
+      EPREM_GPU_OK)
+    fprintf(stderr, "GPU path: eParts not page-locked (%s); copies will not overlap\n",
+            eprem_gpu_last_error());
 }
 
 /* SetDT (src/simCore.c:800-880) changes config.tDel between steps of a
@@ -211,19 +214,6 @@ static void dropin_unpack_nodes(uint64_t mask) {
     }
 }
 
-/* eParts (with the INNER_SHELL ghost) <-> f[s][k][E][M] */
-static void dropin_pack_f(void) {
-  const size_t chunk = (size_t)TOTAL_NUM_SHELLS * SPEM;
-  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
-    memcpy(dropin_f + s * chunk, eParts + s * SSPEM + SPEM, sizeof(double) * chunk);
-}
-
-static void dropin_unpack_f(void) {
-  const size_t chunk = (size_t)TOTAL_NUM_SHELLS * SPEM;
-  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
-    memcpy(eParts + s * SSPEM + SPEM, dropin_f + s * chunk, sizeof(double) * chunk);
-}
-
 #define DROPIN_EP_IN                                                                     \
   (EPREM_NODE_MASK(EPREM_NODE_RX) | EPREM_NODE_MASK(EPREM_NODE_RY) |                    \
    EPREM_NODE_MASK(EPREM_NODE_RZ) | EPREM_NODE_MASK(EPREM_NODE_RMAG) |                  \
@@ -237,17 +227,18 @@ void updateEnergeticParticles(void) {
   dropin_init();
   dropin_sync_step();
   double t0 = MPI_Wtime();
-  dropin_pack_f();
   dropin_pack_nodes(DROPIN_EP_IN);
   dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, DROPIN_EP_IN), "upload nodes");
-  /* f goes up, through the update and back in overlapped chunks */
-  dropin_check(eprem_gpu_update_energetic_particles_host(dropin_run, dropin_f, dropin_f, t_global),
+  /* f goes up, through the update and back in overlapped chunks, straight
+   * from eParts: stream s's shells 1..N follow its INNER_SHELL ghost, stream
+   * after stream at a pitch of SSPEM (src/global.h:61) */
+  dropin_check(eprem_gpu_update_energetic_particles_host(dropin_run, eParts + SPEM, eParts + SPEM,
+                                                         (size_t)SSPEM, t_global),
                "updateEnergeticParticles");
   eprem_ep_stats_t st;
   dropin_check(eprem_gpu_read_stats(dropin_run, &st), "updateEnergeticParticles");
   dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, DROPIN_EP_OUT),
                "download nodes");
-  dropin_unpack_f();
   dropin_unpack_nodes(DROPIN_EP_OUT);
   /* the driver's per-step report (src/eprem.c:694-716) */
   if (st.max_subcycles_change > maxsubcycles_energychange)

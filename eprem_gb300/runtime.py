@@ -38,9 +38,11 @@ EXPORTS = [
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_set_time_step", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_update_energetic_particles_host", C.c_int,
-     [C.c_void_p, DP, DP, C.c_double]),
+     [C.c_void_p, DP, DP, C.c_size_t, C.c_double]),
     ("eprem_gpu_host_alloc", C.c_void_p, [C.c_size_t]),
     ("eprem_gpu_host_free", None, [C.c_void_p]),
+    ("eprem_gpu_host_register", C.c_int, [C.c_void_p, C.c_size_t]),
+    ("eprem_gpu_host_unregister", C.c_int, [C.c_void_p]),
     ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_omni_flux_static", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_synchronize", C.c_int, [C.c_void_p]),
@@ -211,17 +213,21 @@ class EpremRun:
         self._check(self.lib.eprem_gpu_move_nodes(self.handle, dt))
 
     def update_energetic_particles_host(self, f_in: np.ndarray, f_out: np.ndarray = None,
-                                       t_global: float = 0.0) -> np.ndarray:
+                                       t_global: float = 0.0, stream_pitch: int = 0) -> np.ndarray:
         """updateEnergeticParticles with f in host memory, copies overlapped
-        with the update chunk by chunk (f_out may be f_in; pinned memory
-        lets the copies overlap)."""
-        n = self.num_cells
-        assert f_in.dtype == np.float64 and f_in.size == n and f_in.flags["C_CONTIGUOUS"]
+        with the update chunk by chunk.  Stream s's N*E*M values start at
+        element s * stream_pitch (0: N*E*M, contiguous).  f_out may be f_in;
+        page-locked memory lets the copies overlap."""
+        d = self.dims
+        per_stream = d.num_nodes * d.num_energies * d.num_mu
+        pitch = stream_pitch or per_stream
+        need = (d.num_streams - 1) * pitch + per_stream
+        assert f_in.dtype == np.float64 and f_in.size >= need and f_in.flags["C_CONTIGUOUS"]
         if f_out is None:
-            f_out = np.empty(n)
-        assert f_out.dtype == np.float64 and f_out.size == n and f_out.flags["C_CONTIGUOUS"]
+            f_out = np.empty(need)
+        assert f_out.dtype == np.float64 and f_out.size >= need and f_out.flags["C_CONTIGUOUS"]
         self._check(self.lib.eprem_gpu_update_energetic_particles_host(
-            self.handle, f_in.ctypes.data_as(DP), f_out.ctypes.data_as(DP), t_global))
+            self.handle, f_in.ctypes.data_as(DP), f_out.ctypes.data_as(DP), stream_pitch, t_global))
         return f_out
 
     def set_time_step(self, t_del: float):

@@ -244,20 +244,25 @@ int eprem_gpu_download_nodes(eprem_gpu_run *run, double *nodes_host,
  * are not supported. */
 int eprem_gpu_update_energetic_particles(eprem_gpu_run *run, double t_global);
 
-/* The same update with f in host memory (f_in and f_out: S*N*E*M doubles,
- * stream-major as eprem_gpu_upload_f; they may be the same array): what the
- * drop-in's updateEnergeticParticles does with eParts.  The streams go
- * through in chunks (a short first and last one around six long ones), and
- * each chunk's host-to-device copy, update and device-to-host copy overlap
- * the neighbouring chunks' work, so the copies hide behind the update (with
- * page-locked host memory).  Node fields
- * are not copied: upload and download them as for
- * eprem_gpu_update_energetic_particles.  Returns when f_out holds the result;
- * statistics accumulate as for that call.  No reference counterpart beyond
- * the gather / update / scatter of src/simCore.c:178-318 and
+/* The same update with f in host memory: stream s's N*E*M values start at
+ * f_in + s * stream_pitch (and f_out + s * stream_pitch); stream_pitch 0
+ * means N*E*M (f stream-major and contiguous, as eprem_gpu_upload_f).  The
+ * drop-in passes the reference's own array, eParts + SPEM with pitch SSPEM
+ * (one ghost shell before each stream's shells, src/global.h:61,
+ * src/global.c:112), so nothing is packed on the host.  f_in and f_out may be
+ * the same array.  The streams go through in chunks (a short first and last
+ * one around six long ones), and each chunk's host-to-device copy, update
+ * and device-to-host copy overlap the neighbouring chunks' work, so the
+ * copies hide behind the update when the host memory is page-locked
+ * (eprem_gpu_host_alloc, or eprem_gpu_host_register on an existing
+ * allocation).  Node fields are not copied: upload and download them as for
+ * eprem_gpu_update_energetic_particles.  Returns when f_out holds the
+ * result; statistics accumulate as for that call.  No reference counterpart
+ * beyond the gather / update / scatter of src/simCore.c:178-318 and
  * src/energeticParticles.c:70-203. */
 int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *run, const double *f_in,
-                                              double *f_out, double t_global);
+                                              double *f_out, size_t stream_pitch,
+                                              double t_global);
 
 /* Page-locked host memory (NULL on failure) for the host arrays of the calls
  * above: copies from it run asynchronously at the link's rate, which the
@@ -265,6 +270,11 @@ int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *run, const double *
  * malloc of the host staging a caller would otherwise use. */
 void *eprem_gpu_host_alloc(size_t bytes);
 void eprem_gpu_host_free(void *ptr);
+/* Page-lock an existing host allocation in place (cudaHostRegister), e.g.
+ * the reference's eParts; EPREM_GPU_ERR_CUDA if the memory cannot be locked
+ * (copies from it then stay correct but do not overlap). */
+int eprem_gpu_host_register(void *ptr, size_t bytes);
+int eprem_gpu_host_unregister(void *ptr);
 
 /* Statistics accumulated since the previous read (then reset), as the driver
  * prints and resets them once per step (src/eprem.c:694-716).  Synchronizes. */

@@ -192,11 +192,27 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
 void *eprem_gpu_host_alloc(size_t bytes) { return malloc(bytes ? bytes : 1); }
 void eprem_gpu_host_free(void *p) { free(p); }
 
+int eprem_gpu_host_register(void *p, size_t bytes) {
+  (void)p; (void)bytes;
+  return EPREM_GPU_OK;
+}
+int eprem_gpu_host_unregister(void *p) {
+  (void)p;
+  return EPREM_GPU_OK;
+}
+
 int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_in,
-                                              double *f_out, double t_global) {
-  int rc = eprem_gpu_upload_f(r, f_in);
-  if (rc == EPREM_GPU_OK) rc = eprem_gpu_update_energetic_particles(r, t_global);
-  if (rc == EPREM_GPU_OK) rc = eprem_gpu_download_f(r, f_out);
+                                              double *f_out, size_t stream_pitch,
+                                              double t_global) {
+  const size_t per = (size_t)r->d.num_nodes * r->d.num_energies * r->d.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : per;
+  if (pitch < per) return abi_fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
+  for (int s = 0; s < r->d.num_streams; s++)
+    memcpy(r->f + (size_t)s * per, f_in + (size_t)s * pitch, per * sizeof(double));
+  int rc = eprem_gpu_update_energetic_particles(r, t_global);
+  if (rc == EPREM_GPU_OK)
+    for (int s = 0; s < r->d.num_streams; s++)
+      memcpy(f_out + (size_t)s * pitch, r->f + (size_t)s * per, per * sizeof(double));
   return rc;
 }
 

@@ -55,3 +55,31 @@ def test_host_update_reports_the_run_stream(oracle_lib):
     assert ei.value.code == abi.EPREM_GPU_ERR_NAN
     assert f"stream {s_bad}" in str(ei.value), str(ei.value)
     run.close()
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+def test_host_update_with_a_stream_pitch(oracle_lib, precision):
+    """f laid out as the reference's eParts: a ghost shell of E*M values
+    before each stream's N shells (pitch (N+1)*E*M).  The result matches the
+    contiguous call and the ghost shells stay as they were."""
+    w = W.custom(1, 5, 60, 8, 8, num_ep_steps=2)
+    d, g, f, nodes = primed_state(w, oracle_lib, precision)
+    S, N, E, M = d.num_streams, d.num_nodes, d.num_energies, d.num_mu
+    per, ghost = N * E * M, E * M
+    pitch = per + ghost
+    padded = np.full(S * pitch, -7.0)
+    view = padded.reshape(S, pitch)
+    view[:, ghost:] = f.reshape(S, per)
+    run = EpremRun(d, w.params, g)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles_host(padded[ghost:], padded[ghost:], 0.0, stream_pitch=pitch)
+    st = run.read_stats()
+    run.close()
+    ref = EpremRun(d, w.params, g)
+    ref.upload_nodes(nodes)
+    f_ref = ref.update_energetic_particles_host(f.copy(), None, 0.0)
+    st_ref = ref.read_stats()
+    ref.close()
+    np.testing.assert_array_equal(view[:, ghost:].reshape(-1), f_ref)
+    assert np.all(view[:, :ghost] == -7.0)
+    assert st.as_dict() == st_ref.as_dict()
