@@ -181,10 +181,13 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
 // A CTA's 128 rows are contiguous in f: they pass through shared memory
 // (float4 loads and stores, rows padded to an odd pitch so each thread's row
 // reads are free of bank conflicts) instead of one strided row per thread.
-template <int P>
+// FULL: M fills the register row (M = P), so every cell guard and the row /
+// column split of the staging loops are known at compile time.
+template <int P, bool FULL>
 __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
   extern __shared__ float tile[];  // [kFocusThreads][pitch]
-  const int E = r.E, M = r.M, N = r.N;
+  const int E = r.E, N = r.N;
+  const int M = FULL ? P : r.M;
   const int pitch = M | 1;
   const size_t rows = (size_t)r.S * N * E;
   const size_t it0 = (size_t)blockIdx.x * kFocusThreads;
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
     const float xs[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int i = 4 * v + k, rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+      const int i = 4 * v + k, rr = FULL ? i / P : (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
       tile[rr * pitch + cc] = xs[k];
     }
   }
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
     float xs[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int i = 4 * v + k, rr = (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
+      const int i = 4 * v + k, rr = FULL ? i / P : (int)(((float)i + 0.5f) * inv_m), cc = i - rr * M;
       xs[k] = tile[rr * pitch + cc];
     }
     reinterpret_cast<float4 *>(base)[v] = make_float4(xs[0], xs[1], xs[2], xs[3]);
@@ -373,8 +376,11 @@ template <int P>
 static void launch_focus_t(const RunView &r, cudaStream_t st) {
   const size_t rows = (size_t)r.S * r.N * r.E;
   const size_t smem = (size_t)kFocusThreads * (r.M | 1) * sizeof(float);
-  k_focus32<P><<<(unsigned)((rows + kFocusThreads - 1) / kFocusThreads), kFocusThreads, smem, st>>>(
-      r);
+  const unsigned blocks = (unsigned)((rows + kFocusThreads - 1) / kFocusThreads);
+  if (r.M == P)
+    k_focus32<P, true><<<blocks, kFocusThreads, smem, st>>>(r);
+  else
+    k_focus32<P, false><<<blocks, kFocusThreads, smem, st>>>(r);
 }
 
 static void launch_change(const RunView &r, cudaStream_t st) {
