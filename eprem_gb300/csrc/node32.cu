@@ -304,7 +304,9 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
   float *fc = lnf + tid;                                       // stride kChangeThreads
   constexpr int T = kChangeThreads;
   const float lns = (float)r.ln_f_shift;  // the shift of the FP32 store, off ln f
-  for (int e = 0; e < E; ++e) fc[e * T] = logf(col[e * M]) - lns;
+  // the hardware approximations: ~1e-6 absolute on ln f, i.e. ~1e-6
+  // relative on f, far inside the FP32 form's 1e-3 flux tolerance
+  for (int e = 0; e < E; ++e) fc[e * T] = __logf(col[e * M]) - lns;
   if (c.ns_c > 0) {
     const float mu = r.mugrid32[m];
     const float am = -mu * c.dupar;
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
   }
   int code = 0;
   for (int e = 0; e < E; ++e) {
-    const float v = expf(fc[e * T] + lns);
+    const float v = __expf(fc[e * T] + lns);
     if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / N), (int)(g % N), e, m);
     col[e * M] = v < FLT_MIN ? FLT_MIN : v;
   }
