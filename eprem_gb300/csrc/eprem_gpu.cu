@@ -295,6 +295,7 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
     if (ev) cudaEventDestroy(ev);
   if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
   cudaFree(r->d_flux);
+  cudaFree(r->d_tmpl);
   for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
   for (auto &slot : r->mas_allocs)
     for (void *p : slot) cudaFree(p);
@@ -382,6 +383,77 @@ extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
     CK(cudaStreamWaitEvent(r->stream, copied[0], 0));
   }
   return check_status(r, false, nullptr);
+}
+
+static RunView stream_range_view(const eprem_gpu_run *r, int s0, int s1);
+
+// Pitched forms: stream s's N*E*M values at f + s * stream_pitch.  The FP32
+// form goes through the staging buffer a group of whole streams at a time.
+static int copy_f_pitched(eprem_gpu_run *r, double *host, size_t stream_pitch, bool up) {
+  const size_t per = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : per;
+  if (pitch < per) return fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
+  if (pitch == per) return up ? eprem_gpu_upload_f(r, host) : eprem_gpu_download_f(r, host);
+  const int S = r->dims.num_streams;
+  const size_t row = per * sizeof(double);
+  if (r->dims.precision == EPREM_FP64) {
+    if (up)
+      CK(cudaMemcpy2DAsync(r->d_f, row, host, pitch * sizeof(double), row, S,
+                           cudaMemcpyHostToDevice, r->stream));
+    else
+      CK(cudaMemcpy2DAsync(host, pitch * sizeof(double), r->d_f, row, row, S,
+                           cudaMemcpyDeviceToHost, r->stream));
+    return up ? EPREM_GPU_OK : check_status(r, false, nullptr);
+  }
+  const int group = std::max(1, (int)std::min<size_t>((size_t)S, kStageChunk / per));
+  int rc = ensure_stage(r, (size_t)group * per);
+  if (rc) return rc;
+  // the copy stream's downloads may still read the staging buffers
+  CK(cudaEventRecord(r->stage_ev[2], r->copy_stream));
+  CK(cudaStreamWaitEvent(r->stream, r->stage_ev[2], 0));
+  for (int s0 = 0; s0 < S; s0 += group) {
+    const int ns = std::min(group, S - s0);
+    const RunView v = stream_range_view(r, s0, s0 + ns);
+    double *buf = r->d_stage;
+    if (up) {
+      CK(cudaMemcpy2DAsync(buf, row, host + (size_t)s0 * pitch, pitch * sizeof(double), row, ns,
+                           cudaMemcpyHostToDevice, r->stream));
+      rc = launch_convert_f(v, buf, static_cast<double *>(v.f), 1, ns * per, r->stream,
+                            &r->launches);
+    } else {
+      rc = launch_convert_f(v, static_cast<const double *>(v.f), buf, 0, ns * per, r->stream,
+                            &r->launches);
+      if (!rc)
+        CK(cudaMemcpy2DAsync(host + (size_t)s0 * pitch, pitch * sizeof(double), buf, row, row, ns,
+                             cudaMemcpyDeviceToHost, r->stream));
+    }
+    if (rc) return fail(rc, "conversion kernel launch failed");
+  }
+  return up ? EPREM_GPU_OK : check_status(r, false, nullptr);
+}
+
+extern "C" int eprem_gpu_upload_f_pitched(eprem_gpu_run *r, const double *f, size_t stream_pitch) {
+  if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  return copy_f_pitched(r, const_cast<double *>(f), stream_pitch, true);
+}
+
+extern "C" int eprem_gpu_download_f_pitched(eprem_gpu_run *r, double *f, size_t stream_pitch) {
+  if (!r || !f) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  return copy_f_pitched(r, f, stream_pitch, false);
+}
+
+extern "C" int eprem_gpu_ripple_f(eprem_gpu_run *r, const double *tmpl, size_t stream_pitch) {
+  if (!r || !tmpl) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  const size_t em = (size_t)r->dims.num_energies * r->dims.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : em;
+  if (pitch < em) return fail(EPREM_GPU_ERR_ARG, "stream_pitch below E*M");
+  const int S = r->dims.num_streams;
+  if (!r->d_tmpl) CK(cudaMalloc(&r->d_tmpl, (size_t)S * em * sizeof(double)));
+  CK(cudaMemcpy2DAsync(r->d_tmpl, em * sizeof(double), tmpl, pitch * sizeof(double),
+                       em * sizeof(double), S, cudaMemcpyHostToDevice, r->stream));
+  if (launch_ripple_f(r->v, r->d_tmpl, r->stream, &r->launches))
+    return cuda_fail(cudaGetLastError(), "ripple launch");
+  return EPREM_GPU_OK;
 }
 
 extern "C" int eprem_gpu_upload_nodes(eprem_gpu_run *r, const double *nodes, uint64_t mask) {

@@ -211,6 +211,44 @@ int launch_convert_f(const RunView &r, const double *src64, double *dst64, int t
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
+// rippleShellsOut (src/simCore.c:700-735) for f: node k of every stream takes
+// node k-1's values (the outermost node's are dropped) and node 0 takes the
+// stream's template row (the reference's INNER_SHELL).  A thread owns one
+// (stream, energy, mu) cell and walks the nodes outward-in, reading a batch
+// of nodes before writing them, so every value is read before it is
+// overwritten; tmpl: S*E*M doubles, converted like an upload.
+template <typename Real>
+__global__ void k_ripple_f(RunView r, const double *tmpl) {
+  const size_t EM = (size_t)r.E * r.M;
+  const size_t cells = (size_t)r.S * EM;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < cells;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = c / EM, j = c - s * EM;
+    Real *p = reinterpret_cast<Real *>(r.f) + s * r.N * EM + j;
+    for (int k = r.N - 1; k >= 1; k -= 8) {
+      const int cnt = k < 8 ? k : 8;
+      Real v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (u < cnt) v[u] = p[(size_t)(k - 1 - u) * EM];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (u < cnt) p[(size_t)(k - u) * EM] = v[u];
+    }
+    p[0] = to_real<Real>(tmpl[c] * r.f_scale);
+  }
+}
+
+int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint64_t *launches) {
+  const size_t cells = (size_t)r.S * r.E * r.M;
+  if (r.precision == EPREM_FP64)
+    k_ripple_f<double><<<grid_for(cells), 256, 0, st>>>(r, tmpl);
+  else
+    k_ripple_f<float><<<grid_for(cells), 256, 0, st>>>(r, tmpl);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
 // Synthetic seed population: f = sepSeedFunction(E, r) (1 + perturb U) per
 // (stream, node, energy), isotropic in mu, with U in (-1, 1) from the top 53
 // bits of splitmix64(seed) at index (stream * N + node) * E + energy + 1 --

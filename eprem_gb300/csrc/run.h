@@ -53,6 +53,7 @@ struct eprem_gpu_run {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t stage_ev[4] = {};  // converted[2], copied[2]
   double *d_flux = nullptr;
+  double *d_tmpl = nullptr;   // [S][E][M] template rows of eprem_gpu_ripple_f
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch
   bool timing = false;

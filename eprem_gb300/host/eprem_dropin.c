@@ -7,8 +7,20 @@
  *   updateMhd()                 src/flow.c:36-154
  *   moveNodes(dt)               src/simCore.c:737-785
  *   masMoveNodes(dt)            src/masInterp.c:1344-1393
+ *   rotSunAndSpawnShell(dt)     src/simCore.c:443-630
+ * and around
+ *   dataDumpIO()                src/unifiedOutput.c:1479-1531
+ *   initEnergeticParticles()    src/energeticParticlesInit.c:103-147
  * (the originals are renamed with -D at compile time so that the driver
  * src/eprem.c, unchanged, calls these).
+ *
+ * f lives on the device from the first shell ripple on: the EP update works
+ * on it there, rotSunAndSpawnShell ripples it there (the grid still ripples
+ * on the host), and eParts is brought up to date only before the driver
+ * reads it, in dataDumpIO.  The driver writes eParts only through
+ * initEnergeticParticles (after seeding, at the first EP step, and after
+ * every step of the seed test); the device copy is dropped then and taken
+ * again at its next use.
  *
  * The reference keeps its state in globals (grid[], eParts[], config, the
  * 1-D grids of energeticParticlesTypes.h); each call here packs what the GPU
@@ -47,8 +59,17 @@
 
 #include "eprem_gpu.h"
 
+/* The reference's own output routine and seed-population initialisation,
+ * renamed at compile time (-DdataDumpIO=dataDumpIO_cpu on
+ * src/unifiedOutput.c, -DinitEnergeticParticles=initEnergeticParticles_cpu on
+ * src/energeticParticlesInit.c). */
+void dataDumpIO_cpu(void);
+void initEnergeticParticles_cpu(void);
+
 static eprem_gpu_run *dropin_run = NULL;
 static double dropin_t_del = 0.0;   /* config.tDel as last passed to the run */
+static int dropin_f_dev = 0;        /* the device holds f (eParts shells 1..N) */
+static int dropin_f_stale = 0;      /* eParts is older than the device's f     */
 static double *dropin_nodes = NULL; /* [field][S*N] host staging of grid[]   */
 static size_t dropin_sn = 0;
 
@@ -223,18 +244,32 @@ static void dropin_unpack_nodes(uint64_t mask) {
   (EPREM_NODE_MASK(EPREM_NODE_DS) | EPREM_NODE_MASK(EPREM_NODE_BMAG_PLUS) |             \
    EPREM_NODE_MASK(EPREM_NODE_BMAG_MINUS))
 
+/* f between eParts (shells 1..N of each stream, pitch SSPEM past the
+ * INNER_SHELL row, src/global.h:61) and the device */
+static void dropin_f_to_device(void) {
+  if (dropin_f_dev) return;
+  dropin_check(eprem_gpu_upload_f_pitched(dropin_run, eParts + SPEM, (size_t)SSPEM), "upload f");
+  dropin_f_dev = 1;
+  dropin_f_stale = 0;
+}
+
+static void dropin_f_to_host(void) {
+  if (!dropin_f_stale) return;
+  dropin_f_stale = 0;
+  dropin_check(eprem_gpu_download_f_pitched(dropin_run, eParts + SPEM, (size_t)SSPEM),
+               "download f");
+}
+
 void updateEnergeticParticles(void) {
   dropin_init();
   dropin_sync_step();
   double t0 = MPI_Wtime();
+  dropin_f_to_device();
   dropin_pack_nodes(DROPIN_EP_IN);
   dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, DROPIN_EP_IN), "upload nodes");
-  /* f goes up, through the update and back in overlapped chunks, straight
-   * from eParts: stream s's shells 1..N follow its INNER_SHELL ghost, stream
-   * after stream at a pitch of SSPEM (src/global.h:61) */
-  dropin_check(eprem_gpu_update_energetic_particles_host(dropin_run, eParts + SPEM, eParts + SPEM,
-                                                         (size_t)SSPEM, t_global),
+  dropin_check(eprem_gpu_update_energetic_particles(dropin_run, t_global),
                "updateEnergeticParticles");
+  dropin_f_stale = 1;
   eprem_ep_stats_t st;
   dropin_check(eprem_gpu_read_stats(dropin_run, &st), "updateEnergeticParticles");
   dropin_check(eprem_gpu_download_nodes(dropin_run, dropin_nodes, DROPIN_EP_OUT),
@@ -247,6 +282,49 @@ void updateEnergeticParticles(void) {
     maxsubcycles_focusing = st.max_subcycles_focusing;
   if (st.min_tau < min_tau) min_tau = st.min_tau;
   timer_diffusestream += MPI_Wtime() - t0;
+}
+
+/* rotSunAndSpawnShell for one rank (no shell arrives from an inner rank,
+ * src/simCore.c:481-599): rotate the sun, ripple the shells out -- the nodes
+ * on the host as rippleShellsOut does (src/simCore.c:700-735: each node takes
+ * its inner neighbour's data but keeps its own neighbour links), f on the
+ * device with the INNER_SHELL rows as the new first shell -- and spawn the
+ * new shell's positions with the reference's own spawnNewShell. */
+void rotSunAndSpawnShell(Time_t t_sun_del) {
+  dropin_init();
+  azi_sun += (config.omegaSun * t_sun_del);
+  if (azi_sun > PI) azi_sun -= TWO_PI;
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    for (Index_t shell = OUTER_SHELL; shell > INNER_SHELL; shell--) {
+      Node_t *dst = &grid[s * LOCAL_NUM_SHELLS + shell];
+      const Neighbor_t n = dst->n, e = dst->e, w = dst->w, so = dst->s;
+      const Neighbor_t in = dst->streamIn, out = dst->streamOut;
+      *dst = *(dst - 1);
+      dst->n = n;
+      dst->e = e;
+      dst->w = w;
+      dst->s = so;
+      dst->streamIn = in;
+      dst->streamOut = out;
+    }
+  dropin_f_to_device();
+  dropin_check(eprem_gpu_ripple_f(dropin_run, eParts, (size_t)SSPEM), "rotSunAndSpawnShell");
+  dropin_f_stale = 1;
+  spawnNewShell();
+}
+
+/* The driver's output reads eParts: bring it up to date first. */
+void dataDumpIO(void) {
+  if (dropin_run) dropin_f_to_host();
+  dataDumpIO_cpu();
+}
+
+/* The driver sets eParts to the seed population: eParts is the current f
+ * from here on, the device's copy is taken again at its next use. */
+void initEnergeticParticles(void) {
+  initEnergeticParticles_cpu();
+  dropin_f_dev = 0;
+  dropin_f_stale = 0;
 }
 
 /* ---- MAS background --------------------------------------------------- */

@@ -42,6 +42,9 @@ EXPORTS = [
     ("eprem_gpu_host_alloc", C.c_void_p, [C.c_size_t]),
     ("eprem_gpu_host_free", None, [C.c_void_p]),
     ("eprem_gpu_host_register", C.c_int, [C.c_void_p, C.c_size_t]),
+    ("eprem_gpu_upload_f_pitched", C.c_int, [C.c_void_p, DP, C.c_size_t]),
+    ("eprem_gpu_download_f_pitched", C.c_int, [C.c_void_p, DP, C.c_size_t]),
+    ("eprem_gpu_ripple_f", C.c_int, [C.c_void_p, DP, C.c_size_t]),
     ("eprem_gpu_host_unregister", C.c_int, [C.c_void_p]),
     ("eprem_gpu_omni_flux", C.c_int, [C.c_void_p, DP]),
     ("eprem_gpu_omni_flux_static", C.c_int, [C.c_void_p, DP]),
@@ -229,6 +232,23 @@ class EpremRun:
         self._check(self.lib.eprem_gpu_update_energetic_particles_host(
             self.handle, f_in.ctypes.data_as(DP), f_out.ctypes.data_as(DP), stream_pitch, t_global))
         return f_out
+
+    def upload_f_pitched(self, f: np.ndarray, stream_pitch: int):
+        """Upload f whose stream s starts at element s * stream_pitch."""
+        assert f.dtype == np.float64 and f.flags["C_CONTIGUOUS"]
+        self._check(self.lib.eprem_gpu_upload_f_pitched(self.handle, f.ctypes.data_as(DP),
+                                                        stream_pitch))
+
+    def download_f_pitched(self, f: np.ndarray, stream_pitch: int):
+        assert f.dtype == np.float64 and f.flags["C_CONTIGUOUS"]
+        self._check(self.lib.eprem_gpu_download_f_pitched(self.handle, f.ctypes.data_as(DP),
+                                                          stream_pitch))
+
+    def ripple_f(self, tmpl: np.ndarray, stream_pitch: int = 0):
+        """rippleShellsOut for f: nodes move out by one, node 0 takes tmpl."""
+        assert tmpl.dtype == np.float64 and tmpl.flags["C_CONTIGUOUS"]
+        self._check(self.lib.eprem_gpu_ripple_f(self.handle, tmpl.ctypes.data_as(DP),
+                                                stream_pitch))
 
     def set_time_step(self, t_del: float):
         """A new config.tDel from the next call on, as SetDT

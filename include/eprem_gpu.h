@@ -224,6 +224,21 @@ int eprem_gpu_destroy(eprem_gpu_run *run);
 int eprem_gpu_upload_f(eprem_gpu_run *run, const double *f_host);
 int eprem_gpu_download_f(eprem_gpu_run *run, double *f_host);
 
+/* The same with stream s's N*E*M values at f + s * stream_pitch (0: N*E*M):
+ * the reference's eParts + SPEM with pitch SSPEM (src/global.h:61) directly,
+ * as the drop-in moves f only when the driver reads or writes it there. */
+int eprem_gpu_upload_f_pitched(eprem_gpu_run *run, const double *f_host, size_t stream_pitch);
+int eprem_gpu_download_f_pitched(eprem_gpu_run *run, double *f_host, size_t stream_pitch);
+
+/* rippleShellsOut (src/simCore.c:700-735) for f, on the device: node k of
+ * every stream takes node k-1's values (the outermost node's are dropped)
+ * and node 0 takes the stream's template row, E*M doubles at
+ * tmpl_host + s * stream_pitch (0: E*M) -- the reference's INNER_SHELL, so
+ * eParts with pitch SSPEM.  With it the drop-in keeps f on the device from
+ * step to step: rotSunAndSpawnShell (src/simCore.c:443-630) ripples it there
+ * instead of moving all of eParts on the host. */
+int eprem_gpu_ripple_f(eprem_gpu_run *run, const double *tmpl_host, size_t stream_pitch);
+
 /* nodes: EPREM_NODE_NFIELDS*S*N doubles, [field][stream*N+node]; only the
  * fields whose bit is set in field_mask are copied. */
 int eprem_gpu_upload_nodes(eprem_gpu_run *run, const double *nodes_host,

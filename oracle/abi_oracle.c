@@ -164,6 +164,36 @@ int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
   memcpy(f, r->f, n * sizeof(double));
   return EPREM_GPU_OK;
 }
+int eprem_gpu_upload_f_pitched(eprem_gpu_run *r, const double *f, size_t stream_pitch) {
+  const size_t per = (size_t)r->d.num_nodes * r->d.num_energies * r->d.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : per;
+  if (pitch < per) return abi_fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
+  for (int s = 0; s < r->d.num_streams; s++)
+    memcpy(r->f + (size_t)s * per, f + (size_t)s * pitch, per * sizeof(double));
+  return EPREM_GPU_OK;
+}
+int eprem_gpu_download_f_pitched(eprem_gpu_run *r, double *f, size_t stream_pitch) {
+  const size_t per = (size_t)r->d.num_nodes * r->d.num_energies * r->d.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : per;
+  if (pitch < per) return abi_fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
+  for (int s = 0; s < r->d.num_streams; s++)
+    memcpy(f + (size_t)s * pitch, r->f + (size_t)s * per, per * sizeof(double));
+  return EPREM_GPU_OK;
+}
+/* rippleShellsOut (src/simCore.c:700-735) for f held here */
+int eprem_gpu_ripple_f(eprem_gpu_run *r, const double *tmpl, size_t stream_pitch) {
+  const size_t em = (size_t)r->d.num_energies * r->d.num_mu;
+  const size_t pitch = stream_pitch ? stream_pitch : em;
+  const int N = r->d.num_nodes;
+  if (pitch < em) return abi_fail(EPREM_GPU_ERR_ARG, "stream_pitch below E*M");
+  for (int s = 0; s < r->d.num_streams; s++) {
+    double *p = r->f + (size_t)s * N * em;
+    memmove(p + em, p, (size_t)(N - 1) * em * sizeof(double));
+    memcpy(p, tmpl + (size_t)s * pitch, em * sizeof(double));
+  }
+  return EPREM_GPU_OK;
+}
+
 int eprem_gpu_upload_nodes(eprem_gpu_run *r, const double *nodes, uint64_t mask) {
   const size_t sn = (size_t)r->d.num_streams * r->d.num_nodes;
   for (int k = 0; k < EPREM_NODE_NFIELDS; k++)

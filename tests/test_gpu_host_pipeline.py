@@ -83,3 +83,40 @@ def test_host_update_with_a_stream_pitch(oracle_lib, precision):
     np.testing.assert_array_equal(view[:, ghost:].reshape(-1), f_ref)
     assert np.all(view[:, :ghost] == -7.0)
     assert st.as_dict() == st_ref.as_dict()
+
+
+def _as_stored(x, precision):
+    """Values as the run holds them (FP32: float rounding; 2^64 shift exact)."""
+    return x if precision == abi.EPREM_FP64 else x.astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+def test_pitched_f_round_trip_and_ripple(oracle_lib, precision):
+    """eParts-shaped host f (a template row before each stream's N rows):
+    pitched upload / download, and rippleShellsOut on the device -- node k
+    takes node k-1, node 0 the stream's template row -- twice in a row."""
+    w = W.custom(1, 2, 40, 6, 8, num_ep_steps=1)
+    d, g, f, nodes = primed_state(w, oracle_lib, precision)
+    S, N, E, M = d.num_streams, d.num_nodes, d.num_energies, d.num_mu
+    em = E * M
+    pitch = (N + 1) * em
+    eparts = np.empty(S * pitch)
+    view = eparts.reshape(S, N + 1, em)
+    view[:, 1:, :] = f.reshape(S, N, em)
+    rng = np.random.default_rng(3)
+    view[:, 0, :] = rng.uniform(1e-6, 1e-3, (S, em))  # INNER_SHELL template rows
+    run = EpremRun(d, w.params, g)
+    run.upload_f_pitched(eparts[em:], pitch)
+    back = np.full_like(eparts, -1.0)
+    run.download_f_pitched(back[em:], pitch)
+    np.testing.assert_array_equal(back.reshape(S, N + 1, em)[:, 1:, :],
+                                  _as_stored(view[:, 1:, :], precision))
+    assert np.all(back.reshape(S, N + 1, em)[:, 0, :] == -1.0)
+    expect = view[:, 1:, :].copy()
+    for _ in range(2):
+        run.ripple_f(eparts, pitch)
+        expect[:, 1:, :] = expect[:, :-1, :].copy()
+        expect[:, 0, :] = view[:, 0, :]
+    got = run.download_f().reshape(S, N, em)
+    run.close()
+    np.testing.assert_array_equal(got, _as_stored(expect, precision))
