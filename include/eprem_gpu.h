@@ -261,11 +261,12 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *run, double t_global);
 
 /* The same update with f in host memory: stream s's N*E*M values start at
  * f_in + s * stream_pitch (and f_out + s * stream_pitch); stream_pitch 0
- * means N*E*M (f stream-major and contiguous, as eprem_gpu_upload_f).  The
- * drop-in passes the reference's own array, eParts + SPEM with pitch SSPEM
- * (one ghost shell before each stream's shells, src/global.h:61,
- * src/global.c:112), so nothing is packed on the host.  f_in and f_out may be
- * the same array.  The streams go through in chunks (a short first and last
+ * means N*E*M (f stream-major and contiguous, as eprem_gpu_upload_f); the
+ * reference's own array is eParts + SPEM with pitch SSPEM (one INNER_SHELL
+ * row before each stream's shells, src/global.h:61, src/global.c:112), so a
+ * caller holding f there packs nothing on the host.  (The drop-in keeps f on
+ * the device across steps instead: eprem_gpu_ripple_f.)  f_in and f_out may
+ * be the same array.  The streams go through in chunks (a short first and last
  * one around six long ones), and each chunk's host-to-device copy, update
  * and device-to-host copy overlap the neighbouring chunks' work, so the
  * copies hide behind the update when the host memory is page-locked
