@@ -281,7 +281,7 @@ static int threads_for(int mmax) {
 
 // variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
 // 3 several list nodes per thread (stream2.cu), 4 the same with packed fp32x2
-// arithmetic (even cell counts per mu half), 5 as 4 with the cell guards
+// arithmetic (an odd mu half padded with a zero cell), 5 as 4 with the cell guards
 // resolved at compile time (M fills its bin, m0 = M/2).  The automatic FP32
 // choice is the first of 5, 4, 3 that fits.  The FP64 form always keeps the
 // coefficients in shared memory.

@@ -16,8 +16,8 @@
 //     last node for mu >= 0, lane 0's first node for mu < 0).
 // A CTA of T threads holds NPT*T >= 1024 nodes for mu bins up to 48, so a
 // 1000-node stream fits one CTA.  Two kernels: k_stream2, the scalar shape
-// (any M and split), and k_stream2_pairs, the packed fp32x2 shapes for even
-// halves, with f held as float2 pairs.
+// (any M and split), and k_stream2_pairs, the packed fp32x2 shapes, with f
+// held as float2 pairs (an odd half padded with a zero cell).
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -263,12 +263,16 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
 
 // The packed shapes: the upwind and relaxation arithmetic on pairs of mu
 // cells with the packed fp32x2 instructions (two cells per instruction, the
-// same roundings as the scalar fused multiply-adds of k_stream2), for even
-// halves (m0 and M - m0 even).  f is held as pairs (float2) from load to
-// store, so every pair sits in an aligned register pair.  FILLED: both halves
+// same roundings as the scalar fused multiply-adds of k_stream2).  f is held
+// as pairs (float2) from load to store, so every pair sits in an aligned
+// register pair.  FILLED: both halves
 // fill their MMAX/2 slots (M = MMAX, m0 = M/2), every cell guard is known at
 // compile time and rows move as float4 (MMAX is a multiple of 8: 16-byte
-// aligned rows); otherwise rows move as float2 under run-time guards.
+// aligned rows).  Otherwise rows move cell by cell under run-time guards,
+// and a half with an odd number of cells is padded at slot 0 with a cell
+// held at zero: its upwind value stays 0 (0 + c (0 - 0), the neighbours'
+// padding is zero too), it adds nothing to the isotropisation sum, and it is
+// zeroed again after the seed boundary and the relaxation set it.
 template <int MMAX, bool FILLED>
 __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(RunView r, int m0) {
   constexpr int T = Stream2Shape<MMAX>::T;
@@ -291,7 +295,8 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
   const int N = r.N;
   const int M = FILLED ? MMAX : r.M;
   if (FILLED) m0 = H;
-  const int nPL = FILLED ? P : m0 / 2, nPR = FILLED ? P : (M - m0) / 2;  // pairs per half
+  const int shL = FILLED ? 0 : (m0 & 1), shR = FILLED ? 0 : ((M - m0) & 1);  // padding
+  const int nPL = FILLED ? P : (m0 + shL) / 2, nPR = FILLED ? P : (M - m0 + shR) / 2;
   const int L = r.list_size[s];
   if (L < 3) return;
 
@@ -340,23 +345,28 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
           Rf[q][2 * t] = make_float2(b.x, b.y);
           Rf[q][2 * t + 1] = make_float2(b.z, b.w);
         }
-      } else {
-        const float2 *fp = reinterpret_cast<const float2 *>(row);
+      } else {  // slot j holds cell j - sh of its half
 #pragma unroll
         for (int t = 0; t < P; ++t) {
-          if (t < nPL) Lf[q][t] = fp[t];
-          if (t < nPR) Rf[q][t] = fp[m0 / 2 + t];
+          if (t < nPL) {
+            if (t > 0 || !shL) Lf[q][t].x = row[2 * t - shL];
+            Lf[q][t].y = row[2 * t + 1 - shL];
+          }
+          if (t < nPR) {
+            if (t > 0 || !shR) Rf[q][t].x = row[m0 + 2 * t - shR];
+            Rf[q][t].y = row[m0 + 2 * t + 1 - shR];
+          }
         }
       }
-      if (r.check_seed) {  // as (double)v < seed: no float between
+      if (r.check_seed) {  // as (double)v < seed: no float between; padding stays 0
 #pragma unroll
         for (int t = 0; t < P; ++t) {
           if (FILLED || t < nPL) {
-            Lf[q][t].x = Lf[q][t].x < seedf ? seedf : Lf[q][t].x;
+            if (t > 0 || !shL) Lf[q][t].x = Lf[q][t].x < seedf ? seedf : Lf[q][t].x;
             Lf[q][t].y = Lf[q][t].y < seedf ? seedf : Lf[q][t].y;
           }
           if (FILLED || t < nPR) {
-            Rf[q][t].x = Rf[q][t].x < seedf ? seedf : Rf[q][t].x;
+            if (t > 0 || !shR) Rf[q][t].x = Rf[q][t].x < seedf ? seedf : Rf[q][t].x;
             Rf[q][t].y = Rf[q][t].y < seedf ? seedf : Rf[q][t].y;
           }
         }
@@ -369,9 +379,10 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
       if (il < 3) s_bcv[il] = seedf;
     }
   }
-  const float dl0 = (float)(vdt * r.mugrid[0]);
-  const float dr0 = (float)(vdt * r.mugrid[m0 < M ? m0 : M - 1]);
+  // del of slot j: vdt mugrid(cell j - sh) = (first cell's del - sh ddel) + j ddel
   const float ddel = (float)(vdt * r.dmu);
+  const float dl0 = (float)(vdt * r.mugrid[0]) - (float)shL * ddel;
+  const float dr0 = (float)(vdt * r.mugrid[m0 < M ? m0 : M - 1]) - (float)shR * ddel;
   const float inv_m = (float)(1.0 / M);
   float *next_hi0 = (C > 1 && crank < C - 1) ? cluster.map_shared_rank(halo, crank + 1) : nullptr;
   float *prev_loW = (C > 1 && crank > 0) ? cluster.map_shared_rank(halo, crank - 1) : nullptr;
@@ -390,6 +401,8 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
           const float b = s_bcv[i0 + q];
 #pragma unroll
           for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(b, b);
+          if (shL) Lf[q][0].x = 0.f;  // padding
+          if (shR) Rf[q][0].x = 0.f;
         }
       }
     }
@@ -500,6 +513,13 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
         Rf[q][p] = __ffma2_rn(Rf[q][p], em[q], iso2);
       }
     }
+    if (!FILLED && (shL | shR)) {  // padding back to zero (uniform branch)
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        if (shL) Lf[q][0].x = 0.f;
+        if (shR) Rf[q][0].x = 0.f;
+      }
+    }
   }
 
 #pragma unroll
@@ -512,12 +532,14 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
       for (int p = 0; p < P; ++p) {
         float2 a = Lf[q][p], b = Rf[q][p];
         if (FILLED || p < nPL) {
-          if (bad_value(a.x, &code)) set_error(r, code, 1, s, k, e, 2 * p);
-          if (bad_value(a.y, &code)) set_error(r, code, 1, s, k, e, 2 * p + 1);
+          if ((p > 0 || !shL) && bad_value(a.x, &code))
+            set_error(r, code, 1, s, k, e, 2 * p - shL);
+          if (bad_value(a.y, &code)) set_error(r, code, 1, s, k, e, 2 * p + 1 - shL);
         }
         if (FILLED || p < nPR) {
-          if (bad_value(b.x, &code)) set_error(r, code, 1, s, k, e, m0 + 2 * p);
-          if (bad_value(b.y, &code)) set_error(r, code, 1, s, k, e, m0 + 2 * p + 1);
+          if ((p > 0 || !shR) && bad_value(b.x, &code))
+            set_error(r, code, 1, s, k, e, m0 + 2 * p - shR);
+          if (bad_value(b.y, &code)) set_error(r, code, 1, s, k, e, m0 + 2 * p + 1 - shR);
         }
         a.x = a.x < FLT_MIN ? FLT_MIN : a.x; a.y = a.y < FLT_MIN ? FLT_MIN : a.y;
         b.x = b.x < FLT_MIN ? FLT_MIN : b.x; b.y = b.y < FLT_MIN ? FLT_MIN : b.y;
@@ -538,11 +560,16 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
                                         Rf[q][2 * t + 1].y);
           }
         } else {
-          float2 *op = reinterpret_cast<float2 *>(row);
 #pragma unroll
           for (int t = 0; t < P; ++t) {
-            if (t < nPL) op[t] = Lf[q][t];
-            if (t < nPR) op[m0 / 2 + t] = Rf[q][t];
+            if (t < nPL) {
+              if (t > 0 || !shL) row[2 * t - shL] = Lf[q][t].x;
+              row[2 * t + 1 - shL] = Lf[q][t].y;
+            }
+            if (t < nPR) {
+              if (t > 0 || !shR) row[m0 + 2 * t - shR] = Rf[q][t].x;
+              row[m0 + 2 * t + 1 - shR] = Rf[q][t].y;
+            }
           }
         }
       }
@@ -615,7 +642,7 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *pla
   plan->reg_coef = 2;  // marks the several-nodes-per-thread kernel
   plan->packed = packed ? 1 : 0;
   plan->filled = 0;
-  if (packed && ((m0 & 1) || ((M - m0) & 1))) return EPREM_GPU_ERR_ARG;  // pairs of cells
+  // packed: odd halves take one padding cell (mmax/2 is even, so it fits)
   if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
   plan->filled = filled ? 1 : 0;
   plan->cluster = (N + npt * T - 1) / (npt * T);

@@ -85,3 +85,27 @@ def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
     for v, o in zip((1, 2, 4, 5), outs[:2] + outs[3:]):
         err = np.max(np.abs(o - outs[2]) / outs[2])
         assert err <= 1e-3, f"variant {v} vs variant 3: {err:.3e}"
+
+
+@pytest.mark.parametrize("mu", [6, 22, 23])
+def test_fp32_packed_shape_with_odd_halves(oracle_lib, mu):
+    """Odd numbers of cells per mu half (6: 3 + 3, 22: 11 + 11, 23: 11 + 12)
+    take the packed shape with a zero padding cell: the same update as the
+    scalar shape up to float rounding, and within 1e-3 of the FP64 oracle."""
+    w = W.custom(1, 1, 300, 4, mu, num_ep_steps=2)
+    d, g, f, nodes_arr = primed_state(w, oracle_lib)
+    f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes_arr)
+    outs = {}
+    for variant in (3, 4, 0):
+        w.params.stream_variant = variant
+        run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+        run.upload_f(f)
+        run.upload_nodes(nodes_arr)
+        run.update_energetic_particles(0.0)
+        run.read_stats()
+        outs[variant] = run.download_f()
+        run.close()
+    w.params.stream_variant = 0
+    np.testing.assert_array_equal(outs[0], outs[4])  # the automatic choice is the packed shape
+    assert np.max(np.abs(outs[4] - outs[3]) / outs[3]) <= 1e-4
+    assert np.max(np.abs(outs[4] - f_ref) / f_ref) <= 1e-3
