@@ -115,7 +115,8 @@ class EpStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "pad"}
 
 
-KERNEL_KINDS = ["geometry", "stream", "node", "seed_check", "mhd", "move", "flux", "convert"]
+KERNEL_KINDS = ["geometry", "stream", "node", "seed_check", "mhd", "move", "flux", "convert",
+                "shell"]
 
 
 class KernelTime(C.Structure):

@@ -17,14 +17,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libeprem_gpu.so")
-SOURCES = ["eprem_gpu.cu", "geometry.cu", "stream.cu", "node.cu", "mhd.cu", "peak.cu", "node32.cu", "mas.cu", "stream2.cu", "mlp.cu", "surrogate.cu", "ensemble.cu", "surrogate_host.cu"]
+SOURCES = ["eprem_gpu.cu", "geometry.cu", "stream.cu", "node.cu", "mhd.cu", "peak.cu", "node32.cu", "mas.cu", "stream2.cu", "mlp.cu", "surrogate.cu", "ensemble.cu", "surrogate_host.cu", "shell.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 # The background and node-motion kernels evaluate the reference's geometry
 # (acos(z / |r|), sqrt(|r|^2 - z^2)) without fused multiply-adds, as the
 # reference does: a contracted |r| can fall below |z| at the poles and turn
 # those into NaN.  They are a negligible share of a step.
-PER_FILE_FLAGS = {"mas.cu": ["-fmad=false"], "mhd.cu": ["-fmad=false"]}
+PER_FILE_FLAGS = {"mas.cu": ["-fmad=false"], "mhd.cu": ["-fmad=false"], "shell.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

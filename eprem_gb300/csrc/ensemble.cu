@@ -157,6 +157,8 @@ extern "C" int eprem_gpu_ensemble_create(eprem_gpu_run *const *runs, int n,
                   "ensemble steps use the analytic background; MAS runs step one by one");
     if (runs[i]->surr)
       return fail(EPREM_GPU_ERR_UNSUPPORTED, "surrogate-form runs step one by one");
+    if (runs[i]->shell_on)
+      return fail(EPREM_GPU_ERR_UNSUPPORTED, "runs with shell diffusion step one by one");
     for (int j = 0; j < i; j++)
       if (runs[j] == runs[i]) return fail(EPREM_GPU_ERR_ARG, "run listed twice in ensemble");
   }
@@ -302,6 +304,9 @@ extern "C" int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *e, int chains) 
 
 extern "C" int eprem_gpu_ensemble_step(eprem_gpu_ensemble *e) {
   if (!e) return fail(EPREM_GPU_ERR_ARG, "null ensemble");
+  for (eprem_gpu_run *r : e->runs)  // switched on after the ensemble was made
+    if (r->shell_on)
+      return fail(EPREM_GPU_ERR_UNSUPPORTED, "runs with shell diffusion step one by one");
   if (!e->exec) {
     const int rc = ensemble_capture(e);
     if (rc) return rc;

@@ -51,6 +51,7 @@ static const char *where_name(int w) {
     case 2: return "Adiabatic Focusing";
     case 3: return "Adiabatic Change";
     case 4: return "stream geometry";
+    case 6: return "DiffuseShellData";
     default: return "energetic-particle update";
   }
 }
@@ -296,6 +297,11 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
   cudaFree(r->d_flux);
   cudaFree(r->d_tmpl);
+  cudaFree(r->d_news);
+  cudaFree(r->d_shell_rowptr);
+  cudaFree(r->d_shell_ent);
+  cudaFree(r->d_shell_del);
+  cudaFree(r->d_shell_f);
   for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
   for (auto &slot : r->mas_allocs)
     for (void *p : slot) cudaFree(p);
@@ -521,6 +527,17 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
                [&] { return launch_node32_setup(v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "focusing/change set-up launch");
   }
+  // shell diffusion couples the streams: only a whole-run view reaches here
+  // with it on (the stream-range entries route around it)
+  const bool shell = r->shell_on && v.S == r->dims.num_streams;
+  if (r->shell_on && !shell) return fail(EPREM_GPU_ERR_UNSUPPORTED, "shell diffusion on a stream range");
+  if (shell) {
+    rc = timed(r, EPREM_KERNEL_SHELL, [&] {
+      return launch_shell_coef(v, r->d_news, r->kperxkpar, r->d_shell_del, r->stream,
+                               &r->launches);
+    });
+    if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion set-up launch");
+  }
   for (int step = 0; step < p.num_ep_steps; step++) {
     if (v.use_stream)
       rc = timed(r, EPREM_KERNEL_STREAM,
@@ -538,6 +555,14 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
                                : launch_node(v, r->nplan, r->stream, &r->launches);
       });
       if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
+    }
+    // DiffuseShellData after every stream's sub-step (src/energeticParticles.c:178-182)
+    if (shell) {
+      rc = timed(r, EPREM_KERNEL_SHELL, [&] {
+        return launch_shell_diffuse(v, r->d_shell_rowptr, r->d_shell_ent, r->d_shell_del,
+                                    r->d_shell_f, r->stream, &r->launches);
+      });
+      if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion launch");
     }
   }
   return EPREM_GPU_OK;
@@ -565,12 +590,11 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
   const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
   const size_t pitch = stream_pitch ? stream_pitch : per_stream;
   if (pitch < per_stream) return fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
-  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {  // those phases work on the whole run
-    if (pitch != per_stream)
-      return fail(EPREM_GPU_ERR_UNSUPPORTED, "split / surrogate node phases take contiguous f");
-    int rc = eprem_gpu_upload_f(r, f_in);
+  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE || r->shell_on) {
+    // those phases, and shell diffusion, work on the whole run
+    int rc = eprem_gpu_upload_f_pitched(r, f_in, pitch);
     if (!rc) rc = ep_update(r, r->v);
-    if (!rc) rc = eprem_gpu_download_f(r, f_out);
+    if (!rc) rc = eprem_gpu_download_f_pitched(r, f_out, pitch);
     return rc;
   }
   // Chunks: a short first and last one (1/32 of the streams each: the first
@@ -800,6 +824,51 @@ extern "C" int eprem_gpu_set_time_step(eprem_gpu_run *r, double t_del) {
   r->v.dt = t_del / (1.0 * r->params.num_ep_steps);  // src/energeticParticles.c:99
   r->v.dt_full = r->v.dt * r->params.num_ep_steps;
   r->mhd.t_del = t_del;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *news,
+                                             double kperxkpar) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (!news) {
+    r->shell_on = false;
+    return EPREM_GPU_OK;
+  }
+  const int S = r->dims.num_streams;
+  // configuration.c reads kperxkpar with a lower bound of VERYSMALL
+  if (!(kperxkpar >= kVerySmall) || !std::isfinite(kperxkpar))
+    return fail(EPREM_GPU_ERR_ARG, "kperxkpar must be finite and >= 1e-33");
+  for (int i = 0; i < 4 * S; i++)
+    if (news[i] < 0 || news[i] >= S) return fail(EPREM_GPU_ERR_ARG, "NEWS neighbour out of range");
+  // Per target stream, its incoming terms in the reference's order: source
+  // streams ascending and, per source, north, east, west, south, then the
+  // source's own loss (entry source * 8 + 4).
+  std::vector<std::vector<int>> lists(S);
+  for (int i = 0; i < S; i++) {
+    for (int d = 0; d < 4; d++) lists[news[i * 4 + d]].push_back(i * 8 + d);
+    lists[i].push_back(i * 8 + 4);
+  }
+  std::vector<int> rowptr(S + 1, 0), ent;
+  ent.reserve(5 * (size_t)S);
+  for (int j = 0; j < S; j++) {
+    ent.insert(ent.end(), lists[j].begin(), lists[j].end());
+    rowptr[j + 1] = (int)ent.size();
+  }
+  CK(cudaStreamSynchronize(r->stream));  // earlier launches may read the old lists
+  if (!r->d_news) {
+    const size_t elem = r->dims.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
+    CK(cudaMalloc(&r->d_news, sizeof(int) * 4 * (size_t)S));
+    CK(cudaMalloc(&r->d_shell_rowptr, sizeof(int) * (size_t)(S + 1)));
+    CK(cudaMalloc(&r->d_shell_ent, sizeof(int) * 5 * (size_t)S));
+    CK(cudaMalloc(&r->d_shell_del, sizeof(double) * 5 * r->sn() * r->dims.num_energies));
+    CK(cudaMalloc(&r->d_shell_f, elem * r->cells()));
+  }
+  CK(cudaMemcpy(r->d_news, news, sizeof(int) * 4 * (size_t)S, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(r->d_shell_rowptr, rowptr.data(), sizeof(int) * (size_t)(S + 1),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(r->d_shell_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice));
+  r->kperxkpar = kperxkpar;
+  r->shell_on = true;
   return EPREM_GPU_OK;
 }
 

@@ -64,6 +64,12 @@ int launch_seed_population(const RunView &r, unsigned long long seed, double per
 int launch_move_nodes(const RunView &r, double dt, cudaStream_t st, uint64_t *launches);
 int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *launches);
 int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint64_t *launches);
+
+// shell.cu -- cross-field (shell) diffusion (DiffuseShellData, ShellData)
+int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, double *del,
+                      cudaStream_t st, uint64_t *launches);
+int launch_shell_diffuse(const RunView &r, const int *rowptr, const int *ent, const double *del,
+                         void *scratch, cudaStream_t st, uint64_t *launches);
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
                      size_t count, cudaStream_t st, uint64_t *launches);
 

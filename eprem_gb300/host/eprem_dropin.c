@@ -132,8 +132,7 @@ static void dropin_init(void) {
   if (N_PROCS != 1) panic("GPU path: run with one MPI rank (every stream lives on the GPU)");
   if (config.masHelCouple > 0)
     panic("GPU path: heliospheric MAS coupling is not supported by this build");
-  if (config.useDrift > 0 || config.useShellDiffusion > 0)
-    panic("GPU path: drift and shell diffusion are not supported by this build");
+  if (config.useDrift > 0) panic("GPU path: drift is not supported by this build");
   eprem_dims_t d;
   d.num_streams = NUM_STREAMS;
   d.num_nodes = TOTAL_NUM_SHELLS;
@@ -240,6 +239,10 @@ static void dropin_unpack_nodes(uint64_t mask) {
    EPREM_NODE_MASK(EPREM_NODE_RZ) | EPREM_NODE_MASK(EPREM_NODE_RMAG) |                  \
    EPREM_NODE_MASK(EPREM_NODE_BMAG) | EPREM_NODE_MASK(EPREM_NODE_DLNB) |                \
    EPREM_NODE_MASK(EPREM_NODE_DLNN) | EPREM_NODE_MASK(EPREM_NODE_DUPAR))
+/* and, with shell diffusion, the direction of B (ShellData) */
+#define DROPIN_SHELL_IN                                                                  \
+  (EPREM_NODE_MASK(EPREM_NODE_BVEC_X) | EPREM_NODE_MASK(EPREM_NODE_BVEC_Y) |            \
+   EPREM_NODE_MASK(EPREM_NODE_BVEC_Z))
 #define DROPIN_EP_OUT                                                                    \
   (EPREM_NODE_MASK(EPREM_NODE_DS) | EPREM_NODE_MASK(EPREM_NODE_BMAG_PLUS) |             \
    EPREM_NODE_MASK(EPREM_NODE_BMAG_MINUS))
@@ -260,13 +263,42 @@ static void dropin_f_to_host(void) {
                "download f");
 }
 
+/* useShellDiffusion: hand the run the NEWS links gridStructInit gave every
+ * shell (initNEWS + initCopyAll, src/cubeShellInit.c:46-94) as stream
+ * indices.  The driver's first updateMhd comes before gridStructInit
+ * (src/eprem.c:470-480), so this waits for the first particle update.  The
+ * run forms ShellData's lengths itself at each update; the driver's own
+ * ShellData call (src/eprem.c:647-650) only fills host fields nothing here
+ * reads. */
+static int dropin_shell_ready = 0;
+static void dropin_shell_setup(void) {
+  if (dropin_shell_ready || config.useShellDiffusion <= 0) return;
+  int32_t *news = (int32_t *)malloc(sizeof(int32_t) * 4 * (size_t)NUM_STREAMS);
+  if (!news) panic("GPU path: allocation failed");
+  for (Index_t face = 0; face < NUM_FACES; face++)
+    for (Index_t row = 0; row < FACE_ROWS; row++)
+      for (Index_t col = 0; col < FACE_COLS; col++) {
+        const Node_t *nd = &grid[idx_frcs(face, row, col, INNER_ACTIVE_SHELL)];
+        const Neighbor_t *nb[4] = {&nd->n, &nd->e, &nd->w, &nd->s};
+        const size_t s = ((size_t)face * FACE_ROWS + row) * FACE_COLS + col;
+        for (int k = 0; k < 4; k++)
+          news[s * 4 + k] = (int32_t)((nb[k]->face * FACE_ROWS + nb[k]->row) * FACE_COLS + nb[k]->col);
+      }
+  dropin_check(eprem_gpu_set_shell_diffusion(dropin_run, news, config.kperxkpar),
+               "shell diffusion");
+  free(news);
+  dropin_shell_ready = 1;
+}
+
 void updateEnergeticParticles(void) {
   dropin_init();
   dropin_sync_step();
+  dropin_shell_setup();
   double t0 = MPI_Wtime();
   dropin_f_to_device();
-  dropin_pack_nodes(DROPIN_EP_IN);
-  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, DROPIN_EP_IN), "upload nodes");
+  const uint64_t in = DROPIN_EP_IN | (config.useShellDiffusion > 0 ? DROPIN_SHELL_IN : 0);
+  dropin_pack_nodes(in);
+  dropin_check(eprem_gpu_upload_nodes(dropin_run, dropin_nodes, in), "upload nodes");
   dropin_check(eprem_gpu_update_energetic_particles(dropin_run, t_global),
                "updateEnergeticParticles");
   dropin_f_stale = 1;

@@ -37,6 +37,8 @@ EXPORTS = [
     ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_set_time_step", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_set_shell_diffusion", C.c_int,
+     [C.c_void_p, C.POINTER(C.c_int32), C.c_double]),
     ("eprem_gpu_update_energetic_particles_host", C.c_int,
      [C.c_void_p, DP, DP, C.c_size_t, C.c_double]),
     ("eprem_gpu_host_alloc", C.c_void_p, [C.c_size_t]),
@@ -254,6 +256,19 @@ class EpremRun:
         """A new config.tDel from the next call on, as SetDT
         (src/simCore.c:800-880) sets it in MAS-coupled runs."""
         self._check(self.lib.eprem_gpu_set_time_step(self.handle, t_del))
+
+    def set_shell_diffusion(self, news, kperxkpar: float = 0.01):
+        """useShellDiffusion with config.kperxkpar: DiffuseShellData after
+        every sub-step.  news: num_streams x 4 stream indices of each
+        stream's north, east, west and south neighbour (None: off)."""
+        if news is None:
+            self._check(self.lib.eprem_gpu_set_shell_diffusion(self.handle, None, 0.0))
+            return
+        nw = np.ascontiguousarray(news, dtype=np.int32)
+        if nw.shape != (self.dims.num_streams, 4):
+            raise ValueError("news must be num_streams x 4")
+        self._check(self.lib.eprem_gpu_set_shell_diffusion(
+            self.handle, nw.ctypes.data_as(C.POINTER(C.c_int32)), kperxkpar))
 
     # -- MAS background ------------------------------------------------------
     def mas_init(self, mas_params: abi.MasParams):

@@ -200,6 +200,7 @@ enum eprem_kernel_kind {
   EPREM_KERNEL_MOVE,          /* moveNodes                                      */
   EPREM_KERNEL_FLUX,          /* omnidirectional flux                           */
   EPREM_KERNEL_CONVERT,       /* f format conversion (FP32 form)                */
+  EPREM_KERNEL_SHELL,         /* ShellData + DiffuseShellData                   */
   EPREM_KERNEL_NKINDS
 };
 typedef struct {
@@ -312,6 +313,24 @@ int eprem_gpu_move_nodes(eprem_gpu_run *run, double dt);
  * before the change keeps the step it captured (rebuild it).  t_del must be
  * finite and > 0. */
 int eprem_gpu_set_time_step(eprem_gpu_run *run, double t_del);
+
+/* Cross-field (shell) diffusion: config.useShellDiffusion = 1 with
+ * config.kperxkpar (src/configuration.c:77, :124).  Every later
+ * eprem_gpu_update_energetic_particles then runs DiffuseShellData
+ * (src/energeticParticles.c:419-554) after each sub-step's streaming,
+ * focusing and change of all streams (:178-182), with the perpendicular
+ * neighbour lengths of ShellData (:254-413) formed at the start of the call
+ * from the node positions and B, as the driver calls ShellData right before
+ * the update (src/eprem.c:647-671).  news: num_streams*4 stream indices
+ * (face*R*C + row*C + col) of each stream's north, east, west and south
+ * neighbour on its shell -- the Node_t links n, e, w, s of
+ * src/cubeShellStruct.h that initNEWS / initCopyAll set, the same on every
+ * shell; NULL switches the diffusion off.  Allocates the gather lists and an
+ * f-sized scratch on the first call.  The diffusion couples the streams, so
+ * eprem_gpu_update_energetic_particles_host then moves all of f in one copy
+ * each way instead of pipelining chunks, and ensembles refuse such runs.
+ * EPREM_GPU_ERR_ARG for a neighbour out of range or kperxkpar < 1e-33. */
+int eprem_gpu_set_shell_diffusion(eprem_gpu_run *run, const int32_t *news, double kperxkpar);
 
 /* Omnidirectional flux J = 2 E <f>_mu per (stream, node, energy), the
  * quantity computeFlux writes (src/unifiedOutput.c:153-180), without its

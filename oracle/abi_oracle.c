@@ -38,6 +38,8 @@ struct eprem_gpu_run {
   int mas_ready, mas_on;
   eprem_mas_slice_t slot[2];
   orc_mas_t mas;
+  int32_t *news; /* shell diffusion: NEWS links, NULL when off */
+  double kperxkpar;
 };
 
 static char abi_err[320] = "";
@@ -106,6 +108,10 @@ static void rec_call(const eprem_gpu_run *r, int kind, double arg) {
   rec_put(fp, "dlnp", 0, &r->g.dlnp, 1);
   rec_put(fp, "dmu", 0, &r->g.dmu, 1);
   if (kind == REC_EP) rec_put(fp, "f", 0, r->f, sn * E * M);
+  if (kind == REC_EP && r->news) {
+    rec_put(fp, "news", 2, r->news, 4 * (int64_t)d->num_streams);
+    rec_put(fp, "kperxkpar", 0, &r->kperxkpar, 1);
+  }
   rec_put(fp, "nodes", 0, r->nodes, sn * EPREM_NODE_NFIELDS);
   rec_put(fp, "mas_on", 2, &mas_on, 1);
   if (r->mas_ready) {
@@ -215,8 +221,11 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
   char err[256] = "";
   const char *env = getenv("EPREM_ORACLE_THREADS");
   const int nt = env ? atoi(env) : 1;
-  const int rc = orc_update_energetic_particles(&r->d, &r->p, &r->g, r->f, r->nodes, &r->stats,
-                                                nt > 0 ? nt : 1, err);
+  const int rc =
+      r->news ? orc_update_energetic_particles_news(&r->d, &r->p, &r->g, r->f, r->nodes, r->news,
+                                                    r->kperxkpar, &r->stats, nt > 0 ? nt : 1, err)
+              : orc_update_energetic_particles(&r->d, &r->p, &r->g, r->f, r->nodes, &r->stats,
+                                               nt > 0 ? nt : 1, err);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, err);
 }
 void *eprem_gpu_host_alloc(size_t bytes) { return malloc(bytes ? bytes : 1); }
@@ -244,6 +253,18 @@ int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const double *f_
     for (int s = 0; s < r->d.num_streams; s++)
       memcpy(f_out + (size_t)s * pitch, r->f + (size_t)s * per, per * sizeof(double));
   return rc;
+}
+
+int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *news, double kperxkpar) {
+  free(r->news);
+  r->news = NULL;
+  if (!news) return EPREM_GPU_OK;
+  if (!(kperxkpar >= 1.0e-33)) return abi_fail(EPREM_GPU_ERR_ARG, "kperxkpar below 1e-33");
+  const size_t n = 4 * (size_t)r->d.num_streams;
+  r->news = (int32_t *)malloc(n * sizeof(int32_t));
+  memcpy(r->news, news, n * sizeof(int32_t));
+  r->kperxkpar = kperxkpar;
+  return EPREM_GPU_OK;
 }
 
 int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *s) {

@@ -159,6 +159,7 @@ typedef struct {
   const eprem_grids_t *g;
   double *f, *nodes;
   int s0, s1;
+  int step0, step1;  /* sub-steps [step0, step1) of the call */
   eprem_ep_stats_t stats;
   int status;
   char err[256];
@@ -786,10 +787,11 @@ static void orc_work_free(orc_work_t *w) {
 }
 
 /* updateEnergeticParticles (src/energeticParticles.c:70-203) for the streams
- * of one job.  The reference loops sub-steps outermost and, inside each,
- * streams all streams before focusing/changing them; the streams share no
- * data, so running each stream's sub-steps back to back gives the same
- * values. */
+ * of one job, sub-steps [step0, step1).  The reference loops sub-steps
+ * outermost and, inside each, streams all streams before focusing/changing
+ * them; without shell diffusion the streams share no data, so running each
+ * stream's sub-steps back to back gives the same values.  With it, the caller
+ * runs one sub-step at a time and diffuses across streams in between. */
 static void *orc_job_run(void *arg) {
   orc_job_t *job = (orc_job_t *)arg;
   const eprem_dims_t *d = job->d;
@@ -802,7 +804,7 @@ static void *orc_job_run(void *arg) {
   orc_work_alloc(&w, N, E, d->num_mu);
   double dt = p->t_del / (1.0 * p->num_ep_steps);
   for (int s = job->s0; s < job->s1 && job->status == EPREM_GPU_OK; s++) {
-    for (int step = 0; step < p->num_ep_steps; step++) {
+    for (int step = job->step0; step < job->step1; step++) {
       orc_stream_values(job, s);
       if (p->check_seed_population > 0) orc_seed_check(job, s);
       if (p->use_parallel_diffusion > 0) {
@@ -848,16 +850,107 @@ static int orc_validate(const eprem_dims_t *d, const eprem_params_t *p, char *er
   return EPREM_GPU_OK;
 }
 
-int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_params_t *p,
-                                         const eprem_grids_t *g, double *f, double *nodes,
-                                         int s0, int s1, eprem_ep_stats_t *stats, int nthreads,
-                                         char *errbuf) {
+/* ShellData (src/energeticParticles.c:254-413): per node and NEWS neighbour,
+ * the distance dl to the neighbour's node on the same shell and its part
+ * perpendicular to B, dl * sqrt(1 - (e_n . e_B)^2).  dlper: [S][N][4] in the
+ * order north, east, west, south. */
+static void orc_shell_lengths(const eprem_dims_t *d, const eprem_params_t *p,
+                              const double *nodes, const int32_t *news, double *dlper) {
+  const int S = d->num_streams, N = d->num_nodes;
+  const size_t SN = (size_t)S * N;
+  const double rs = p->r_scale;
+  for (int s = 0; s < S; s++)
+    for (int k = 0; k < N; k++) {
+      double rx = NODE(EPREM_NODE_RX, s, k) * rs, ry = NODE(EPREM_NODE_RY, s, k) * rs,
+             rz = NODE(EPREM_NODE_RZ, s, k) * rs;
+      double bmag = NODE(EPREM_NODE_BMAG, s, k);
+      double ebx = NODE(EPREM_NODE_BVEC_X, s, k) / bmag, eby = NODE(EPREM_NODE_BVEC_Y, s, k) / bmag,
+             ebz = NODE(EPREM_NODE_BVEC_Z, s, k) / bmag;
+      for (int dir = 0; dir < 4; dir++) {
+        const int o = news[s * 4 + dir];
+        double ex = NODE(EPREM_NODE_RX, o, k) * rs - rx, ey = NODE(EPREM_NODE_RY, o, k) * rs - ry,
+               ez = NODE(EPREM_NODE_RZ, o, k) * rs - rz;
+        double dl = sqrt(ex * ex + ey * ey + ez * ez);
+        ex /= dl;
+        ey /= dl;
+        ez /= dl;
+        double dot = ex * ebx + ey * eby + ez * ebz;
+        dlper[((size_t)s * N + k) * 4 + dir] = dl * sqrt(1.0 - dot * dot);
+      }
+    }
+}
+
+/* DiffuseShellData (src/energeticParticles.c:419-554), one sub-step of
+ * length dt over all streams, nodes 1..N-1 (shells innerComputeShell on):
+ * per node and energy, each stream hands delta = min(dt kper / dlPer^2,
+ * 0.025) of its f to each NEWS neighbour, kper = dt * 0.33333333 * mfp * v
+ * * kperxkpar as the reference writes it; all deltas of one node and energy
+ * are summed (in the reference's order: source streams ascending, north,
+ * east, west, south, then the source's own loss) before f changes. */
+static int orc_shell_diffuse(const eprem_dims_t *d, const eprem_params_t *p,
+                             const eprem_grids_t *g, double *f, const double *nodes,
+                             const int32_t *news, double kperxkpar, const double *dlper,
+                             double dt, char *errbuf) {
+  const int S = d->num_streams, N = d->num_nodes, E = d->num_energies, M = d->num_mu;
+  const size_t SN = (size_t)S * N;
+  const double thresh = 0.025, verysmall = 1.0e-33;
+  double *delta = (double *)malloc(sizeof(double) * (size_t)S * M);
+  int rc = EPREM_GPU_OK;
+  for (int k = 1; k < N && !rc; k++)
+    for (int e = 0; e < E && !rc; e++) {
+      for (size_t i = 0; i < (size_t)S * M; i++) delta[i] = 0.0;
+      for (int s = 0; s < S; s++) {
+        double mfp = orc_mfp(p, g, e, NODE(EPREM_NODE_RMAG, s, k), NODE(EPREM_NODE_BMAG, s, k));
+        double dt_kper = dt * 0.33333333 * mfp * g->vgrid[e] * kperxkpar;
+        double del[4];
+        for (int dir = 0; dir < 4; dir++) {
+          double l = dlper[((size_t)s * N + k) * 4 + dir];
+          del[dir] = dt_kper / (l * l + verysmall);
+          if (del[dir] > thresh) del[dir] = thresh;
+        }
+        const double *fs = &f[FIDX(s, k, e, 0)];
+        for (int m = 0; m < M; m++) {
+          for (int dir = 0; dir < 4; dir++) delta[(size_t)news[s * 4 + dir] * M + m] += del[dir] * fs[m];
+          delta[(size_t)s * M + m] -= (del[0] + del[1] + del[2] + del[3]) * fs[m];
+        }
+      }
+      for (int s = 0; s < S && !rc; s++)
+        for (int m = 0; m < M; m++) {
+          double v = f[FIDX(s, k, e, m)] += delta[(size_t)s * M + m];
+          if (isnan(v) || isinf(v)) {
+            rc = isnan(v) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF;
+            if (errbuf)
+              snprintf(errbuf, 256, "%s in DiffuseShellData (stream %d, node %d)",
+                       isnan(v) ? "NaN value" : "Inf value", s, k);
+            break;
+          }
+        }
+    }
+  free(delta);
+  return rc;
+}
+
+static int orc_update_core(const eprem_dims_t *d, const eprem_params_t *p, const eprem_grids_t *g,
+                           double *f, double *nodes, int s0, int s1, const int32_t *news,
+                           double kperxkpar, eprem_ep_stats_t *stats, int nthreads,
+                           char *errbuf) {
   int rc = orc_validate(d, p, errbuf);
   if (rc) return rc;
   if (s0 < 0) s0 = 0;
   if (s1 > d->num_streams) s1 = d->num_streams;
   int ns = s1 - s0;
   if (ns <= 0) return EPREM_GPU_OK;
+  if (news) {
+    if (ns != d->num_streams) {
+      if (errbuf) snprintf(errbuf, 256, "shell diffusion couples all streams: no stream range");
+      return EPREM_GPU_ERR_ARG;
+    }
+    for (int i = 0; i < 4 * d->num_streams; i++)
+      if (news[i] < 0 || news[i] >= d->num_streams) {
+        if (errbuf) snprintf(errbuf, 256, "NEWS neighbour out of range");
+        return EPREM_GPU_ERR_ARG;
+      }
+  }
   if (nthreads < 1) nthreads = 1;
   if (nthreads > ns) nthreads = ns;
   orc_job_t *jobs = (orc_job_t *)calloc(nthreads, sizeof(orc_job_t));
@@ -869,12 +962,35 @@ int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_para
     jobs[t].stats.min_tau = DBL_MAX;
     jobs[t].status = EPREM_GPU_OK;
   }
-  if (nthreads == 1) {
-    orc_job_run(&jobs[0]);
-  } else {
-    for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, orc_job_run, &jobs[t]);
-    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  /* Without shell diffusion one pass runs every sub-step; with it, one pass
+   * per sub-step, each followed by the diffusion over all streams. */
+  const int passes = news ? p->num_ep_steps : 1;
+  double *dlper = NULL;
+  if (news) {
+    dlper = (double *)malloc(sizeof(double) * 4 * (size_t)d->num_streams * d->num_nodes);
+    orc_shell_lengths(d, p, nodes, news, dlper);
   }
+  const double dt = p->t_del / (1.0 * p->num_ep_steps);
+  int diff_rc = EPREM_GPU_OK;
+  char diff_err[256] = "";
+  for (int pass = 0; pass < passes && !diff_rc; pass++) {
+    for (int t = 0; t < nthreads; t++) {
+      jobs[t].step0 = news ? pass : 0;
+      jobs[t].step1 = news ? pass + 1 : p->num_ep_steps;
+    }
+    if (nthreads == 1) {
+      orc_job_run(&jobs[0]);
+    } else {
+      for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, orc_job_run, &jobs[t]);
+      for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    }
+    int failed = 0;
+    for (int t = 0; t < nthreads; t++) failed |= jobs[t].status != EPREM_GPU_OK;
+    if (failed) break;
+    if (news)
+      diff_rc = orc_shell_diffuse(d, p, g, f, nodes, news, kperxkpar, dlper, dt, diff_err);
+  }
+  free(dlper);
   rc = EPREM_GPU_OK;
   for (int t = 0; t < nthreads; t++) {
     eprem_ep_stats_t *js = &jobs[t].stats;
@@ -893,9 +1009,28 @@ int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_para
       if (errbuf) snprintf(errbuf, 256, "%s", jobs[t].err);
     }
   }
+  if (rc == EPREM_GPU_OK && diff_rc != EPREM_GPU_OK) {
+    rc = diff_rc;
+    if (errbuf) snprintf(errbuf, 256, "%s", diff_err);
+  }
   free(jobs);
   free(th);
   return rc;
+}
+
+int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_params_t *p,
+                                         const eprem_grids_t *g, double *f, double *nodes,
+                                         int s0, int s1, eprem_ep_stats_t *stats, int nthreads,
+                                         char *errbuf) {
+  return orc_update_core(d, p, g, f, nodes, s0, s1, NULL, 0.0, stats, nthreads, errbuf);
+}
+
+int orc_update_energetic_particles_news(const eprem_dims_t *d, const eprem_params_t *p,
+                                        const eprem_grids_t *g, double *f, double *nodes,
+                                        const int32_t *news, double kperxkpar,
+                                        eprem_ep_stats_t *stats, int nthreads, char *errbuf) {
+  return orc_update_core(d, p, g, f, nodes, 0, d->num_streams, news, kperxkpar, stats, nthreads,
+                         errbuf);
 }
 
 int orc_update_energetic_particles(const eprem_dims_t *d, const eprem_params_t *p,

@@ -57,6 +57,22 @@ int orc_update_energetic_particles_range(const eprem_dims_t *d,
                                          eprem_ep_stats_t *stats, int nthreads,
                                          char *errbuf);
 
+/* updateEnergeticParticles with useShellDiffusion on: after each sub-step's
+ * streaming, focusing and change of all streams, DiffuseShellData
+ * (src/energeticParticles.c:419-554) couples the streams of every shell,
+ * with the perpendicular neighbour lengths of ShellData (:254-413) formed
+ * from the node positions and B at the start of the call, as the driver
+ * calls ShellData right before updateEnergeticParticles (src/eprem.c:647-671).
+ * news: S*4 stream indices (face*R*C + row*C + col) of each stream's north,
+ * east, west and south neighbour -- the Node_t links n, e, w, s
+ * (src/cubeShellStruct.h), the same on every shell.  kperxkpar:
+ * config.kperxkpar. */
+int orc_update_energetic_particles_news(const eprem_dims_t *d, const eprem_params_t *p,
+                                        const eprem_grids_t *g, double *f, double *nodes,
+                                        const int32_t *news, double kperxkpar,
+                                        eprem_ep_stats_t *stats, int nthreads,
+                                        char *errbuf);
+
 /* updateMhd for the analytic background (src/flow.c:36-154). */
 int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p,
                    double *nodes, double t_global);

@@ -48,6 +48,10 @@ class Oracle:
             C.POINTER(abi.Dims), C.POINTER(abi.Params), C.POINTER(abi.Grids), DP, DP, C.c_int,
             C.c_int, C.POINTER(abi.EpStats), C.c_int, C.c_char_p]
         lib.orc_update_energetic_particles_range.restype = C.c_int
+        lib.orc_update_energetic_particles_news.argtypes = [
+            C.POINTER(abi.Dims), C.POINTER(abi.Params), C.POINTER(abi.Grids), DP, DP,
+            C.POINTER(C.c_int32), C.c_double, C.POINTER(abi.EpStats), C.c_int, C.c_char_p]
+        lib.orc_update_energetic_particles_news.restype = C.c_int
         lib.orc_update_mhd.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
         lib.orc_move_nodes.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
         lib.orc_omni_flux.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Grids), DP, DP]
@@ -80,10 +84,19 @@ class Oracle:
         return out
 
     def update_energetic_particles(self, dims, params, grids_s, f, nodes, nthreads=1,
-                                   streams=None):
+                                   streams=None, news=None, kperxkpar=0.01):
+        """news: S x 4 NEWS neighbour stream indices to diffuse across shells
+        (DiffuseShellData) after every sub-step; None leaves it off."""
         st = abi.EpStats()
         st.min_tau = np.finfo(np.float64).max
         err = C.create_string_buffer(256)
+        if news is not None:
+            nw = np.ascontiguousarray(news, dtype=np.int32)
+            assert streams is None and nw.shape == (dims.num_streams, 4)
+            rc = self.lib.orc_update_energetic_particles_news(
+                C.byref(dims), C.byref(params), C.byref(grids_s), _dp(f), _dp(nodes),
+                nw.ctypes.data_as(C.POINTER(C.c_int32)), kperxkpar, C.byref(st), nthreads, err)
+            return rc, st, err.value.decode()
         s0, s1 = (0, dims.num_streams) if streams is None else streams
         rc = self.lib.orc_update_energetic_particles_range(
             C.byref(dims), C.byref(params), C.byref(grids_s), _dp(f), _dp(nodes), s0, s1,
@@ -136,7 +149,15 @@ class Reference:
         lib.ref_mas_setup.argtypes = [C.POINTER(abi.MasParams), C.POINTER(abi.MasSlice),
                                       C.POINTER(abi.MasSlice), C.c_double, C.c_double]
         lib.ref_mas_move_nodes.argtypes = [C.c_double]
+        lib.ref_shell_diffusion.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_int32)]
         self.lib = lib
+
+    def shell_diffusion(self, kperxkpar, num_streams):
+        """Switch on DiffuseShellData; returns the reference's NEWS links
+        (num_streams x 4 stream indices: north, east, west, south)."""
+        news = np.zeros((num_streams, 4), dtype=np.int32)
+        self.lib.ref_shell_diffusion(1, kperxkpar, news.ctypes.data_as(C.POINTER(C.c_int32)))
+        return news
 
     def mas_setup(self, mp, s0, s1, s_cor, phi_offset):
         self._mas_keep = (mp, s0, s1)

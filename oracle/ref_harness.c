@@ -27,6 +27,7 @@
 
 #include "baseTypes.h"
 #include "configuration.h"
+#include "cubeShellInit.h"
 #include "cubeShellStruct.h"
 #include "energeticParticles.h"
 #include "energeticParticlesInit.h"
@@ -253,7 +254,29 @@ int ref_store(double *f, double *nodes) {
   return 0;
 }
 
-/* The reference entry points.  A panic inside returns its MPI_Abort code. */
+/* Switch useShellDiffusion on (on = 1) with config.kperxkpar: the grid gets
+ * the reference's own NEWS links (initNEWS on the inner shell, then
+ * initCopyAll to every shell, as gridStructInit does, src/cubeShellInit.c:
+ * 46-94), returned in news as stream indices face*R*C + row*C + col, four per
+ * stream in the order north, east, west, south.  initCopyAll also places the
+ * nodes on the unit sphere; ref_load sets them afterwards. */
+int ref_shell_diffusion(int on, double kperxkpar, int32_t *news) {
+  initNEWS(INNER_SHELL);
+  initCopyAll();
+  for (int s = 0; s < ref_S; s++) {
+    const Node_t *n = &grid[(size_t)s * LOCAL_NUM_SHELLS + INNER_ACTIVE_SHELL];
+    const Neighbor_t *nb[4] = {&n->n, &n->e, &n->w, &n->s};
+    for (int d = 0; d < 4; d++)
+      news[s * 4 + d] = (int32_t)((nb[d]->face * FACE_ROWS + nb[d]->row) * FACE_COLS + nb[d]->col);
+  }
+  config.useShellDiffusion = on;
+  config.kperxkpar = kperxkpar;
+  return 0;
+}
+
+/* The reference entry points.  A panic inside returns its MPI_Abort code.
+ * With useShellDiffusion on, ShellData runs first, as the driver calls it
+ * right before updateEnergeticParticles (src/eprem.c:647-671). */
 int ref_update_energetic_particles(double tg, eprem_ep_stats_t *st) {
   t_global = tg;
   maxsubcycles_energychange = 0;
@@ -262,7 +285,10 @@ int ref_update_energetic_particles(double tg, eprem_ep_stats_t *st) {
   refshim_abort_hook = ref_abort;
   ref_abort_armed = 1;
   int code = setjmp(ref_abort_jmp);
-  if (code == 0) updateEnergeticParticles();
+  if (code == 0) {
+    if (config.useShellDiffusion > 0) ShellData();
+    updateEnergeticParticles();
+  }
   ref_abort_armed = 0;
   st->max_subcycles_change = maxsubcycles_energychange;
   st->max_subcycles_focusing = maxsubcycles_focusing;
