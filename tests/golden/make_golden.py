@@ -8,7 +8,7 @@ updateEnergeticParticles advances f.  Inputs and outputs are stored so the
 tests can check the oracle against the reference where the reference tree is
 absent.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
 (needs /root/reference; each case runs in a fresh process because the
 reference allocates its globals once per process).
 """
@@ -36,7 +36,16 @@ def cases():
                                            adiabatic_change_alg=2, mfp_type=2, damp_cooling=0.4),
         "seed_only": W.custom(1, 1, 16, 8, 6, num_ep_steps=2, use_parallel_diffusion=0,
                               use_adiabatic_focus=0, use_adiabatic_change=0),
+        # shell diffusion (DiffuseShellData) on the reference's own NEWS links:
+        # a weak coupling and one strong enough that most hand-overs hit the
+        # 0.025 cap
+        "shell_2x2_weak": W.custom(2, 2, 16, 8, 6, num_ep_steps=3),
+        "shell_3x2_capped": W.custom(3, 2, 12, 6, 6, num_ep_steps=2),
     }
+
+
+# kperxkpar of the shell-diffusion cases
+SHELL = {"shell_2x2_weak": 0.01, "shell_3x2_capped": 50.0}
 
 
 def run_case(name, q):
@@ -45,6 +54,10 @@ def run_case(name, q):
     w = cases()[name]
     ref = O.Reference()
     g = ref.setup(w)
+    extra = {}
+    if name in SHELL:  # before ref.load: the NEWS set-up also places nodes
+        extra = dict(news=ref.shell_diffusion(SHELL[name], w.dims().num_streams),
+                     kperxkpar=np.array([SHELL[name]]))
     nodes0 = W.initial_nodes(w)
     f0 = np.zeros(w.cells)
     ref.load(f0, nodes0)
@@ -65,12 +78,12 @@ def run_case(name, q):
                dims=np.frombuffer(bytes(w.dims()), dtype=np.uint8),
                params=np.frombuffer(bytes(w.params), dtype=np.uint8),
                grids=np.concatenate([g["egrid"], g["vgrid"], g["vgrid_i"], g["rigidity"],
-                                     g["mugrid"], [g["dlnp"], g["dmu"]]])))
+                                     g["mugrid"], [g["dlnp"], g["dmu"]]]), **extra))
 
 
-def main():
+def main(names=None):
     ctx = mp.get_context("spawn")
-    for name in cases():
+    for name in names or cases():
         q = ctx.Queue()
         p = ctx.Process(target=run_case, args=(name, q))
         p.start()
@@ -84,4 +97,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -30,7 +30,8 @@ def load(path):
 
 
 def test_golden_files_present():
-    assert len(FILES) >= 5
+    assert len(FILES) >= 7
+    assert sum("news" in np.load(f) for f in FILES) >= 2  # shell-diffusion cases
 
 
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f) for f in FILES])
@@ -40,7 +41,8 @@ def test_oracle_update_matches_reference_outputs(path, oracle_lib):
     gs, keep = W.grids_struct(g)
     f = z["f_in"].copy()
     nodes = z["nodes_in"].copy()
-    rc, st, err = oracle_lib.update_energetic_particles(dims, params, gs, f, nodes)
+    shell = {"news": z["news"], "kperxkpar": float(z["kperxkpar"][0])} if "news" in z else {}
+    rc, st, err = oracle_lib.update_energetic_particles(dims, params, gs, f, nodes, **shell)
     assert rc == 0, err
     ref = z["f_out"]
     assert np.max(np.abs(f - ref) / np.abs(ref)) <= 1e-13

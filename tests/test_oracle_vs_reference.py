@@ -25,13 +25,20 @@ CASES = {
     "mfpB_damped_noseedcheck": lambda: W.custom(1, 1, 30, 10, 8, num_ep_steps=3, mfp_type=2,
                                                 damp_cooling=0.4, check_seed_population=0),
     "no_boundary_odd_mu": lambda: W.custom(1, 1, 30, 9, 7, num_ep_steps=3, use_ep_boundary=0),
+    # shell diffusion (DiffuseShellData) on the reference's own NEWS links
+    "shell_1x1_faces": lambda: W.custom(1, 1, 20, 8, 6, num_ep_steps=2),
+    "shell_2x2_faces": lambda: W.custom(2, 2, 24, 10, 8, num_ep_steps=3),
+    "shell_3x2_capped_alg3": lambda: W.custom(3, 2, 16, 6, 6, num_ep_steps=2,
+                                              adiabatic_focus_alg=3, adiabatic_change_alg=3),
 }
+SHELL = {"shell_1x1_faces": 0.5, "shell_2x2_faces": 0.05, "shell_3x2_capped_alg3": 50.0}
 
 
 def _reference_run(name, q):
     w = CASES[name]()
     ref = O.Reference()
     g = ref.setup(w)
+    news = ref.shell_diffusion(SHELL[name], w.dims().num_streams) if name in SHELL else None
     nodes0 = W.initial_nodes(w)
     f0 = np.zeros(w.cells)
     ref.load(f0, nodes0)
@@ -49,7 +56,7 @@ def _reference_run(name, q):
     f_out = np.zeros_like(f_in)
     nodes_out = np.zeros_like(nodes_in)
     ref.store(f_out, nodes_out)
-    q.put((g, nodes0, nodes_in, f_in, f_out, nodes_out, outs))
+    q.put((g, nodes0, nodes_in, f_in, f_out, nodes_out, outs, news))
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -58,7 +65,7 @@ def test_oracle_bit_exact_with_reference(name, oracle_lib):
     q = ctx.Queue()
     p = ctx.Process(target=_reference_run, args=(name, q))
     p.start()
-    g_ref, nodes0, nodes_in_ref, f_in, f_out_ref, nodes_out_ref, outs = q.get(timeout=300)
+    g_ref, nodes0, nodes_in_ref, f_in, f_out_ref, nodes_out_ref, outs, news = q.get(timeout=300)
     p.join()
     w = CASES[name]()
     g = oracle_lib.grids(w.num_energies, w.num_mu, w.e_min, w.e_max, w.mass, w.charge,
@@ -74,7 +81,8 @@ def test_oracle_bit_exact_with_reference(name, oracle_lib):
     gs, keep = W.grids_struct(g)
     f = f_in.copy()
     for call in range(2):
-        rc, st, err = oracle_lib.update_energetic_particles(d, w.params, gs, f, nodes)
+        shell = {} if news is None else {"news": news, "kperxkpar": SHELL[name]}
+        rc, st, err = oracle_lib.update_energetic_particles(d, w.params, gs, f, nodes, **shell)
         assert rc == outs[call][0] == 0, err
         assert (st.max_subcycles_change, st.max_subcycles_focusing) == outs[call][1:3]
         assert st.min_tau == outs[call][3]
