@@ -298,7 +298,6 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_flux);
   cudaFree(r->d_tmpl);
   cudaFree(r->d_news);
-  cudaFree(r->d_shell_rowptr);
   cudaFree(r->d_shell_ent);
   cudaFree(r->d_shell_del);
   cudaFree(r->d_shell_f);
@@ -529,7 +528,8 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
   }
   // shell diffusion couples the streams: only a whole-run view reaches here
   // with it on (the stream-range entries route around it)
-  const bool shell = r->shell_on && v.S == r->dims.num_streams;
+  // (each step swaps the run's two f buffers, which v, the run's own view, sees)
+  const bool shell = r->shell_on && &v == &r->v;
   if (r->shell_on && !shell) return fail(EPREM_GPU_ERR_UNSUPPORTED, "shell diffusion on a stream range");
   if (shell) {
     rc = timed(r, EPREM_KERNEL_SHELL, [&] {
@@ -559,10 +559,12 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
     // DiffuseShellData after every stream's sub-step (src/energeticParticles.c:178-182)
     if (shell) {
       rc = timed(r, EPREM_KERNEL_SHELL, [&] {
-        return launch_shell_diffuse(v, r->d_shell_rowptr, r->d_shell_ent, r->d_shell_del,
-                                    r->d_shell_f, r->stream, &r->launches);
+        return launch_shell_diffuse(v, r->d_shell_ent, r->shell_L, r->d_shell_del, r->d_shell_f,
+                                    r->stream, &r->launches);
       });
       if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion launch");
+      std::swap(r->d_f, r->d_shell_f);  // the new f is the other buffer
+      r->v.f = r->d_f;
     }
   }
   return EPREM_GPU_OK;
@@ -842,31 +844,30 @@ extern "C" int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *ne
     if (news[i] < 0 || news[i] >= S) return fail(EPREM_GPU_ERR_ARG, "NEWS neighbour out of range");
   // Per target stream, its incoming terms in the reference's order: source
   // streams ascending and, per source, north, east, west, south, then the
-  // source's own loss (entry source * 8 + 4).
+  // source's own loss (entry source * 8 + 4); rows padded to the longest.
   std::vector<std::vector<int>> lists(S);
   for (int i = 0; i < S; i++) {
     for (int d = 0; d < 4; d++) lists[news[i * 4 + d]].push_back(i * 8 + d);
     lists[i].push_back(i * 8 + 4);
   }
-  std::vector<int> rowptr(S + 1, 0), ent;
-  ent.reserve(5 * (size_t)S);
-  for (int j = 0; j < S; j++) {
-    ent.insert(ent.end(), lists[j].begin(), lists[j].end());
-    rowptr[j + 1] = (int)ent.size();
-  }
+  size_t L = 0;
+  for (const auto &l : lists) L = std::max(L, l.size());
+  std::vector<int> ent(L * S, -1);
+  for (int j = 0; j < S; j++) std::copy(lists[j].begin(), lists[j].end(), ent.begin() + j * L);
   CK(cudaStreamSynchronize(r->stream));  // earlier launches may read the old lists
   if (!r->d_news) {
     const size_t elem = r->dims.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
     CK(cudaMalloc(&r->d_news, sizeof(int) * 4 * (size_t)S));
-    CK(cudaMalloc(&r->d_shell_rowptr, sizeof(int) * (size_t)(S + 1)));
-    CK(cudaMalloc(&r->d_shell_ent, sizeof(int) * 5 * (size_t)S));
     CK(cudaMalloc(&r->d_shell_del, sizeof(double) * 5 * r->sn() * r->dims.num_energies));
-    CK(cudaMalloc(&r->d_shell_f, elem * r->cells()));
+    CK(cudaMalloc(&r->d_shell_f, elem * r->cells() + 16));  // as d_f, tail zeroed as there
+    CK(cudaMemset(r->d_shell_f, 0, elem * r->cells() + 16));
   }
+  cudaFree(r->d_shell_ent);
+  r->d_shell_ent = nullptr;
+  CK(cudaMalloc(&r->d_shell_ent, sizeof(int) * ent.size()));
   CK(cudaMemcpy(r->d_news, news, sizeof(int) * 4 * (size_t)S, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(r->d_shell_rowptr, rowptr.data(), sizeof(int) * (size_t)(S + 1),
-                cudaMemcpyHostToDevice));
   CK(cudaMemcpy(r->d_shell_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice));
+  r->shell_L = (int)L;
   r->kperxkpar = kperxkpar;
   r->shell_on = true;
   return EPREM_GPU_OK;

@@ -68,8 +68,8 @@ int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint6
 // shell.cu -- cross-field (shell) diffusion (DiffuseShellData, ShellData)
 int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, double *del,
                       cudaStream_t st, uint64_t *launches);
-int launch_shell_diffuse(const RunView &r, const int *rowptr, const int *ent, const double *del,
-                         void *scratch, cudaStream_t st, uint64_t *launches);
+int launch_shell_diffuse(const RunView &r, const int *ent, int L, const double *del, void *out,
+                         cudaStream_t st, uint64_t *launches);
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
                      size_t count, cudaStream_t st, uint64_t *launches);
 

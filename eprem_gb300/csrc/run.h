@@ -55,11 +55,13 @@ struct eprem_gpu_run {
   double *d_flux = nullptr;
   double *d_tmpl = nullptr;   // [S][E][M] template rows of eprem_gpu_ripple_f
   // shell diffusion (eprem_gpu_set_shell_diffusion): NEWS links, per-target
-  // gather lists, per-call fractions and an f-sized scratch
+  // gather lists (S x shell_L, padded with -1), per-call fractions and a
+  // second f buffer that each diffusion step writes and then swaps with d_f
   bool shell_on = false;
   double kperxkpar = 0.0;
-  int *d_news = nullptr, *d_shell_rowptr = nullptr, *d_shell_ent = nullptr;
-  double *d_shell_del = nullptr;  // [S][N][E][5]
+  int shell_L = 0;
+  int *d_news = nullptr, *d_shell_ent = nullptr;
+  double *d_shell_del = nullptr;  // [N][E][S][5]
   void *d_shell_f = nullptr;      // Real[S][N][E][M]
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch

@@ -23,7 +23,8 @@
 namespace eprem {
 
 // One thread per node (s, k >= 1): ShellData's four lengths, then per energy
-// the four fractions and their sum, del[((s*N + k)*E + e)*5 + {0..3, 4}].
+// the four fractions and their sum, slice-major so that one (node, energy)
+// slice's fractions sit together: del[((k*E + e)*S + s)*5 + {0..3, 4}].
 __global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, double *del) {
   const size_t SN = (size_t)r.S * r.N;
   const double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
@@ -56,7 +57,7 @@ __global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, doubl
       const double mfp = __dmul_rn(r.ec[e].rig_lamo, mf);
       const double dt_kper =
           __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(r.dt, 0.33333333), mfp), r.ec[e].vgrid), kperxkpar);
-      double *out = del + (g * r.E + e) * 5;
+      double *out = del + (((size_t)k * r.E + e) * r.S + s) * 5;
       double sum = 0.0;
       for (int d = 0; d < 4; d++) {
         double v = dt_kper / __dadd_rn(__dmul_rn(dlper[d], dlper[d]), kVerySmall);
@@ -78,42 +79,82 @@ __device__ __forceinline__ double sd_fms(double a, double b, double acc) {
 __device__ __forceinline__ float sd_fma(float a, float b, float acc) { return __fmaf_rn(a, b, acc); }
 __device__ __forceinline__ float sd_fms(float a, float b, float acc) { return __fmaf_rn(-a, b, acc); }
 
-// One thread per cell of nodes 1..N-1, ordered (k, e, stream, mu): one
-// (node, energy) slice of all streams is in flight at a time, so the
-// neighbours' reads of a slice come from L2.  Writes f + delta to out (same
-// layout as f); the caller copies it back once every cell has been read.
-// ent[p] = source stream * 8 + direction (0..3 north..south, 4 own loss).
-template <typename Real>
-__global__ void k_shell_diffuse(RunView r, const int *rowptr, const int *ent, const double *del,
-                                Real *out) {
-  const Real *f = static_cast<const Real *>(r.f);
+// All cells, ordered (k, e, stream, mu): one (node, energy) slice of all
+// streams is in flight at a time, so the neighbours' reads of a slice come
+// from L2 and f crosses HBM once each way.  Writes the new f to out (node 0
+// copied unchanged); the caller then makes out the run's f.  ent[s*L + p] =
+// source stream * 8 + direction (0..3 north..south, 4 the target's own loss),
+// -1 past the end of the target's list.  Each thread takes two cells a
+// stride apart and issues every load of a chunk of C list entries before the
+// ordered sums, so a warp waits once per chunk rather than once per term.
+template <typename Real, int C>
+__global__ void __launch_bounds__(256) k_shell_diffuse(RunView r, const int *__restrict__ ent,
+                                                       int L, const double *__restrict__ del,
+                                                       Real *__restrict__ out) {
+  const Real *__restrict__ f = static_cast<const Real *>(r.f);
   const size_t M = r.M, S = r.S, E = r.E;
   const size_t per_stream = (size_t)r.N * E * M;
-  const size_t total = (size_t)(r.N - 1) * E * S * M;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
-       t += (size_t)gridDim.x * blockDim.x) {
-    const int m = (int)(t % M);
-    size_t q = t / M;
-    const int s = (int)(q % S);
-    q /= S;
-    const int e = (int)(q % E);
-    const int k = 1 + (int)(q / E);
-    const size_t off = ((size_t)k * E + e) * M + m;
-    const size_t ke5 = ((size_t)k * E + e) * 5;
-    Real acc = Real(0);
-    const int p1 = rowptr[s + 1];
-    for (int p = rowptr[s]; p < p1; p++) {
-      const int code = ent[p];
-      const int i = code >> 3, d = code & 7;
-      const Real a = (Real)del[(size_t)i * r.N * E * 5 + ke5 + d];
-      const Real fi = f[(size_t)i * per_stream + off];
-      acc = d < 4 ? sd_fma(a, fi, acc) : sd_fms(a, fi, acc);
+  const size_t total = (size_t)r.N * E * S * M;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t0 < total; t0 += 2 * stride) {
+    int s[2], k[2], e[2], m[2];
+    bool ok[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const size_t t = t0 + u * stride;
+      ok[u] = t < total;
+      const size_t tc = ok[u] ? t : t0;
+      m[u] = (int)(tc % M);
+      size_t q = tc / M;
+      s[u] = (int)(q % S);
+      q /= S;
+      e[u] = (int)(q % E);
+      k[u] = (int)(q / E);
     }
-    const size_t gi = (size_t)s * per_stream + off;
-    const Real v = f[gi] + acc;
-    out[gi] = v;
-    if (isnan((double)v) || isinf((double)v))
-      set_error(r, isnan((double)v) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, 6, s, k, e, m);
+    Real acc[2] = {Real(0), Real(0)};
+    for (int p0 = 0; p0 < L; p0 += C) {
+      int code[2][C];
+      Real a[2][C], fi[2][C];
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+#pragma unroll
+        for (int q = 0; q < C; q++)
+          code[u][q] = (k[u] > 0 && p0 + q < L) ? __ldg(ent + (size_t)s[u] * L + p0 + q) : -1;
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+#pragma unroll
+        for (int q = 0; q < C; q++) {
+          a[u][q] = Real(0);
+          fi[u][q] = Real(0);
+          if (code[u][q] >= 0) {
+            const int i = code[u][q] >> 3, d = code[u][q] & 7;
+            a[u][q] = (Real)__ldg(del + (((size_t)k[u] * E + e[u]) * S + i) * 5 + d);
+            fi[u][q] = __ldg(f + (size_t)i * per_stream + ((size_t)k[u] * E + e[u]) * M + m[u]);
+          }
+        }
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+#pragma unroll
+        for (int q = 0; q < C; q++)
+          if (code[u][q] >= 0)
+            acc[u] = (code[u][q] & 7) < 4 ? sd_fma(a[u][q], fi[u][q], acc[u])
+                                          : sd_fms(a[u][q], fi[u][q], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      if (!ok[u]) continue;
+      const size_t gi = (size_t)s[u] * per_stream + ((size_t)k[u] * E + e[u]) * M + m[u];
+      const Real fo = f[gi];
+      if (k[u] == 0) {
+        out[gi] = fo;
+        continue;
+      }
+      const Real v = fo + acc[u];
+      out[gi] = v;
+      if (isnan((double)v) || isinf((double)v))
+        set_error(r, isnan((double)v) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, 6, s[u], k[u],
+                  e[u], m[u]);
+    }
   }
 }
 
@@ -126,25 +167,25 @@ int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, doubl
   return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
-int launch_shell_diffuse(const RunView &r, const int *rowptr, const int *ent, const double *del,
-                         void *scratch, cudaStream_t st, uint64_t *launches) {
-  const size_t total = (size_t)(r.N - 1) * r.E * r.S * r.M;
-  const int blocks = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
-  if (r.precision == EPREM_FP32)
-    k_shell_diffuse<float><<<blocks, 256, 0, st>>>(r, rowptr, ent, del, (float *)scratch);
+template <typename Real>
+static void shell_diffuse_as(const RunView &r, const int *ent, int L, const double *del,
+                             void *out, int blocks, cudaStream_t st) {
+  if (L <= 5)
+    k_shell_diffuse<Real, 5><<<blocks, 256, 0, st>>>(r, ent, L, del, (Real *)out);
   else
-    k_shell_diffuse<double><<<blocks, 256, 0, st>>>(r, rowptr, ent, del, (double *)scratch);
+    k_shell_diffuse<Real, 8><<<blocks, 256, 0, st>>>(r, ent, L, del, (Real *)out);
+}
+
+int launch_shell_diffuse(const RunView &r, const int *ent, int L, const double *del, void *out,
+                         cudaStream_t st, uint64_t *launches) {
+  const size_t total = (size_t)r.N * r.E * r.S * r.M;
+  const int blocks = (int)std::min<size_t>((total + 511) / 512, 152 * 8);
+  if (r.precision == EPREM_FP32)
+    shell_diffuse_as<float>(r, ent, L, del, out, blocks, st);
+  else
+    shell_diffuse_as<double>(r, ent, L, del, out, blocks, st);
   ++*launches;
-  if (cudaPeekAtLastError() != cudaSuccess) return EPREM_GPU_ERR_CUDA;
-  // nodes 1..N-1 of every stream back into f
-  const size_t elem = r.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
-  const size_t em = (size_t)r.E * r.M, pitch = (size_t)r.N * em * elem;
-  char *dst = static_cast<char *>(r.f) + em * elem;
-  const char *src = static_cast<const char *>(scratch) + em * elem;
-  return cudaMemcpy2DAsync(dst, pitch, src, pitch, (size_t)(r.N - 1) * em * elem, r.S,
-                           cudaMemcpyDeviceToDevice, st) == cudaSuccess
-             ? 0
-             : EPREM_GPU_ERR_CUDA;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
 }  // namespace eprem
