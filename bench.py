@@ -75,6 +75,10 @@ def parse():
     ap.add_argument("--profile-step", choices=["fp32", "fp64"], default=None,
                     help="run one EP sub-step of the 96-stream subset and exit "
                          "(the case the ncu captures use)")
+    ap.add_argument("--shell-diffusion", type=float, default=None, metavar="KPERXKPAR",
+                    help="with --profile-step: shell diffusion on (torus NEWS links, every "
+                         "stream with four in-links as on the cube sphere); prints the "
+                         "CUDA-event time of each kernel kind of the second of two steps")
     return ap.parse_args()
 
 
@@ -786,10 +790,23 @@ def profile_step(args):
     prec = abi.EPREM_FP32 if args.profile_step == "fp32" else abi.EPREM_FP64
     run, g, nodes = make_state(sub, prec, EpremRun, abi, W)
     run.upload_f(W.fill_initial_f(sub, nodes, g, np.empty(sub.cells)))
+    extra = {}
+    if args.shell_diffusion is not None:
+        S, C = sub.num_streams, 4 * sub.cols
+        s = np.arange(S)
+        run.set_shell_diffusion(np.stack([(s - C) % S, (s + 1) % S, (s - 1) % S, (s + C) % S],
+                                         axis=1), args.shell_diffusion)
+        run.update_energetic_particles(0.0)
+        run.read_stats()
+        run.set_kernel_timing(True)
+        run.read_kernel_timing()
     run.update_energetic_particles(0.0)
     run.synchronize()
+    if args.shell_diffusion is not None:
+        extra["kernel_ms"] = {k: v[1] for k, v in run.read_kernel_timing().items() if v[0]}
+        extra["shell_diffusion"] = args.shell_diffusion
     print(json.dumps({"profile_step": args.profile_step, "workload": sub.name,
-                      "stats": run.read_stats().as_dict()}))
+                      "stats": run.read_stats().as_dict(), **extra}))
     run.close()
 
 

@@ -66,9 +66,9 @@ int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *l
 int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint64_t *launches);
 
 // shell.cu -- cross-field (shell) diffusion (DiffuseShellData, ShellData)
-int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, double *del,
+int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void *del,
                       cudaStream_t st, uint64_t *launches);
-int launch_shell_diffuse(const RunView &r, const int *ent, int L, const double *del, void *out,
+int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
                          cudaStream_t st, uint64_t *launches);
 int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
                      size_t count, cudaStream_t st, uint64_t *launches);

@@ -61,7 +61,7 @@ struct eprem_gpu_run {
   double kperxkpar = 0.0;
   int shell_L = 0;
   int *d_news = nullptr, *d_shell_ent = nullptr;
-  double *d_shell_del = nullptr;  // [N][E][S][5]
+  void *d_shell_del = nullptr;    // Real[N][E][S][5]
   void *d_shell_f = nullptr;      // Real[S][N][E][M]
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch

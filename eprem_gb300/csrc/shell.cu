@@ -25,7 +25,10 @@ namespace eprem {
 // One thread per node (s, k >= 1): ShellData's four lengths, then per energy
 // the four fractions and their sum, slice-major so that one (node, energy)
 // slice's fractions sit together: del[((k*E + e)*S + s)*5 + {0..3, 4}].
-__global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, double *del) {
+// Formed in double, stored as the f type (float in the FP32 form, whose
+// diffusion then runs without FP64 instructions).
+template <typename Real>
+__global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, Real *del) {
   const size_t SN = (size_t)r.S * r.N;
   const double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
                *rz = node_field(r, EPREM_NODE_RZ), *bm = node_field(r, EPREM_NODE_BMAG),
@@ -57,15 +60,15 @@ __global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, doubl
       const double mfp = __dmul_rn(r.ec[e].rig_lamo, mf);
       const double dt_kper =
           __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(r.dt, 0.33333333), mfp), r.ec[e].vgrid), kperxkpar);
-      double *out = del + (((size_t)k * r.E + e) * r.S + s) * 5;
+      Real *out = del + (((size_t)k * r.E + e) * r.S + s) * 5;
       double sum = 0.0;
       for (int d = 0; d < 4; d++) {
         double v = dt_kper / __dadd_rn(__dmul_rn(dlper[d], dlper[d]), kVerySmall);
         if (v > 0.025) v = 0.025;
-        out[d] = v;
+        out[d] = (Real)v;
         sum = d == 0 ? v : __dadd_rn(sum, v);
       }
-      out[4] = sum;
+      out[4] = (Real)sum;
     }
   }
 }
@@ -79,107 +82,173 @@ __device__ __forceinline__ double sd_fms(double a, double b, double acc) {
 __device__ __forceinline__ float sd_fma(float a, float b, float acc) { return __fmaf_rn(a, b, acc); }
 __device__ __forceinline__ float sd_fms(float a, float b, float acc) { return __fmaf_rn(-a, b, acc); }
 
-// All cells, ordered (k, e, stream, mu): one (node, energy) slice of all
-// streams is in flight at a time, so the neighbours' reads of a slice come
-// from L2 and f crosses HBM once each way.  Writes the new f to out (node 0
-// copied unchanged); the caller then makes out the run's f.  ent[s*L + p] =
-// source stream * 8 + direction (0..3 north..south, 4 the target's own loss),
-// -1 past the end of the target's list.  Each thread takes two cells a
-// stride apart and issues every load of a chunk of C list entries before the
-// ordered sums, so a warp waits once per chunk rather than once per term.
-template <typename Real, int C>
-__global__ void __launch_bounds__(256) k_shell_diffuse(RunView r, const int *__restrict__ ent,
-                                                       int L, const double *__restrict__ del,
-                                                       Real *__restrict__ out) {
+// NaN or Inf, by the exponent bits (no floating-point instruction)
+__device__ __forceinline__ bool nonfinite(double v) {
+  return (__double_as_longlong(v) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool nonfinite(float v) {
+  return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
+}
+
+// V consecutive values of f (V = 1 or 2: one 8- or 16-byte access)
+template <int V, typename Real>
+__device__ __forceinline__ void ld_vec(const Real *p, Real (&x)[V]) {
+  if constexpr (V == 1) {
+    x[0] = __ldg(p);
+  } else if constexpr (sizeof(Real) == 4) {
+    const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+    x[0] = t.x, x[1] = t.y;
+  } else {
+    const double2 t = __ldg(reinterpret_cast<const double2 *>(p));
+    x[0] = t.x, x[1] = t.y;
+  }
+}
+template <int V, typename Real>
+__device__ __forceinline__ void st_vec(Real *p, const Real (&x)[V]) {
+  if constexpr (V == 1) {
+    p[0] = x[0];
+  } else if constexpr (sizeof(Real) == 4) {
+    *reinterpret_cast<float2 *>(p) = make_float2(x[0], x[1]);
+  } else {
+    *reinterpret_cast<double2 *>(p) = make_double2(x[0], x[1]);
+  }
+}
+
+// One (node, energy) slice of all streams per block at a time (blocks stride
+// over the N*E slices), so the neighbours' reads of a slice come from L2 and
+// f crosses HBM once each way.  Writes the new f to out (node 0 copied
+// unchanged); the caller then makes out the run's f.  ent[s*L + p] = source
+// stream * 8 + direction (0..3 north..south, 4 the target's own loss), -1
+// past the end of the target's list.  A thread takes V adjacent mu cells
+// (V = 2 when M is even: the list and fractions are read once for both) at
+// two places of the slice blockDim apart ((stream, mu) stepped by counters,
+// no divisions), and issues every load of a chunk of C list entries before
+// the ordered sums.
+template <typename Real, int C, int V>
+__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
+    k_shell_diffuse(RunView r, const int *__restrict__ ent, int L, const Real *__restrict__ del,
+                    Real *__restrict__ out) {
   const Real *__restrict__ f = static_cast<const Real *>(r.f);
-  const size_t M = r.M, S = r.S, E = r.E;
+  const int M = r.M, S = r.S, E = r.E;
+  const int MV = M / V;      // V-cell groups per row
+  const int groups = S * MV;  // of one slice
   const size_t per_stream = (size_t)r.N * E * M;
-  const size_t total = (size_t)r.N * E * S * M;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t0 < total; t0 += 2 * stride) {
-    int s[2], k[2], e[2], m[2];
-    bool ok[2];
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-      const size_t t = t0 + u * stride;
-      ok[u] = t < total;
-      const size_t tc = ok[u] ? t : t0;
-      m[u] = (int)(tc % M);
-      size_t q = tc / M;
-      s[u] = (int)(q % S);
-      q /= S;
-      e[u] = (int)(q % E);
-      k[u] = (int)(q / E);
-    }
-    Real acc[2] = {Real(0), Real(0)};
-    for (int p0 = 0; p0 < L; p0 += C) {
-      int code[2][C];
-      Real a[2][C], fi[2][C];
+  const int nslices = r.N * E;
+  const int inc_s = blockDim.x / MV, inc_m = blockDim.x % MV;
+  const int s_first = threadIdx.x / MV, m_first = threadIdx.x % MV;
+  for (int sl = blockIdx.x; sl < nslices; sl += gridDim.x) {
+    const int k = sl / E, e = sl - (sl / E) * E;
+    const size_t row = (size_t)sl * M;                 // (k*E + e)*M within a stream
+    const Real *__restrict__ dsl = del + (size_t)sl * S * 5;
+    int s0 = s_first, m0 = m_first;
+    for (int c = threadIdx.x; c < groups; c += 2 * blockDim.x) {
+      int s[2], m[2];
+      s[0] = s0;
+      m[0] = m0;
+      s[1] = s0 + inc_s;
+      m[1] = m0 + inc_m;
+      if (m[1] >= MV) {
+        m[1] -= MV;
+        s[1]++;
+      }
+      const bool ok1 = c + (int)blockDim.x < groups;
+      if (!ok1) s[1] = s[0], m[1] = m[0];
+      s0 = s[1] + inc_s;  // the next pair starts blockDim past the second group
+      m0 = m[1] + inc_m;
+      if (m0 >= MV) {
+        m0 -= MV;
+        s0++;
+      }
+      Real acc[2][V];
 #pragma unroll
       for (int u = 0; u < 2; u++)
 #pragma unroll
-        for (int q = 0; q < C; q++)
-          code[u][q] = (k[u] > 0 && p0 + q < L) ? __ldg(ent + (size_t)s[u] * L + p0 + q) : -1;
+        for (int j = 0; j < V; j++) acc[u][j] = Real(0);
+      for (int p0 = 0; k > 0 && p0 < L; p0 += C) {
+        int code[2][C];
+        Real a[2][C], fi[2][C][V];
 #pragma unroll
-      for (int u = 0; u < 2; u++)
+        for (int u = 0; u < 2; u++)
 #pragma unroll
-        for (int q = 0; q < C; q++) {
-          a[u][q] = Real(0);
-          fi[u][q] = Real(0);
-          if (code[u][q] >= 0) {
-            const int i = code[u][q] >> 3, d = code[u][q] & 7;
-            a[u][q] = (Real)__ldg(del + (((size_t)k[u] * E + e[u]) * S + i) * 5 + d);
-            fi[u][q] = __ldg(f + (size_t)i * per_stream + ((size_t)k[u] * E + e[u]) * M + m[u]);
+          for (int q = 0; q < C; q++)
+            code[u][q] = p0 + q < L ? __ldg(ent + s[u] * L + p0 + q) : -1;
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+          for (int q = 0; q < C; q++) {
+            a[u][q] = Real(0);
+#pragma unroll
+            for (int j = 0; j < V; j++) fi[u][q][j] = Real(0);
+            if (code[u][q] >= 0) {
+              const int i = code[u][q] >> 3;
+              a[u][q] = __ldg(dsl + i * 5 + (code[u][q] & 7));
+              ld_vec<V>(f + (size_t)i * per_stream + row + (size_t)m[u] * V, fi[u][q]);
+            }
+          }
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+          for (int q = 0; q < C; q++)
+            if (code[u][q] >= 0) {
+              const bool gain = (code[u][q] & 7) < 4;
+#pragma unroll
+              for (int j = 0; j < V; j++)
+                acc[u][j] = gain ? sd_fma(a[u][q], fi[u][q][j], acc[u][j])
+                                 : sd_fms(a[u][q], fi[u][q][j], acc[u][j]);
+            }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+        if (u == 1 && !ok1) break;
+        const size_t gi = (size_t)s[u] * per_stream + row + (size_t)m[u] * V;
+        Real v[V];
+        ld_vec<V>(f + gi, v);
+        if (k > 0) {
+#pragma unroll
+          for (int j = 0; j < V; j++) {
+            v[j] = v[j] + acc[u][j];
+            if (nonfinite(v[j]))
+              set_error(r, isnan(v[j]) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, 6, s[u], k, e,
+                        m[u] * V + j);
           }
         }
-#pragma unroll
-      for (int u = 0; u < 2; u++)
-#pragma unroll
-        for (int q = 0; q < C; q++)
-          if (code[u][q] >= 0)
-            acc[u] = (code[u][q] & 7) < 4 ? sd_fma(a[u][q], fi[u][q], acc[u])
-                                          : sd_fms(a[u][q], fi[u][q], acc[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-      if (!ok[u]) continue;
-      const size_t gi = (size_t)s[u] * per_stream + ((size_t)k[u] * E + e[u]) * M + m[u];
-      const Real fo = f[gi];
-      if (k[u] == 0) {
-        out[gi] = fo;
-        continue;
+        st_vec<V>(out + gi, v);
       }
-      const Real v = fo + acc[u];
-      out[gi] = v;
-      if (isnan((double)v) || isinf((double)v))
-        set_error(r, isnan((double)v) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, 6, s[u], k[u],
-                  e[u], m[u]);
     }
   }
 }
 
-int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, double *del,
+int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void *del,
                       cudaStream_t st, uint64_t *launches) {
   const size_t SN = (size_t)r.S * r.N;
   const int blocks = (int)std::min<size_t>((SN + 127) / 128, 152 * 8);
-  k_shell_coef<<<blocks, 128, 0, st>>>(r, news, kperxkpar, del);
+  if (r.precision == EPREM_FP32)
+    k_shell_coef<float><<<blocks, 128, 0, st>>>(r, news, kperxkpar, (float *)del);
+  else
+    k_shell_coef<double><<<blocks, 128, 0, st>>>(r, news, kperxkpar, (double *)del);
   ++*launches;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
 template <typename Real>
-static void shell_diffuse_as(const RunView &r, const int *ent, int L, const double *del,
+static void shell_diffuse_as(const RunView &r, const int *ent, int L, const void *del,
                              void *out, int blocks, cudaStream_t st) {
-  if (L <= 5)
-    k_shell_diffuse<Real, 5><<<blocks, 256, 0, st>>>(r, ent, L, del, (Real *)out);
+  const Real *d = (const Real *)del;
+  Real *o = (Real *)out;
+  const bool pairs = r.M % 2 == 0;
+  if (L <= 5 && pairs)
+    k_shell_diffuse<Real, 5, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+  else if (L <= 5)
+    k_shell_diffuse<Real, 5, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+  else if (pairs)
+    k_shell_diffuse<Real, 8, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
   else
-    k_shell_diffuse<Real, 8><<<blocks, 256, 0, st>>>(r, ent, L, del, (Real *)out);
+    k_shell_diffuse<Real, 8, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
 }
 
-int launch_shell_diffuse(const RunView &r, const int *ent, int L, const double *del, void *out,
+int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
                          cudaStream_t st, uint64_t *launches) {
-  const size_t total = (size_t)r.N * r.E * r.S * r.M;
-  const int blocks = (int)std::min<size_t>((total + 511) / 512, 152 * 8);
+  const int blocks = std::min(r.N * r.E, 152 * 8);
   if (r.precision == EPREM_FP32)
     shell_diffuse_as<float>(r, ent, L, del, out, blocks, st);
   else
