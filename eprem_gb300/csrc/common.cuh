@@ -45,6 +45,9 @@ struct EnergyConsts {
   double seed_power;     // pow(E/normE1, -gamma)           (src/energeticParticlesBoundary.c:101)
   double seed_exp;       // exp(-(E/normE0))                (:102)
   float v32, vi32;       // vgrid, vgrid_i rounded to float (FP32 stencils)
+  float dvi32;           // vgrid_i[e+1] - vgrid_i[e-1] (0 at the ends), from FP64
+  int seed_k;            // FP32 streaming seeds are held as seed * 2^seed_k, so that
+                         // the energy-only factor of sepSeedFunction is near 1
 };
 
 // Per-node coefficients of the FP32 focusing / change kernels, fixed for one
@@ -54,13 +57,18 @@ struct NodeCoef32 {
   int ok, ns_f, ns_c, pad0;
   float dlnbds, dupar, b, scale_f;  // focusing: a_E = -v dlnbds - (2/v) dupar
   float cool, dlnb, dlnn, scale_c;  // change (rates per unit time)
-  float bc0, bc1, pad1, pad2;       // ln seed at the first and last energy
+  // ln seed at the first and last energy as kbc * ln 2 + bc: the integer
+  // part of log2 seed apart, so the change kernel can form the boundary
+  // value relative to a row's exponent without losing the fraction
+  float bc0, bc1;
+  int kbc0, kbc1;
 };
 
 struct RunView {
   int S, N, E, M;
   int precision;
   void *f;                 // Real*
+  short *fexp;             // [S][N][E] FP32 form: row exponents, f = f_stored * 2^-fexp
   double *nodes;           // [NF][S*N]
   const double *mugrid;    // [M]
   const EnergyConsts *ec;  // [E]
@@ -78,8 +86,6 @@ struct RunView {
   // parameters
   double r_scale, dt, dt_full, dmu, dlnp;
   double norm_j0, bf_xi, dsh_min, damp_cooling;
-  double f_scale, f_unscale;  // device f = f * f_scale (2^kF32Shift in the FP32 form, else 1)
-  double ln_f_shift;          // ln f_scale (0 in FP64): the change operator works on ln f itself
   // A view of streams [s_base, s_base + S) of the run (stream_range_view):
   // node field k of node g is nodes[k * node_stride + g]
   size_t node_stride;
@@ -119,19 +125,50 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double 
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
-// The FP32 form holds f multiplied by 2^kF32Shift.  Streaming,
-// isotropisation and focusing are linear in f, so the shift changes none of
-// their results beyond rounding.  Adiabatic change advects ln f in flux form
-// with a velocity that varies along ln p, which is not invariant under
-// ln f -> ln f + const: its kernels take ln f_scale off on load (and off the
-// seed boundary values) and put it back before the exponential.  The shift
-// moves the float window from [1.2e-38, 3.4e38]
-// to [6.4e-58, 1.8e19] in EPREM's normalised units, where the distributions
-// of real runs live: their far tails (f down to 1e-240 in the MAS testsuite
-// runs) then floor 20 decades lower, so floored cells stop feeding the
-// fluxes within 30 decades of the peak.  Conversions, seeds and the flux
-// apply the shift; FP64 runs use a scale of 1.
-constexpr int kF32Shift = 64;
+// The FP32 form holds each (stream, node, energy) row of M cells as floats
+// with its own binary exponent: f = stored * 2^-fexp[row].  The reference's
+// distributions span 230 decades across energies (the exponential cut-off
+// of the seed spectrum), far beyond a float's 76, and its adiabatic change
+// works on ln f, so a cell floored by the float range would feed a wrong
+// ln f into its neighbours in energy; with one exponent per row every row
+// keeps its own 76 decades.  A normalised row has its largest value in
+// [2^kRowTop, 2^(kRowTop+1)): streaming, linear in f, brings every row of a
+// (stream, energy) slab to the slab's common exponent on load and renormalises
+// the slab; focusing keeps the row's exponent (its values grow at most M-fold);
+// the change, in ln f, renormalises each row it writes.  Exponents stay at or
+// below kRowExpMax, where the float floor FLT_MIN is the reference's DBL_MIN:
+// no row ever floors below the reference's floor.
+constexpr int kRowTop = 95;
+constexpr int kRowExpMax = 896;   // FLT_MIN * 2^-896 = 2^-1022 = DBL_MIN
+constexpr int kRowExpMin = -1000;
+constexpr int kNoExp = -(1 << 20);  // log2 of a zero
+
+__device__ __forceinline__ int clamp_exp(int k) {
+  return k > kRowExpMax ? kRowExpMax : (k < kRowExpMin ? kRowExpMin : k);
+}
+// 2^k as a float, k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+// x * 2^k for any k (two exact power-of-two steps; results below the float
+// range underflow as a product would)
+__device__ __forceinline__ float ldexp_f(float x, int k) {
+  const int k1 = k > 127 ? 127 : (k < -126 ? -126 : k);
+  int k2 = k - k1;
+  k2 = k2 > 127 ? 127 : (k2 < -126 ? -126 : k2);
+  return (x * pow2f(k1)) * pow2f(k2);
+}
+// floor(log2 x) of a non-negative float from its bits; kNoExp for zero
+__device__ __forceinline__ int ilogb_f(float x) {
+  const int b = __float_as_int(x) & 0x7fffffff;
+  const int ex = b >> 23;
+  if (ex) return ex - 127;
+  const int m = b & 0x7fffff;
+  return m ? -149 + (31 - __clz(m)) : kNoExp;
+}
+// the exponent that brings a row whose largest true value has floor(log2) = lg
+// to [2^kRowTop, 2^(kRowTop+1))
+__device__ __forceinline__ int row_exp_for(int lg) {
+  return lg == kNoExp ? 0 : clamp_exp(kRowTop - lg);
+}
 
 // sepSeedFunction (src/energeticParticlesBoundary.c:67-116) with the
 // node-only factor (radial term) and the energy-only factors precomputed:
@@ -142,7 +179,7 @@ __device__ __forceinline__ double seed_value(const RunView &r, const EnergyConst
   double normJ = normJHe / r.bf_xi;
   double normf = normJ / (2.0 * ec.egrid);
   if (normf < DBL_MIN) normf = DBL_MIN;
-  return normf * r.f_scale;  // in the device's units of f (exact: a power of two)
+  return normf;
 }
 
 // Floor value below which the reference resets f (DBL_MIN); the FP32 form

@@ -17,7 +17,7 @@ using namespace eprem;
 // streams (the kernel that takes 90 % of a step) and keeps the fastest.  The
 // copy has its own status block, so the run's statistics are untouched.
 namespace {
-constexpr int kTuneVariants[] = {5, 4, 3, 2, 1};
+constexpr int kTuneVariants[] = {5, 4, 3};
 
 int tune_stream(eprem_gpu_run *r, int *chosen) {
   const eprem_params_t &p = r->params;
@@ -30,19 +30,26 @@ int tune_stream(eprem_gpu_run *r, int *chosen) {
     return cuda_fail(cudaGetLastError(), "autotune coefficient launch");
   const int S_sub = r->dims.num_streams < 96 ? r->dims.num_streams : 96;
   const size_t n = (size_t)S_sub * r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
+  const size_t nrows = n / r->dims.num_mu;
   void *f = nullptr;
+  short *fx = nullptr;  // the copy's row exponents
   DevStatus *st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaMalloc(&f, n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&fx, nrows * sizeof(short));
   if (e == cudaSuccess) e = cudaMalloc(&st, sizeof(DevStatus));
   if (e == cudaSuccess) e = cudaMemsetAsync(st, 0, sizeof(DevStatus), r->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(f, r->d_f, n * sizeof(float), cudaMemcpyDeviceToDevice, r->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(fx, r->d_fexp, nrows * sizeof(short), cudaMemcpyDeviceToDevice,
+                        r->stream);
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   RunView v = r->v;
   v.S = S_sub;
   v.f = f;
+  v.fexp = fx;
   v.status = st;
   float best = -1.f;
   int best_variant = 0;
@@ -70,6 +77,7 @@ int tune_stream(eprem_gpu_run *r, int *chosen) {
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
   cudaFree(f);
+  cudaFree(fx);
   cudaFree(st);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

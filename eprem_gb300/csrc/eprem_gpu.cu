@@ -156,6 +156,9 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   const size_t SN = r->sn(), cells = r->cells();
   const size_t fbytes = dims->precision == EPREM_FP64 ? sizeof(double) : sizeof(float);
   if (e == cudaSuccess) e = cudaMalloc(&r->d_f, cells * fbytes + 16);
+  if (e == cudaSuccess && dims->precision == EPREM_FP32) e = dalloc(&r->d_fexp, SN * E);
+  if (e == cudaSuccess && r->d_fexp)
+    e = cudaMemsetAsync(r->d_fexp, 0, SN * E * sizeof(short), r->stream);
   if (e == cudaSuccess) e = dalloc(&r->d_nodes, (size_t)EPREM_NODE_NFIELDS * SN);
   if (e == cudaSuccess) e = dalloc(&r->d_mugrid, (size_t)M);
   if (e == cudaSuccess) e = dalloc(&r->d_mugrid32, (size_t)M);
@@ -184,6 +187,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   const eprem_params_t &p = r->params;
   std::vector<EnergyConsts> ec(E);
   const double normE1 = 1.0 * kEfac, normE0 = p.bf_ecutoff * kEfac;
+  const double norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);
   for (int i = 0; i < E; i++) {
     ec[i].egrid = grids->egrid[i];
     ec[i].vgrid = grids->vgrid[i];
@@ -193,6 +197,11 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
     ec[i].seed_exp = exp(-(grids->egrid[i] / normE0));
     ec[i].v32 = (float)grids->vgrid[i];
     ec[i].vi32 = (float)grids->vgrid_i[i];
+    ec[i].dvi32 = (i >= 1 && i + 1 < E)
+                      ? (float)(grids->vgrid_i[i + 1] - grids->vgrid_i[i - 1]) : 0.f;
+    // the energy-only factor of sepSeedFunction, normalised to [1, 2) by 2^seed_k
+    const double ce = norm_j0 * ec[i].seed_power * ec[i].seed_exp / p.bf_xi / (2.0 * ec[i].egrid);
+    ec[i].seed_k = (std::isfinite(ce) && ce >= DBL_MIN) ? -ilogb(ce) : 1022;
   }
   std::vector<float> mu32(M);
   for (int m = 0; m < M; m++) mu32[m] = (float)grids->mugrid[m];
@@ -217,6 +226,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.S = S; v.N = N; v.E = E; v.M = M;
   v.precision = dims->precision;
   v.f = r->d_f;
+  v.fexp = r->d_fexp;
   v.nodes = r->d_nodes;
   v.mugrid = r->d_mugrid;
   v.mugrid32 = r->d_mugrid32;
@@ -235,13 +245,9 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   v.r_scale = p.r_scale;
   v.dt = p.t_del / (1.0 * p.num_ep_steps);  // src/energeticParticles.c:99
   v.dt_full = v.dt * p.num_ep_steps;        // :861, :1582
-  const bool fp32 = dims->precision == EPREM_FP32;
-  v.f_scale = fp32 ? ldexp(1.0, kF32Shift) : 1.0;
-  v.f_unscale = fp32 ? ldexp(1.0, -kF32Shift) : 1.0;
-  v.ln_f_shift = fp32 ? kF32Shift * 0.69314718055994530942 : 0.0;  // ln 2^K
   v.dmu = grids->dmu;
   v.dlnp = grids->dlnp;
-  v.norm_j0 = p.bf_amplitude * (kMp * kC) / (kMhdDensityNorm * kMev);
+  v.norm_j0 = norm_j0;
   v.bf_xi = p.bf_xi;
   v.dsh_min = p.dsh_min;
   v.damp_cooling = p.damp_cooling;
@@ -276,6 +282,8 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   if (!r) return EPREM_GPU_OK;
   if (r->stream) cudaStreamSynchronize(r->stream);
   cudaFree(r->d_f);
+  cudaFree(r->d_fexp);
+  cudaFree(r->d_shell_fexp);
   cudaFree(r->d_nodes);
   cudaFree(r->d_mugrid);
   cudaFree(r->d_mugrid32);
@@ -324,8 +332,10 @@ static int ensure_stage(eprem_gpu_run *r, size_t elems) {
   return EPREM_GPU_OK;
 }
 
-// Chunk of doubles staged at a time when converting f for the FP32 form.
+// Chunk of doubles staged at a time when converting f for the FP32 form:
+// whole rows of M cells (each row is converted with its exponent).
 static const size_t kStageChunk = (size_t)1 << 27;
+static size_t stage_chunk(size_t M) { return kStageChunk / M * M; }
 
 // Upload of an FP32-form f: chunks of FP64 host values through a staging
 // buffer, converted on the run's stream (the host-to-device copies run at the
@@ -337,7 +347,8 @@ extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
     CK(cudaMemcpyAsync(r->d_f, f, n * sizeof(double), cudaMemcpyHostToDevice, r->stream));
     return EPREM_GPU_OK;
   }
-  const size_t chunk = n < kStageChunk ? n : kStageChunk;
+  const size_t M = r->dims.num_mu;
+  const size_t chunk = n < stage_chunk(M) ? n : stage_chunk(M);  // whole rows
   int rc = ensure_stage(r, chunk);
   if (rc) return rc;
   // the copy stream's downloads may still read the staging buffers
@@ -348,8 +359,7 @@ extern "C" int eprem_gpu_upload_f(eprem_gpu_run *r, const double *f) {
     const size_t c = (n - off) < chunk ? (n - off) : chunk;
     double *buf = r->d_stage + (k & 1) * r->stage_elems;
     CK(cudaMemcpyAsync(buf, f + off, c * sizeof(double), cudaMemcpyHostToDevice, r->stream));
-    rc = launch_convert_f(r->v, buf, reinterpret_cast<double *>(static_cast<float *>(r->d_f) + off),
-                          1, c, r->stream, &r->launches);
+    rc = launch_convert_f(r->v, off / M, c / M, buf, 1, r->stream, &r->launches);
     if (rc) return fail(rc, "conversion kernel launch failed");
   }
   return EPREM_GPU_OK;
@@ -364,7 +374,8 @@ extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
   if (r->dims.precision == EPREM_FP64) {
     CK(cudaMemcpyAsync(f, r->d_f, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
   } else {
-    const size_t chunk = n < kStageChunk ? n : kStageChunk;
+    const size_t M = r->dims.num_mu;
+    const size_t chunk = n < stage_chunk(M) ? n : stage_chunk(M);  // whole rows
     int rc = ensure_stage(r, chunk);
     if (rc) return rc;
     cudaEvent_t *converted = r->stage_ev, *copied = r->stage_ev + 2;
@@ -375,9 +386,7 @@ extern "C" int eprem_gpu_download_f(eprem_gpu_run *r, double *f) {
       const size_t c = (n - off) < chunk ? (n - off) : chunk;
       double *buf = r->d_stage + (k & 1) * r->stage_elems;
       CK(cudaStreamWaitEvent(r->stream, copied[k & 1], 0));
-      rc = launch_convert_f(r->v,
-                            reinterpret_cast<const double *>(static_cast<const float *>(r->d_f) + off),
-                            buf, 0, c, r->stream, &r->launches);
+      rc = launch_convert_f(r->v, off / M, c / M, buf, 0, r->stream, &r->launches);
       if (rc) return fail(rc, "conversion kernel launch failed");
       CK(cudaEventRecord(converted[k & 1], r->stream));
       CK(cudaStreamWaitEvent(r->copy_stream, converted[k & 1], 0));
@@ -420,14 +429,13 @@ static int copy_f_pitched(eprem_gpu_run *r, double *host, size_t stream_pitch, b
     const int ns = std::min(group, S - s0);
     const RunView v = stream_range_view(r, s0, s0 + ns);
     double *buf = r->d_stage;
+    const size_t nrows = (size_t)ns * per / r->dims.num_mu;
     if (up) {
       CK(cudaMemcpy2DAsync(buf, row, host + (size_t)s0 * pitch, pitch * sizeof(double), row, ns,
                            cudaMemcpyHostToDevice, r->stream));
-      rc = launch_convert_f(v, buf, static_cast<double *>(v.f), 1, ns * per, r->stream,
-                            &r->launches);
+      rc = launch_convert_f(v, 0, nrows, buf, 1, r->stream, &r->launches);
     } else {
-      rc = launch_convert_f(v, static_cast<const double *>(v.f), buf, 0, ns * per, r->stream,
-                            &r->launches);
+      rc = launch_convert_f(v, 0, nrows, buf, 0, r->stream, &r->launches);
       if (!rc)
         CK(cudaMemcpy2DAsync(host + (size_t)s0 * pitch, pitch * sizeof(double), buf, row, row, ns,
                              cudaMemcpyDeviceToHost, r->stream));
@@ -495,6 +503,7 @@ static RunView stream_range_view(const eprem_gpu_run *r, int s0, int s1) {
   u.s_base = v.s_base + s0;
   u.f = v.precision == EPREM_FP32 ? static_cast<void *>(static_cast<float *>(v.f) + c0)
                                   : static_cast<void *>(static_cast<double *>(v.f) + c0);
+  if (u.fexp) u.fexp = v.fexp + n0 * v.E;
   u.nodes = v.nodes + n0;
   u.list = v.list + n0;
   u.list_size = v.list_size + s0;
@@ -560,11 +569,13 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
     if (shell) {
       rc = timed(r, EPREM_KERNEL_SHELL, [&] {
         return launch_shell_diffuse(v, r->d_shell_ent, r->shell_L, r->d_shell_del, r->d_shell_f,
-                                    r->stream, &r->launches);
+                                    r->d_shell_fexp, r->stream, &r->launches);
       });
       if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion launch");
       std::swap(r->d_f, r->d_shell_f);  // the new f is the other buffer
+      std::swap(r->d_fexp, r->d_shell_fexp);
       r->v.f = r->d_f;
+      r->v.fexp = r->d_fexp;
     }
   }
   return EPREM_GPU_OK;
@@ -650,15 +661,13 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
     const RunView v = stream_range_view(r, s0, s1);
     CK(cudaStreamWaitEvent(r->stream, arrived[c & 1], 0));
     if (fp32) {
-      rc = launch_convert_f(v, dev64(c), static_cast<double *>(v.f), 1, n, r->stream,
-                            &r->launches);
+      rc = launch_convert_f(v, 0, n / r->dims.num_mu, dev64(c), 1, r->stream, &r->launches);
       if (rc) return fail(rc, "conversion kernel launch failed");
     }
     rc = ep_update(r, v);
     if (rc) break;
     if (fp32) {
-      rc = launch_convert_f(v, static_cast<const double *>(v.f), dev64(c), 0, n, r->stream,
-                            &r->launches);
+      rc = launch_convert_f(v, 0, n / r->dims.num_mu, dev64(c), 0, r->stream, &r->launches);
       if (rc) return fail(rc, "conversion kernel launch failed");
     }
     CK(cudaEventRecord(updated[c & 1], r->stream));
@@ -861,6 +870,10 @@ extern "C" int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *ne
     CK(cudaMalloc(&r->d_shell_del, sizeof(double) * 5 * r->sn() * r->dims.num_energies));
     CK(cudaMalloc(&r->d_shell_f, elem * r->cells() + 16));  // as d_f, tail zeroed as there
     CK(cudaMemset(r->d_shell_f, 0, elem * r->cells() + 16));
+    if (r->dims.precision == EPREM_FP32) {
+      CK(cudaMalloc(&r->d_shell_fexp, sizeof(short) * r->sn() * r->dims.num_energies + 16));
+      CK(cudaMemset(r->d_shell_fexp, 0, sizeof(short) * r->sn() * r->dims.num_energies));
+    }
   }
   cudaFree(r->d_shell_ent);
   r->d_shell_ent = nullptr;

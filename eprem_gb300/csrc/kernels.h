@@ -31,6 +31,8 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *pla
 int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                    uint64_t *launches);
+// seedPopulationCheck alone in the FP32 form (rows renormalised)
+int launch_seed_check32(const RunView &r, cudaStream_t st, uint64_t *launches);
 
 // node.cu -- AdiabaticFocusing + AdiabaticChange
 struct NodePlan {
@@ -68,10 +70,13 @@ int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint6
 // shell.cu -- cross-field (shell) diffusion (DiffuseShellData, ShellData)
 int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void *del,
                       cudaStream_t st, uint64_t *launches);
+// xout: the FP32 form's output row exponents (null in FP64)
 int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
-                         cudaStream_t st, uint64_t *launches);
-int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
-                     size_t count, cudaStream_t st, uint64_t *launches);
+                         short *xout, cudaStream_t st, uint64_t *launches);
+// FP32 form: rows [row0, row0 + nrows) of view r between an FP64 staging
+// buffer and the device's rows with their exponents
+int launch_convert_f(const RunView &r, size_t row0, size_t nrows, double *stage, int to_device,
+                     cudaStream_t st, uint64_t *launches);
 
 // mas.cu -- MAS background (updateMhd MHD_MAS branch, masMoveNodes)
 struct MasSlotDev {

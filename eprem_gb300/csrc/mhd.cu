@@ -141,23 +141,36 @@ __global__ void k_omni_flux(RunView r, double *out) {
     double iso = 0.0;
     for (int m = 0; m < r.M; ++m) iso += (double)fp[m];
     iso /= r.M;
-    out[it] = 2.0 * r.ec[it % r.E].egrid * iso * r.f_unscale;
+    if (sizeof(Real) == 4) iso = ldexp(iso, -(int)r.fexp[it]);  // the row's exponent
+    out[it] = 2.0 * r.ec[it % r.E].egrid * iso;
   }
 }
 
-// double staging buffer <-> device f (float in the FP32 form, shifted by a
-// power of two: scaling is exact, the float rounding is the same)
-__global__ void k_f64_to_f32(const double *src, float *dst, size_t n, double scale) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+// FP64 rows (host values) <-> the FP32 form's rows with their exponents: a
+// row's exponent brings its largest value to [2^kRowTop, 2^(kRowTop+1));
+// scaling by a power of two is exact, so the float rounding is the plain one.
+__global__ void k_rows_to_f32(const double *src, float *dst, short *xp, size_t nrows, int M) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nrows;
        i += (size_t)gridDim.x * blockDim.x) {
-    float v = (float)(src[i] * scale);
-    dst[i] = v < FLT_MIN ? FLT_MIN : v;
+    const double *a = src + i * M;
+    double mx = 0.0;
+    for (int m = 0; m < M; ++m) mx = fmax(mx, a[m]);
+    const int x = mx > 0.0 ? row_exp_for(ilogb(mx)) : 0;
+    float *b = dst + i * M;
+    for (int m = 0; m < M; ++m) {
+      const float v = (float)ldexp(a[m], x);
+      b[m] = v < FLT_MIN ? FLT_MIN : v;
+    }
+    xp[i] = (short)x;
   }
 }
-__global__ void k_f32_to_f64(const float *src, double *dst, size_t n, double unscale) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = (double)src[i] * unscale;
+__global__ void k_rows_to_f64(const float *src, const short *xp, double *dst, size_t nrows,
+                              int M) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nrows;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int x = xp[i];
+    for (int m = 0; m < M; ++m) dst[i * M + m] = ldexp((double)src[i * M + m], -x);
+  }
 }
 
 static int grid_for(size_t n) {
@@ -198,15 +211,16 @@ int launch_omni_flux(const RunView &r, double *out, cudaStream_t st, uint64_t *l
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
-// to_device_real: staging (double) -> f (float); else f (float) -> staging.
-int launch_convert_f(const RunView &r, const double *src64, double *dst64, int to_device_real,
-                     size_t count, cudaStream_t st, uint64_t *launches) {
-  if (to_device_real)
-    k_f64_to_f32<<<grid_for(count), 256, 0, st>>>(src64, reinterpret_cast<float *>(dst64), count,
-                                                  r.f_scale);
+// FP32 form: rows [row0, row0 + nrows) of the view between FP64 staging and
+// the device's rows.  to_device: staging -> f; else f -> staging.
+int launch_convert_f(const RunView &r, size_t row0, size_t nrows, double *stage, int to_device,
+                     cudaStream_t st, uint64_t *launches) {
+  float *f = reinterpret_cast<float *>(r.f) + row0 * r.M;
+  short *xp = r.fexp + row0;
+  if (to_device)
+    k_rows_to_f32<<<grid_for(nrows), 256, 0, st>>>(stage, f, xp, nrows, r.M);
   else
-    k_f32_to_f64<<<grid_for(count), 256, 0, st>>>(reinterpret_cast<const float *>(src64), dst64,
-                                                  count, r.f_unscale);
+    k_rows_to_f64<<<grid_for(nrows), 256, 0, st>>>(f, xp, stage, nrows, r.M);
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
@@ -216,7 +230,8 @@ int launch_convert_f(const RunView &r, const double *src64, double *dst64, int t
 // stream's template row (the reference's INNER_SHELL).  A thread owns one
 // (stream, energy, mu) cell and walks the nodes outward-in, reading a batch
 // of nodes before writing them, so every value is read before it is
-// overwritten; tmpl: S*E*M doubles, converted like an upload.
+// overwritten; in the FP32 form the mu = 0 thread moves the row's exponent
+// alike.  tmpl: S*E*M doubles; node 0's rows are written by k_ripple_rows.
 template <typename Real>
 __global__ void k_ripple_f(RunView r, const double *tmpl) {
   const size_t EM = (size_t)r.E * r.M;
@@ -225,26 +240,57 @@ __global__ void k_ripple_f(RunView r, const double *tmpl) {
        c += (size_t)gridDim.x * blockDim.x) {
     const size_t s = c / EM, j = c - s * EM;
     Real *p = reinterpret_cast<Real *>(r.f) + s * r.N * EM + j;
+    const bool xrow = sizeof(Real) == 4 && j % r.M == 0;
+    short *xp = xrow ? r.fexp + s * r.N * r.E + j / r.M : nullptr;
     for (int k = r.N - 1; k >= 1; k -= 8) {
       const int cnt = k < 8 ? k : 8;
       Real v[8];
+      short x[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u)
-        if (u < cnt) v[u] = p[(size_t)(k - 1 - u) * EM];
+        if (u < cnt) {
+          v[u] = p[(size_t)(k - 1 - u) * EM];
+          if (xrow) x[u] = xp[(size_t)(k - 1 - u) * r.E];
+        }
 #pragma unroll
       for (int u = 0; u < 8; ++u)
-        if (u < cnt) p[(size_t)(k - u) * EM] = v[u];
+        if (u < cnt) {
+          p[(size_t)(k - u) * EM] = v[u];
+          if (xrow) xp[(size_t)(k - u) * r.E] = x[u];
+        }
     }
-    p[0] = to_real<Real>(tmpl[c] * r.f_scale);
+    if (sizeof(Real) == 8) p[0] = (Real)tmpl[c];
+  }
+}
+
+// Node 0's rows from the template (FP32 form), after k_ripple_f.
+__global__ void k_ripple_rows(RunView r, const double *tmpl) {
+  const size_t rows = (size_t)r.S * r.E;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < rows;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = i / r.E, e = i - s * r.E;
+    const double *a = tmpl + i * r.M;
+    double mx = 0.0;
+    for (int m = 0; m < r.M; ++m) mx = fmax(mx, a[m]);
+    const int x = mx > 0.0 ? row_exp_for(ilogb(mx)) : 0;
+    float *b = reinterpret_cast<float *>(r.f) + (s * r.N * r.E + e) * r.M;
+    for (int m = 0; m < r.M; ++m) {
+      const float v = (float)ldexp(a[m], x);
+      b[m] = v < FLT_MIN ? FLT_MIN : v;
+    }
+    r.fexp[s * r.N * r.E + e] = (short)x;
   }
 }
 
 int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint64_t *launches) {
   const size_t cells = (size_t)r.S * r.E * r.M;
-  if (r.precision == EPREM_FP64)
+  if (r.precision == EPREM_FP64) {
     k_ripple_f<double><<<grid_for(cells), 256, 0, st>>>(r, tmpl);
-  else
+  } else {
     k_ripple_f<float><<<grid_for(cells), 256, 0, st>>>(r, tmpl);
+    k_ripple_rows<<<grid_for((size_t)r.S * r.E), 256, 0, st>>>(r, tmpl);
+    *launches += 1;
+  }
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
@@ -271,8 +317,10 @@ __global__ void k_seed_population(RunView r, unsigned long long seed, double per
       for (int m = 0; m < r.M; m++) row[m] = v;
     } else {
       float *row = reinterpret_cast<float *>(r.f) + i * r.M;
-      const float vf = to_real<float>(v);
+      const int x = row_exp_for(ilogb(v));
+      const float vf = to_real<float>(ldexp(v, x));
       for (int m = 0; m < r.M; m++) row[m] = vf;
+      r.fexp[i] = (short)x;
     }
   }
 }

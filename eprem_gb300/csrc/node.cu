@@ -319,9 +319,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       n_c[tid] = dlnndt;
       n_d[tid] = (dlnndt < 0) ? 1.0 - r.damp_cooling : 1.0;
       const double radial = r.seed_radial[g];
-      // ln of the seeds in f's own units (ln f itself in the FP32 form)
-      n_bc0[tid] = log(seed_value(r, r.ec[0], radial)) - r.ln_f_shift;
-      n_bc1[tid] = log(seed_value(r, r.ec[E - 1], radial)) - r.ln_f_shift;
+      n_bc0[tid] = log(seed_value(r, r.ec[0], radial));
+      n_bc1[tid] = log(seed_value(r, r.ec[E - 1], radial));
       vmax_bits[tid] = 0ull;
     }
     __syncthreads();
@@ -386,11 +385,14 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       Real *col = slab + (size_t)g * EM + m;  // stride M
       const double *vcol = vf + (size_t)g * F + m;  // face e at vcol[e*M]
       const Real bc0 = (Real)n_bc0[g], bc1 = (Real)n_bc1[g];
-      const Real lns = (Real)r.ln_f_shift;  // 0 in FP64
+      // FP32 form: ln f itself is ln(stored) - fexp ln 2 (the row's exponent)
+      const short *xrow = (sizeof(Real) == 4) ? r.fexp + (g0 + g) * E : nullptr;
       Real fc[P];
 #pragma unroll
       for (int e = 0; e < P; ++e)
-        if (e < E) fc[e] = log_r<Real>(col[e * M]) - lns;
+        if (e < E)
+          fc[e] = log_r<Real>(col[e * M]) -
+                  (xrow ? (Real)xrow[e] * (Real)0.69314718055994530942 : (Real)0);
       if (ns > 0 && alg == 1) {
         // Euler upwind in ln p, faces pre-scaled by dt_sub/dlnp; the end cells
         // use the reference's one-sided forms with the seed on inflow.
@@ -422,20 +424,52 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
         line_rk3<Real, P>(fl, va, E, ns, (Real)n_dts[g], true, alg, (Real)r.dlnp, bc0, bc1);
         for (int e = 0; e < E; ++e) fc[e] = fl[e];
       }
-      int code = 0;
+      if constexpr (sizeof(Real) == 4) {
+        // ln f stays in the slab; the row pass below renormalises and exponentiates
 #pragma unroll
-      for (int e = 0; e < P; ++e) {
-        if (e < E) {
-          Real v = exp_r<Real>(fc[e] + lns);
-          if (bad_value(v, &code)) {
-            const size_t gg = g0 + g;
-            set_error(r, code, 3, (int)(gg / N), (int)(gg % N), e, m);
+        for (int e = 0; e < P; ++e)
+          if (e < E) col[e * M] = fc[e];
+      } else {
+        int code = 0;
+#pragma unroll
+        for (int e = 0; e < P; ++e) {
+          if (e < E) {
+            Real v = exp_r<Real>(fc[e]);
+            if (bad_value(v, &code)) {
+              const size_t gg = g0 + g;
+              set_error(r, code, 3, (int)(gg / N), (int)(gg % N), e, m);
+            }
+            col[e * M] = v < fl_min ? fl_min : v;
           }
-          col[e * M] = v < fl_min ? fl_min : v;
         }
       }
     }
     __syncthreads();
+    if constexpr (sizeof(Real) == 4) {
+      // FP32 form: each changed row gets the exponent that brings its largest
+      // value to [2^kRowTop, 2^(kRowTop+1))
+      for (int it = tid; it < Gv * E; it += kNodeThreads) {
+        const int g = it / E, e = it % E;
+        if (!n_ok[g]) continue;
+        Real *row = slab + (size_t)g * EM + e * M;
+        Real mx = row[0];
+        for (int m = 1; m < M; ++m) mx = fmaxf(mx, row[m]);
+        const float l2 = fminf(fmaxf(floorf(mx * 1.4426950408889634f), -1.0e6f), 1.0e6f);
+        const int xn = clamp_exp(kRowTop - (int)l2);
+        const float add = (float)xn * 0.6931471805599453f;
+        int code = 0;
+        for (int m = 0; m < M; ++m) {
+          const float v = expf(row[m] + add);
+          if (bad_value(v, &code)) {
+            const size_t gg = g0 + g;
+            set_error(r, code, 3, (int)(gg / N), (int)(gg % N), e, m);
+          }
+          row[m] = v < fl_min ? fl_min : v;
+        }
+        r.fexp[(g0 + g) * E + e] = (short)xn;
+      }
+      __syncthreads();
+    }
   }
   for (int i = tid; i < Gv * EM; i += kNodeThreads) fg[i] = slab[i];
 }

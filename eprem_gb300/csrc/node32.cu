@@ -20,9 +20,9 @@
 //   * k_focus32, every EP sub-step: one thread per (node, energy) row, its M
 //     cells and the split face coefficients max(q,0), min(q,0) in registers
 //     (the CTA's rows staged through shared memory with coalesced copies);
-//   * k_change32, every EP sub-step: one thread per (node, mu) column (a warp
-//     reads 32 consecutive mu of one energy: coalesced), ln f in shared
-//     memory.
+//   * k_change32, every EP sub-step: one thread per (node, mu) column, whole
+//     nodes per CTA (a warp reads consecutive mu of one energy: coalesced),
+//     ln f in shared memory, each row renormalised to its own exponent.
 // No block barriers on the sub-cycle paths.  Only the
 // Euler upwind algorithm (alg 1) runs here; RK3 / WENO3 use node.cu.
 #include "common.cuh"
@@ -146,13 +146,16 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
       c.dlnn = (float)dlnn;
       c.scale_c = (float)((dt / ns_c) / r.dlnp);
       if (lane < 2) {
-        const double radial = r.seed_radial[g];
-        // ln of the seed itself (f is held shifted; see kF32Shift)
-        const float lbc =
-            (float)(log(seed_value(r, r.ec[lane ? E - 1 : 0], radial)) - r.ln_f_shift);
-        const float other = __shfl_down_sync(0x3u, lbc, 1);
-        c.bc0 = lbc;
-        c.bc1 = other;
+        // ln seed = kb ln 2 + ln(seed 2^-kb), the integer part of log2 apart
+        const double sv = seed_value(r, r.ec[lane ? E - 1 : 0], r.seed_radial[g]);
+        const int kb = ilogb(sv);
+        const float fb = (float)log(ldexp(sv, -kb));
+        const float fo = __shfl_down_sync(0x3u, fb, 1);
+        const int ko = __shfl_down_sync(0x3u, kb, 1);
+        c.bc0 = fb;
+        c.bc1 = fo;
+        c.kbc0 = kb;
+        c.kbc1 = ko;
       }
     }
     c.ns_f = ns_f;
@@ -286,32 +289,60 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
 }
 
 // ---- adiabatic change: one (node, mu) column per thread --------------------
-// ln f of the column lives in shared memory, [e][thread] (conflict-free); the
-// change takes one or two sub-cycles per step, so its cost is the log / exp
-// per cell, and a register column would only buy spills.
-__global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
-  extern __shared__ float lnf[];  // [E][kChangeThreads]
-  const int E = r.E, M = r.M, N = r.N;
+// A CTA holds whole nodes (npc = max(1, 128 / M) of them on npc * M threads)
+// so that, after the sub-cycles, it can renormalise every row it writes.
+// ln f of the columns lives in shared memory, [e][thread] (conflict-free), as
+// delta = ln(stored value); row e's true ln f is delta + c_e with
+// c_e = -fexp[e] ln 2.  The reference's flux-form update
+//   l_e -= q_n l_a - q_p l_b   (a, b the upwind cells of faces e+1/2, e-1/2)
+// is not invariant under a shift of l (q_n != q_p), so in delta it reads
+//   delta_e -= q_n delta_a - q_p delta_b
+//              + q_n (c_a - c_e) - q_p (c_b - c_e) + c_e (q_n - q_p),
+// the exponent differences c_a - c_e formed from integers and
+// q_n - q_p = dt_sub/dlnp cool am (1/v_{e+1} - 1/v_{e-1}) / 2 from the FP64
+// difference of the grid (the bm part of the velocity cancels): no float
+// rounding sees the size of ln f itself except through that small velocity
+// difference.  The one-sided end cells and the Dirichlet seeds take the
+// same exponent differences.  The change takes one or two sub-cycles per
+// step, so its cost is the log / exp per cell (hardware approximations, ~1e-6
+// relative on f).
+__global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc) {
+  extern __shared__ float sm[];
+  constexpr float kLn2 = 0.6931471805599453f;
+  const int E = r.E, M = r.M;
+  const int T = npc * M;  // live threads of the CTA
   const int tid = threadIdx.x;
-  const size_t cols = (size_t)r.S * N * M;
-  const size_t it = (size_t)blockIdx.x * kChangeThreads + tid;
-  if (it >= cols) return;
-  const size_t g = it / M;
-  const int m = (int)(it - g * M);
-  const NodeCoef32 c = r.coef32[g];
-  if (!c.ok) return;
-  float *col = reinterpret_cast<float *>(r.f) + g * E * M + m;  // stride M
-  float *fc = lnf + tid;                                       // stride kChangeThreads
-  constexpr int T = kChangeThreads;
-  const float lns = (float)r.ln_f_shift;  // the shift of the FP32 store, off ln f
-  // the hardware approximations: ~1e-6 absolute on ln f, i.e. ~1e-6
-  // relative on f, far inside the FP32 form's 1e-3 flux tolerance
-  for (int e = 0; e < E; ++e) fc[e * T] = __logf(col[e * M]) - lns;
-  if (c.ns_c > 0) {
+  const int j = tid / M, m = tid - (tid / M) * M;
+  const size_t SN = (size_t)r.S * r.N;
+  const size_t g = (size_t)blockIdx.x * npc + j;
+  float *lnf = sm;                                             // [E][T]
+  int *xs = reinterpret_cast<int *>(sm + (size_t)E * T);     // [npc][E] row exponents
+  int *sh = xs + npc * E;                                      // [npc][E] renormalising shifts
+  for (int i = tid; i < npc * E; i += blockDim.x) {
+    const size_t gg = (size_t)blockIdx.x * npc + i / E;
+    xs[i] = gg < SN ? r.fexp[gg * E + i % E] : 0;
+  }
+  bool ok = false;
+  NodeCoef32 c{};
+  if (tid < T && g < SN) {
+    c = r.coef32[g];
+    ok = c.ok != 0;  // the spawn node is not changed
+  }
+  float *col = reinterpret_cast<float *>(r.f) + (ok ? g : 0) * E * M + m;  // stride M
+  float *fc = lnf + tid;                                                    // stride T
+  if (ok)
+    for (int e = 0; e < E; ++e) fc[e * T] = __logf(col[e * M]);
+  __syncthreads();
+  if (ok && c.ns_c > 0) {
+    const int *x = xs + j * E;
     const float mu = r.mugrid32[m];
     const float am = -mu * c.dupar;
     const float bm = mu * mu * (c.dlnn - c.dlnb) + 0.5f * (1.f - mu * mu) * c.dlnb;
-    const float cool = c.cool, sc = c.scale_c, bc0 = c.bc0, bc1 = c.bc1;
+    const float cool = c.cool, sc = c.scale_c;
+    const float hq = sc * 0.5f * cool * am;  // q_n - q_p = hq (1/v_{e+1} - 1/v_{e-1})
+    // the seeds relative to the first and last rows' exponents
+    const float bc0 = c.bc0 + (float)(c.kbc0 + x[0]) * kLn2;
+    const float bc1 = c.bc1 + (float)(c.kbc1 + x[E - 1]) * kLn2;
     const EnergyConsts *ec = r.ec;
     for (int s = 0; s < c.ns_c; ++s) {
       // face e lies between energies e-1 and e: q = dt_sub/dlnp times the
@@ -319,9 +350,11 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
       float vel_lo = cool * (am * ec[0].vi32 + bm);
       float vel_hi = cool * (am * ec[1].vi32 + bm);
       const float q1 = sc * 0.5f * (vel_hi + vel_lo);
-      float f0 = fc[0], f1 = fc[T];
+      const float f0 = fc[0], f1 = fc[T];
+      float dprev = (float)(x[0] - x[1]) * kLn2;  // c_1 - c_0
       float gprev = q1 * (q1 >= 0.f ? f0 : f1);
-      const float d0 = (q1 <= 0.f) ? q1 * (f1 - f0) : q1 * (f0 - bc0);
+      float cprev = q1 >= 0.f ? q1 * dprev : 0.f;  // -q_p (c_b - c_e) of the next cell
+      const float d0 = (q1 <= 0.f) ? q1 * (f1 - f0 + dprev) : q1 * (f0 - bc0);
       float fold_prev = f0;
       fc[0] = f0 - d0;
       float qcur = q1, fe = f1;
@@ -330,23 +363,43 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r) {
         vel_hi = cool * (am * ec[e + 1].vi32 + bm);
         const float qq = sc * 0.5f * (vel_hi + vel_lo);
         const float fn = fc[(e + 1) * T];
+        const float dn = (float)(x[e] - x[e + 1]) * kLn2;  // c_{e+1} - c_e
         const float gnext = qq * (qq >= 0.f ? fe : fn);
+        const float corr =
+            (qq < 0.f ? qq * dn : 0.f) + cprev - ((float)x[e] * kLn2) * (hq * ec[e].dvi32);
         fold_prev = fe;
-        fc[e * T] = fe - (gnext - gprev);
+        fc[e * T] = fe - (gnext - gprev) - corr;
         gprev = gnext;
+        cprev = qq >= 0.f ? qq * dn : 0.f;
         qcur = qq;
         fe = fn;
+        dprev = dn;
       }
       // last energy (e = E-1): upwind from below, or the Dirichlet seed above
-      const float dl = (qcur >= 0.f) ? qcur * (fe - fold_prev) : qcur * (bc1 - fe);
+      const float dl = (qcur >= 0.f) ? qcur * (fe - fold_prev + dprev) : qcur * (bc1 - fe);
       fc[(E - 1) * T] = fe - dl;
     }
   }
-  int code = 0;
-  for (int e = 0; e < E; ++e) {
-    const float v = __expf(fc[e * T] + lns);
-    if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / N), (int)(g % N), e, m);
-    col[e * M] = v < FLT_MIN ? FLT_MIN : v;
+  __syncthreads();
+  // each row's new exponent: its largest value to [2^kRowTop, 2^(kRowTop+1))
+  if (ok)
+    for (int e = m; e < E; e += M) {
+      const float *rowp = lnf + (size_t)e * T + j * M;
+      float mx = rowp[0];
+      for (int mm = 1; mm < M; ++mm) mx = fmaxf(mx, rowp[mm]);
+      const float l2 = fminf(fmaxf(floorf(mx * 1.4426950408889634f), -1.0e6f), 1.0e6f);
+      const int x0 = xs[j * E + e];
+      sh[j * E + e] = clamp_exp(x0 + kRowTop - (int)l2) - x0;
+    }
+  __syncthreads();
+  if (ok) {
+    int code = 0;
+    for (int e = 0; e < E; ++e) {
+      const float v = __expf(fc[e * T] + (float)sh[j * E + e] * kLn2);
+      if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / r.N), (int)(g % r.N), e, m);
+      col[e * M] = v < FLT_MIN ? FLT_MIN : v;
+    }
+    for (int e = m; e < E; e += M) r.fexp[g * E + e] = (short)(xs[j * E + e] + sh[j * E + e]);
   }
 }
 
@@ -386,10 +439,12 @@ static void launch_focus_t(const RunView &r, cudaStream_t st) {
 }
 
 static void launch_change(const RunView &r, cudaStream_t st) {
-  const size_t cols = (size_t)r.S * r.N * r.M;
-  const size_t smem = (size_t)r.E * kChangeThreads * sizeof(float);
-  k_change32<<<(unsigned)((cols + kChangeThreads - 1) / kChangeThreads), kChangeThreads, smem,
-               st>>>(r);
+  const int npc = r.M >= kChangeThreads ? 1 : kChangeThreads / r.M;
+  const size_t SN = (size_t)r.S * r.N;
+  const size_t smem = (size_t)r.E * npc * r.M * sizeof(float) + 2 * (size_t)npc * r.E * sizeof(int);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_change32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_change32<<<(unsigned)((SN + npc - 1) / npc), kChangeThreads, smem, st>>>(r, npc);
 }
 
 #define EPREM_P_SWITCH(p, F, ...)      \

@@ -38,6 +38,7 @@ struct eprem_gpu_run {
   int m0 = 0;
   double norm_radius = 0, neg_beta = 0;
   void *d_f = nullptr;
+  short *d_fexp = nullptr;  // FP32 form: row exponents [S][N][E]
   double *d_nodes = nullptr, *d_mugrid = nullptr;
   float *d_mugrid32 = nullptr;
   eprem::NodeCoef32 *d_coef32 = nullptr;
@@ -63,6 +64,7 @@ struct eprem_gpu_run {
   int *d_news = nullptr, *d_shell_ent = nullptr;
   void *d_shell_del = nullptr;    // Real[N][E][S][5]
   void *d_shell_f = nullptr;      // Real[S][N][E][M]
+  short *d_shell_fexp = nullptr;  // FP32 form: its row exponents
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch
   bool timing = false;

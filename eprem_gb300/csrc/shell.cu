@@ -62,13 +62,18 @@ __global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, Real 
           __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(r.dt, 0.33333333), mfp), r.ec[e].vgrid), kperxkpar);
       Real *out = del + (((size_t)k * r.E + e) * r.S + s) * 5;
       double sum = 0.0;
+      Real rsum = Real(0);
       for (int d = 0; d < 4; d++) {
         double v = dt_kper / __dadd_rn(__dmul_rn(dlper[d], dlper[d]), kVerySmall);
         if (v > 0.025) v = 0.025;
         out[d] = (Real)v;
         sum = d == 0 ? v : __dadd_rn(sum, v);
+        rsum = d == 0 ? out[d] : rsum + out[d];
       }
-      out[4] = (Real)sum;
+      // FP64: the reference's sum.  FP32: the sum of the rounded fractions in
+      // the same order, so that a node's loss is its neighbours' gains up to
+      // the rounding of the accumulation
+      out[4] = sizeof(Real) == 8 ? (Real)sum : rsum;
     }
   }
 }
@@ -124,10 +129,17 @@ __device__ __forceinline__ void st_vec(Real *p, const Real (&x)[V]) {
 // two places of the slice blockDim apart ((stream, mu) stepped by counters,
 // no divisions), and issues every load of a chunk of C list entries before
 // the ordered sums.
+// FP32 form: the terms of a target row come from rows with their own
+// exponents.  The new row's exponent is the target's, lowered where a gain
+// could otherwise leave the float range: a source row's values lie below
+// 2^(kRowTop+7) in its own scale (normalised, then focused at most M-fold),
+// so a gain a f_i stays below 2^120 in an exponent no higher than
+// fexp_i + 17 - log2(a).  Every term is taken to that exponent (exact powers
+// of two) before the sum; xout receives it.
 template <typename Real, int C, int V>
 __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
     k_shell_diffuse(RunView r, const int *__restrict__ ent, int L, const Real *__restrict__ del,
-                    Real *__restrict__ out) {
+                    Real *__restrict__ out, short *__restrict__ xout) {
   const Real *__restrict__ f = static_cast<const Real *>(r.f);
   const int M = r.M, S = r.S, E = r.E;
   const int MV = M / V;      // V-cell groups per row
@@ -164,6 +176,23 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
       for (int u = 0; u < 2; u++)
 #pragma unroll
         for (int j = 0; j < V; j++) acc[u][j] = Real(0);
+      int xt[2] = {0, 0}, xn[2] = {0, 0};  // FP32 form: target's exponent, new exponent
+      if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          xt[u] = r.fexp[((size_t)s[u] * r.N + k) * E + e];
+          int b = xt[u];
+          for (int p = 0; k > 0 && p < L; ++p) {
+            const int cd = __ldg(ent + s[u] * L + p);
+            if (cd < 0 || (cd & 7) >= 4) continue;
+            const float a = (float)__ldg(dsl + (cd >> 3) * 5 + (cd & 7));
+            if (!(a > 0.f)) continue;
+            const int xi = r.fexp[((size_t)(cd >> 3) * r.N + k) * E + e];
+            b = min(b, xi + 17 - ilogb_f(a));
+          }
+          xn[u] = b < xt[u] ? clamp_exp(b) : xt[u];
+        }
+      }
       for (int p0 = 0; k > 0 && p0 < L; p0 += C) {
         int code[2][C];
         Real a[2][C], fi[2][C][V];
@@ -183,6 +212,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
               const int i = code[u][q] >> 3;
               a[u][q] = __ldg(dsl + i * 5 + (code[u][q] & 7));
               ld_vec<V>(f + (size_t)i * per_stream + row + (size_t)m[u] * V, fi[u][q]);
+              if constexpr (sizeof(Real) == 4)  // the source row taken to the new exponent
+                a[u][q] = ldexp_f(a[u][q], xn[u] - r.fexp[((size_t)i * r.N + k) * E + e]);
             }
           }
 #pragma unroll
@@ -203,6 +234,12 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
         const size_t gi = (size_t)s[u] * per_stream + row + (size_t)m[u] * V;
         Real v[V];
         ld_vec<V>(f + gi, v);
+        if constexpr (sizeof(Real) == 4) {
+          if (xn[u] != xt[u])
+#pragma unroll
+            for (int j = 0; j < V; j++) v[j] = ldexp_f(v[j], xn[u] - xt[u]);
+          if (m[u] == 0) xout[((size_t)s[u] * r.N + k) * E + e] = (short)xn[u];
+        }
         if (k > 0) {
 #pragma unroll
           for (int j = 0; j < V; j++) {
@@ -232,27 +269,27 @@ int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void 
 
 template <typename Real>
 static void shell_diffuse_as(const RunView &r, const int *ent, int L, const void *del,
-                             void *out, int blocks, cudaStream_t st) {
+                             void *out, short *xout, int blocks, cudaStream_t st) {
   const Real *d = (const Real *)del;
   Real *o = (Real *)out;
   const bool pairs = r.M % 2 == 0;
   if (L <= 5 && pairs)
-    k_shell_diffuse<Real, 5, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+    k_shell_diffuse<Real, 5, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else if (L <= 5)
-    k_shell_diffuse<Real, 5, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+    k_shell_diffuse<Real, 5, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else if (pairs)
-    k_shell_diffuse<Real, 8, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+    k_shell_diffuse<Real, 8, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else
-    k_shell_diffuse<Real, 8, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o);
+    k_shell_diffuse<Real, 8, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
 }
 
 int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
-                         cudaStream_t st, uint64_t *launches) {
+                         short *xout, cudaStream_t st, uint64_t *launches) {
   const int blocks = std::min(r.N * r.E, 152 * 8);
   if (r.precision == EPREM_FP32)
-    shell_diffuse_as<float>(r, ent, L, del, out, blocks, st);
+    shell_diffuse_as<float>(r, ent, L, del, out, xout, blocks, st);
   else
-    shell_diffuse_as<double>(r, ent, L, del, out, blocks, st);
+    shell_diffuse_as<double>(r, ent, L, del, out, nullptr, blocks, st);
   ++*launches;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

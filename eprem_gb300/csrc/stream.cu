@@ -11,11 +11,10 @@
 //     store -- fills before the sub-cycle's barrier.  The inner loop therefore
 //     only ever loads from local shared memory;
 //   * the isotropisation mean over mu is a register sum in the owning thread.
-// The upwind coefficients mult*del_fac are fixed for the slab: the FP32 form
-// keeps them in registers, the FP64 form (bound by the FP64 pipe, next to
-// which shared-memory loads cost nothing) in shared memory.  A second FP32
-// shape keeps them in shared memory so that 1024 threads -- a whole 1000-node
-// stream -- fit one CTA without a cluster.
+// The upwind coefficients mult*del_fac are fixed for the slab and held in
+// shared memory (the FP64 form is bound by the FP64 pipe, next to which
+// shared-memory loads cost nothing).  This is the plain FP64 form's kernel;
+// the FP32 form streams with stream2.cu.
 // seedPopulationCheck (src/energeticParticlesBoundary.c:28-59) is applied as
 // the slab is loaded; thinned-out nodes receive their reference node's values
 // on write-back, as the reference's shellRef copy does (:2448-2455).
@@ -28,8 +27,7 @@ namespace cg = cooperative_groups;
 
 namespace eprem {
 
-// Threads per CTA (multiples of 128, the register-allocation granule) for
-// register-held coefficients (FP32) and shared-memory coefficients.
+// Threads per CTA (multiples of 128, the register-allocation granule).
 template <typename Real, int MMAX, bool RegCoef> struct StreamShape;
 #define EPREM_STREAM_SHAPE(R, MM, RC, TT) \
   template <> struct StreamShape<R, MM, RC> { static constexpr int T = TT; };
@@ -40,20 +38,6 @@ EPREM_STREAM_SHAPE(double, 32, false, 512)
 EPREM_STREAM_SHAPE(double, 40, false, 512)
 EPREM_STREAM_SHAPE(double, 48, false, 384)
 EPREM_STREAM_SHAPE(double, 64, false, 384)
-EPREM_STREAM_SHAPE(float, 8, true, 1024)
-EPREM_STREAM_SHAPE(float, 16, true, 768)
-EPREM_STREAM_SHAPE(float, 24, true, 512)
-EPREM_STREAM_SHAPE(float, 32, true, 512)
-EPREM_STREAM_SHAPE(float, 40, true, 512)
-EPREM_STREAM_SHAPE(float, 48, true, 384)
-EPREM_STREAM_SHAPE(float, 64, true, 384)
-EPREM_STREAM_SHAPE(float, 8, false, 1024)
-EPREM_STREAM_SHAPE(float, 16, false, 1024)
-EPREM_STREAM_SHAPE(float, 24, false, 1024)
-EPREM_STREAM_SHAPE(float, 32, false, 1024)
-EPREM_STREAM_SHAPE(float, 40, false, 1024)
-EPREM_STREAM_SHAPE(float, 48, false, 768)
-EPREM_STREAM_SHAPE(float, 64, false, 512)
 #undef EPREM_STREAM_SHAPE
 
 // Shared memory of one CTA: coefficient table (shared-coefficient shapes) and
@@ -279,41 +263,27 @@ static int threads_for(int mmax) {
   }
 }
 
-// variant: 0 automatic, 1 coefficients in registers, 2 in shared memory,
-// 3 several list nodes per thread (stream2.cu), 4 the same with packed fp32x2
-// arithmetic (an odd mu half padded with a zero cell), 5 as 4 with the cell guards
-// resolved at compile time (M fills its bin, m0 = M/2).  The automatic FP32
-// choice is the first of 5, 4, 3 that fits.  The FP64 form always keeps the
-// coefficients in shared memory.
+// variant: 0 automatic; FP32 form (stream2.cu): 3 several list nodes per
+// thread, 4 the same with packed fp32x2 arithmetic (an odd mu half padded
+// with a zero cell), 5 as 4 with the cell guards resolved at compile time (M
+// fills its bin, m0 = M/2) -- the automatic choice is the first of 5, 4, 3
+// that fits.  The FP64 form has one shape (k_stream, coefficients in shared
+// memory); variants 1 and 2 name it there.
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
-  if (precision == EPREM_FP32 && (variant == 0 || variant == 5) &&
-      plan_stream2(N, M, m0, true, true, plan) == 0)
-    return 0;
-  if (precision == EPREM_FP32 && (variant == 0 || variant == 4) &&
-      plan_stream2(N, M, m0, true, false, plan) == 0)
-    return 0;
-  if (precision == EPREM_FP32 && (variant == 0 || variant == 3) &&
-      plan_stream2(N, M, m0, false, false, plan) == 0)
-    return 0;
+  if (precision == EPREM_FP32) {
+    if ((variant == 0 || variant == 5) && plan_stream2(N, M, m0, true, true, plan) == 0) return 0;
+    if ((variant == 0 || variant == 4) && plan_stream2(N, M, m0, true, false, plan) == 0) return 0;
+    if ((variant == 0 || variant == 3) && plan_stream2(N, M, m0, false, false, plan) == 0) return 0;
+    return EPREM_GPU_ERR_ARG;
+  }
+  if (variant > 2) return EPREM_GPU_ERR_ARG;
   int mmax = 0;
   for (int b : kStreamBins)
     if (M <= b) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
   plan->mmax = mmax;
-  bool reg;
-  if (precision == EPREM_FP64) {
-    reg = false;
-  } else if (variant == 1) {
-    reg = true;
-  } else if (variant == 2) {
-    reg = false;
-  } else {
-    reg = N > threads_for<float, false>(mmax);  // unreachable: variant 0 goes to stream2
-  }
-  plan->reg_coef = reg ? 1 : 0;
-  plan->threads = precision == EPREM_FP64 ? threads_for<double, false>(mmax)
-                  : reg                   ? threads_for<float, true>(mmax)
-                                          : threads_for<float, false>(mmax);
+  plan->reg_coef = 0;
+  plan->threads = threads_for<double, false>(mmax);
   plan->cluster = (N + plan->threads - 1) / plan->threads;
   if (plan->cluster > 8) return EPREM_GPU_ERR_ARG;  // portable cluster limit
   return 0;
@@ -359,25 +329,18 @@ static cudaError_t dispatch_mmax(const RunView &r, const StreamPlan &pl, int m0,
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches) {
   if (plan.reg_coef == 2) return launch_stream2(r, plan, m0, st, launches);
-  cudaError_t err;
-  if (r.precision == EPREM_FP64)
-    err = dispatch_mmax<double, false>(r, plan, m0, st);
-  else if (plan.reg_coef)
-    err = dispatch_mmax<float, true>(r, plan, m0, st);
-  else
-    err = dispatch_mmax<float, false>(r, plan, m0, st);
+  if (r.precision != EPREM_FP64) return EPREM_GPU_ERR_ARG;
+  const cudaError_t err = dispatch_mmax<double, false>(r, plan, m0, st);
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches) {
+  if (r.precision == EPREM_FP32) return launch_seed_check32(r, st, launches);
   const size_t items = (size_t)r.S * r.N * r.E;
   int blocks = (int)((items + 255) / 256);
   if (blocks > 152 * 32) blocks = 152 * 32;
-  if (r.precision == EPREM_FP64)
-    k_seed_check<double><<<blocks, 256, 0, st>>>(r);
-  else
-    k_seed_check<float><<<blocks, 256, 0, st>>>(r);
+  k_seed_check<double><<<blocks, 256, 0, st>>>(r);
   *launches += 1;
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

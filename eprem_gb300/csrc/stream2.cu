@@ -39,6 +39,46 @@ template <> struct Stream2Shape<40> { static constexpr int T = 256, NPT = 4; };
 template <> struct Stream2Shape<48> { static constexpr int T = 256, NPT = 3; };
 template <> struct Stream2Shape<64> { static constexpr int T = 256, NPT = 2; };
 
+// The common exponent of a (stream, energy) slab (FP32 row exponents): the
+// largest true value of its rows, and of the seeds the sub-step can write,
+// brought to [2^kRowTop, 2^(kRowTop+1)).  lg: this thread's largest
+// floor(log2) of a true value; red: W + 1 ints of shared memory.  A cluster's
+// CTAs combine their maxima through distributed shared memory (the slot read
+// remotely is written once per launch, and the kernel ends in a cluster
+// barrier, so no CTA leaves while it is read).
+template <int T>
+__device__ __forceinline__ int slab_exp(int lg, int *red, cg::cluster_group &cluster, int C) {
+  constexpr int W = T / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  lg = __reduce_max_sync(0xffffffffu, lg);
+  if (lane == 0) red[warp] = lg;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = red[0];
+    for (int w = 1; w < W; ++w) m = max(m, red[w]);
+    red[W] = m;
+  }
+  if (C > 1)
+    cluster.sync();
+  else
+    __syncthreads();
+  int m = red[W];
+  for (int c = 0; c < C && C > 1; ++c) m = max(m, cluster.map_shared_rank(red, c)[W]);
+  return row_exp_for(m);
+}
+
+// The two power-of-two factors of ldexp_f(x, k), formed once for a row.
+struct Pow2Pair {
+  float a, b;
+};
+__device__ __forceinline__ Pow2Pair pow2_pair(int k) {
+  const int k1 = k > 127 ? 127 : (k < -126 ? -126 : k);
+  int k2 = k - k1;
+  k2 = k2 > 127 ? 127 : (k2 < -126 ? -126 : k2);
+  return Pow2Pair{pow2f(k1), pow2f(k2)};
+}
+__device__ __forceinline__ float scale2(float x, Pow2Pair p) { return (x * p.a) * p.b; }
+
 template <int MMAX>
 constexpr size_t stream2_smem_bytes() {
   return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
@@ -92,13 +132,20 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
   // relaxation factor exp(-dtProp/tau) and 1 - it, boundary seed
   float mhi[NPT], mlo[NPT], em[NPT], om[NPT];
   __shared__ float s_bcv[3];  // seeds of list nodes 0..2, the boundary (CTA rank 0)
+  __shared__ int s_red[W + 1];
   const double vdt = ec.vgrid * dtProp;
-  // per list node: mult, relaxation factor and its complement, seed, made
-  // in FP64 once per call (k_stream2_coef) and rounded to float
+  // per list node: mult, relaxation factor and its complement, seed * 2^seed_k,
+  // made in FP64 once per call (k_stream2_coef) and rounded to float
   const float4 *cf = r.scoef + ((size_t)s * r.E + e) * N;
+  int xr[NPT];      // the rows' exponents as loaded
+  float sw[NPT];    // seed * 2^seed_k
+  int lg = kNoExp;  // largest floor(log2) of a true value of this thread's rows and seeds
+  const bool seeds_in = r.check_seed != 0;
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
     mhi[q] = mlo[q] = em[q] = om[q] = 0.f;
+    xr[q] = 0;
+    sw[q] = 0.f;
 #pragma unroll
     for (int j = 0; j < H; ++j) Lf[q][j] = Rf[q][j] = 0.f;
     const int il = i0 + q;
@@ -106,25 +153,52 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
       const int k = r.list[sN + il];
       const size_t gidx = sN + k;
       const float4 c = cf[il];
-      const float seedf = c.w;
       const float *fp = reinterpret_cast<const float *>(r.f) + (gidx * r.E + e) * M;
+      float mx = 0.f;
 #pragma unroll
       for (int j = 0; j < H; ++j) {
         if (j < nL) {
-          float v = fp[j];
-          if (r.check_seed && v < seedf) v = seedf;  // as (double)v < seed: no float between
-          Lf[q][j] = v;
+          Lf[q][j] = fp[j];
+          mx = fmaxf(mx, Lf[q][j]);
         }
         if (j < nR) {
-          float v = fp[m0 + j];
-          if (r.check_seed && v < seedf) v = seedf;
-          Rf[q][j] = v;
+          Rf[q][j] = fp[m0 + j];
+          mx = fmaxf(mx, Rf[q][j]);
         }
       }
+      xr[q] = r.fexp[gidx * r.E + e];
+      sw[q] = c.w;
+      const int lr = ilogb_f(mx);
+      if (lr != kNoExp) lg = max(lg, lr - xr[q]);
+      const int ls = ilogb_f(c.w);
+      if ((seeds_in || (r.use_bc && il < 3)) && ls != kNoExp) lg = max(lg, ls - ec.seed_k);
       mhi[q] = (il == 0) ? 0.f : c.x;
       mlo[q] = (il == L - 1) ? 0.f : c.x;
       em[q] = c.y;
       om[q] = c.z;
+    }
+  }
+  // the slab's common exponent; rows and seeds brought to it (exact powers of two)
+  const int K = slab_exp<T>(lg, s_red, cluster, C);
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il < L) {
+      const Pow2Pair pf = pow2_pair(K - xr[q]);
+      const float seedf = scale2(sw[q], pow2_pair(K - ec.seed_k));
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        if (j < nL) {
+          float v = scale2(Lf[q][j], pf);
+          if (seeds_in && v < seedf) v = seedf;  // seedPopulationCheck
+          Lf[q][j] = v;
+        }
+        if (j < nR) {
+          float v = scale2(Rf[q][j], pf);
+          if (seeds_in && v < seedf) v = seedf;
+          Rf[q][j] = v;
+        }
+      }
       if (il < 3) s_bcv[il] = seedf;
     }
   }
@@ -255,6 +329,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
           if (j < nL) op[j] = Lf[q][j];
           if (j < nR) op[m0 + j] = Rf[q][j];
         }
+        r.fexp[(sN + kk) * r.E + e] = (short)K;
       }
     }
   }
@@ -321,19 +396,24 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
   float2 mhi[NPT], mlo[NPT], em[NPT];
   float om[NPT];
   __shared__ float s_bcv[3];
+  __shared__ int s_red[W + 1];
   const double vdt = ec.vgrid * dtProp;
   const float4 *cf = r.scoef + ((size_t)s * r.E + e) * N;
+  int xr[NPT];      // the rows' exponents as loaded
+  float sw[NPT];    // seed * 2^seed_k
+  int lg = kNoExp;  // largest floor(log2) of a true value of this thread's rows and seeds
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
     mhi[q] = mlo[q] = em[q] = make_float2(0.f, 0.f);
     om[q] = 0.f;
+    xr[q] = 0;
+    sw[q] = 0.f;
 #pragma unroll
     for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(0.f, 0.f);
     const int il = i0 + q;
     if (il < L) {
       const int k = r.list[sN + il];
       const float4 c = cf[il];
-      const float seedf = c.w;
       const float *row = reinterpret_cast<const float *>(r.f) + ((sN + k) * r.E + e) * M;
       if constexpr (FILLED) {
         const float4 *fp = reinterpret_cast<const float4 *>(row);
@@ -358,7 +438,37 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
           }
         }
       }
-      if (r.check_seed) {  // as (double)v < seed: no float between; padding stays 0
+      float mx = 0.f;  // padding cells are zero
+#pragma unroll
+      for (int t = 0; t < P; ++t)
+        mx = fmaxf(mx, fmaxf(fmaxf(Lf[q][t].x, Lf[q][t].y), fmaxf(Rf[q][t].x, Rf[q][t].y)));
+      xr[q] = r.fexp[(sN + k) * r.E + e];
+      sw[q] = c.w;
+      const int lr = ilogb_f(mx);
+      if (lr != kNoExp) lg = max(lg, lr - xr[q]);
+      const int ls = ilogb_f(c.w);
+      if ((r.check_seed || (r.use_bc && il < 3)) && ls != kNoExp) lg = max(lg, ls - ec.seed_k);
+      const float mh = (il == 0) ? 0.f : c.x, ml = (il == L - 1) ? 0.f : c.x;
+      mhi[q] = make_float2(mh, mh);
+      mlo[q] = make_float2(ml, ml);
+      em[q] = make_float2(c.y, c.y);
+      om[q] = c.z;
+    }
+  }
+  // the slab's common exponent; rows and seeds brought to it (exact powers of two)
+  const int K = slab_exp<T>(lg, s_red, cluster, C);
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il < L) {
+      const Pow2Pair pf = pow2_pair(K - xr[q]);
+      const float seedf = scale2(sw[q], pow2_pair(K - ec.seed_k));
+#pragma unroll
+      for (int t = 0; t < P; ++t) {
+        Lf[q][t] = make_float2(scale2(Lf[q][t].x, pf), scale2(Lf[q][t].y, pf));
+        Rf[q][t] = make_float2(scale2(Rf[q][t].x, pf), scale2(Rf[q][t].y, pf));
+      }
+      if (r.check_seed) {  // seedPopulationCheck (scaled alike: the same order); padding stays 0
 #pragma unroll
         for (int t = 0; t < P; ++t) {
           if (FILLED || t < nPL) {
@@ -371,11 +481,6 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
           }
         }
       }
-      const float mh = (il == 0) ? 0.f : c.x, ml = (il == L - 1) ? 0.f : c.x;
-      mhi[q] = make_float2(mh, mh);
-      mlo[q] = make_float2(ml, ml);
-      em[q] = make_float2(c.y, c.y);
-      om[q] = c.z;
       if (il < 3) s_bcv[il] = seedf;
     }
   }
@@ -549,6 +654,7 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
       // node k and the thinned nodes that reference it (previous list node + 1 .. k)
       const int kfirst = (il == 0) ? 0 : r.list[sN + il - 1] + 1;
       for (int kk = kfirst; kk <= k; ++kk) {
+        r.fexp[(sN + kk) * r.E + e] = (short)K;
         float *row = reinterpret_cast<float *>(r.f) + ((sN + kk) * r.E + e) * M;
         if constexpr (FILLED) {
           float4 *op = reinterpret_cast<float4 *>(row);
@@ -579,7 +685,9 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
 }
 
 // Per (stream, energy, list node): mult = ds_i min(tau / dtProp, 1), the
-// relaxation factor exp(-dtProp / tau) and 1 - it, and the seed -- the
+// relaxation factor exp(-dtProp / tau) and 1 - it, and the seed times
+// 2^seed_k (the energy's own power of two, so that seeds far below the float
+// range stay floats; the streaming kernels scale it to the slab) -- the
 // reference's expressions in FP64 (src/energeticParticles.c:2300-2350),
 // rounded to float once per call: the FP32 streaming kernels read them
 // instead of spending FP64 pipe time on them at every launch.
@@ -607,10 +715,45 @@ __global__ void k_stream2_coef(RunView r) {
       // split form: the relaxation runs in the node phase instead
       const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
       out = make_float4((float)mult, (float)emt, (float)(1.0 - emt),
-                        to_real<float>(seed_value(r, ec, r.seed_radial[gidx])));
+                        (float)ldexp(seed_value(r, ec, r.seed_radial[gidx]), ec.seed_k));
     }
     r.scoef[i] = out;
   }
+}
+
+// seedPopulationCheck (src/energeticParticlesBoundary.c:28-59) alone, for
+// runs without parallel diffusion, in the FP32 form: one thread per row,
+// compared in FP64 true values, and the row renormalised (the seed may lie
+// far above the row's values).
+__global__ void k_seed_check32(RunView r) {
+  const size_t items = (size_t)r.S * r.N * r.E;
+  for (size_t it = blockIdx.x * (size_t)blockDim.x + threadIdx.x; it < items;
+       it += (size_t)gridDim.x * blockDim.x) {
+    const size_t g = it / r.E;
+    const int e = (int)(it - g * r.E);
+    const double seed = seed_value(r, r.ec[e], r.seed_radial[g]);
+    float *fp = reinterpret_cast<float *>(r.f) + it * r.M;
+    const int x = r.fexp[it];
+    double mx = seed;
+    for (int m = 0; m < r.M; ++m) mx = fmax(mx, ldexp((double)fp[m], -x));
+    const int xn = row_exp_for(ilogb(mx));
+    for (int m = 0; m < r.M; ++m) {
+      double v = ldexp((double)fp[m], -x);
+      if (v < seed) v = seed;
+      const float w = (float)ldexp(v, xn);
+      fp[m] = w < FLT_MIN ? FLT_MIN : w;
+    }
+    r.fexp[it] = (short)xn;
+  }
+}
+
+int launch_seed_check32(const RunView &r, cudaStream_t st, uint64_t *launches) {
+  const size_t items = (size_t)r.S * r.N * r.E;
+  size_t b = (items + 255) / 256;
+  if (b > 152 * 32) b = 152 * 32;
+  k_seed_check32<<<(unsigned)b, 256, 0, st>>>(r);
+  *launches += 1;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
 int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches) {

@@ -120,6 +120,26 @@ def test_fp32_flux_within_1e3_of_oracle(oracle_lib):
 
 
 @pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+def test_shell_diffusion_alone_conserves_particles(oracle_lib, precision):
+    """With streaming, focusing, change and the seed check off, each sub-step
+    only hands f between streams of a shell: every source's loss is the sum
+    of the fractions its neighbours gain, so the sum over streams of every
+    (node, energy, mu) cell is kept up to the rounding of the accumulation
+    (FP32: the loss is the float sum of the float fractions)."""
+    w = W.custom(2, 2, 40, 8, 6, num_ep_steps=4, use_parallel_diffusion=0,
+                 use_adiabatic_focus=0, use_adiabatic_change=0, check_seed_population=0)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    news = random_news(d.num_streams, seed=11)
+    out, _ = gpu_shell(w.dims(precision), w.params, g, f, nodes, news, 5.0, calls=2)
+    shape = (d.num_streams, d.num_nodes, d.num_energies, d.num_mu)
+    before = f.reshape(shape)[:, 1:].sum(axis=0)
+    after = out.reshape(shape)[:, 1:].sum(axis=0)
+    tol = 1e-13 if precision == abi.EPREM_FP64 else 1e-5
+    assert np.max(np.abs(after - before) / before) <= tol
+    assert rel_err(out, f) > 1e-4  # something moved
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
 def test_host_update_equals_device_update(oracle_lib, precision):
     """With the streams coupled, the host-memory entry moves all of f at once;
     pitched host rows (the reference's eParts layout) included."""
