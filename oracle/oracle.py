@@ -23,15 +23,32 @@ REF_LIB = os.path.join(HERE, "_ref", "libeprem_ref.so")
 DP = C.POINTER(C.c_double)
 
 
-def build(ref: bool = False, reference_root: str = "/root/reference") -> None:
+STAGED = os.path.join(HERE, "_ref", "tree")
+
+
+def reference_root() -> str | None:
+    """The reference's source tree: $EPREM_REF, else the staged copy
+    oracle/_ref/tree (oracle/Makefile `stage`), else None."""
+    for cand in (os.environ.get("EPREM_REF"), STAGED):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
+
+
+def build(ref: bool = False) -> None:
     """Compile liboracle.so and, when asked and the reference tree is
     present, the reference harness (libeprem_ref.so), the reference's own
     driver (eprem_ref) and the driver over the drop-in and this restatement
     (eprem_oracle_dropin)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if ref and os.path.isdir(os.path.join(reference_root, "src")):
+    if not ref:
+        return
+    if not os.environ.get("EPREM_REF"):
+        subprocess.check_call(["make", "-s", "-C", HERE, "stage"])
+    root = reference_root()
+    if root:
         subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref", "ref-dropin",
-                               f"REF={reference_root}"])
+                               f"REF={root}"])
 
 
 def _dp(a: np.ndarray):

@@ -9,7 +9,7 @@ tests can check the oracle against the reference where the reference tree is
 absent.
 
 Run from the repository root:  python tests/golden/make_golden.py [case ...]
-(needs /root/reference; each case runs in a fresh process because the
+(needs the reference tree, oracle.reference_root(); each case runs in a fresh process because the
 reference allocates its globals once per process).
 """
 import ctypes as C

@@ -36,7 +36,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+    os.path.abspath(__file__)))), "oracle"))
+import oracle as _orc  # noqa: E402  (the reference tree's location only)
+
+REF = _orc.reference_root() or ""
 EXE = os.path.join(ROOT, "oracle", "_ref", "eprem_oracle_dropin")
 KINDS = {0: "ep", 1: "mhd", 2: "move", 3: "masmove"}
 PLAN = {"wind": ("ep_last", "mhd_last", "move_last"),

@@ -6,11 +6,15 @@ ABI.  Needs the
 reference source tree (present in the build container only)."""
 import os
 import subprocess
+import sys
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as _orc  # noqa: E402  (the reference tree's location only)
+
+REF = _orc.reference_root() or ""
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),
                                 reason="reference source tree not present")

@@ -14,9 +14,11 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
 LIB = os.path.join(ROOT, "oracle", "_ref", "libeprem_ref.so")
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as _orc  # noqa: E402  (the reference tree's location only)
+
+REF = _orc.reference_root() or ""
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),
                                 reason="reference source tree not present")

@@ -32,8 +32,10 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as _orc  # noqa: E402  (the reference tree's location only)
+
+REF = _orc.reference_root() or ""
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "testsuite")),
                                 reason="reference source tree not present")
