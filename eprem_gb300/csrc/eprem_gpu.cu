@@ -115,6 +115,10 @@ static int validate(const eprem_dims_t *d, const eprem_params_t *p, const eprem_
   return EPREM_GPU_OK;
 }
 
+namespace {
+int flux_static_buffer(int device, double **out);
+}
+
 template <typename T>
 static cudaError_t dalloc(T **p, size_t n) {
   return cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T) + 16);
@@ -152,6 +156,14 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
                                    "(num_nodes per stream or E*M too large)");
   }
   cudaError_t e = cudaGetDevice(&r->device);
+  // the static flux buffer's module is loaded (and its 8 MiB made resident)
+  // here, before this run's own allocations, so that a run set sized to fill
+  // the device never meets that load later
+  double *flux_static = nullptr;
+  if (e == cudaSuccess && flux_static_buffer(r->device, &flux_static) != EPREM_GPU_OK) {
+    delete r;
+    return EPREM_GPU_ERR_CUDA;  // the message is set
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
   const size_t SN = r->sn(), cells = r->cells();
   const size_t fbytes = dims->precision == EPREM_FP64 ? sizeof(double) : sizeof(float);
@@ -900,28 +912,27 @@ extern "C" int eprem_gpu_omni_flux(eprem_gpu_run *r, double *out) {
 // Omnidirectional flux staged in a fixed device buffer, for callers that may
 // not allocate once their run is set up (a run set sized to fill the GPU's
 // memory, a host that budgets device memory at start-up).  The buffer is a
-// file-scope device array, created with the module on each device; its
-// address is looked up once per device, with that device current, by the
-// first call there, so that call should come before any stream capture.
-// Every value is written by the flux kernel before it is copied out, so no
-// part of the buffer needs zeroing.  All runs on a device share it: calls
-// that overlap in time race on it and must be serialised by the caller.
+// file-scope device array of this file's module; with lazy module loading
+// the module -- and the buffer -- becomes resident when its address is first
+// looked up, which eprem_gpu_create does for its device (with that device
+// current) before it allocates anything, so the entry point itself never
+// loads or allocates.  Every value is written by the flux kernel before it is
+// copied out, so no part of the buffer needs zeroing.  All runs on a device
+// share it: calls that overlap in time race on it and must be serialised by
+// the caller.
 namespace {
 __device__ __align__(256) double g_flux_static[EPREM_GPU_FLUX_STATIC_MAX];
 std::mutex g_flux_static_mutex;
 double *g_flux_static_addr[kMaxDevices] = {};
 
+// device: the current device (the caller makes it so)
 int flux_static_buffer(int device, double **out) {
   if (device < 0 || device >= kMaxDevices)
     return fail(EPREM_GPU_ERR_ARG, "device ordinal beyond the static flux buffer table");
   std::lock_guard<std::mutex> lock(g_flux_static_mutex);
   if (!g_flux_static_addr[device]) {
-    int current = -1;
-    CK(cudaGetDevice(&current));
-    if (current != device) CK(cudaSetDevice(device));
     void *addr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&addr, g_flux_static);
-    if (current != device) CK(cudaSetDevice(current));
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static flux buffer)");
     g_flux_static_addr[device] = static_cast<double *>(addr);
   }
@@ -932,6 +943,10 @@ int flux_static_buffer(int device, double **out) {
 
 extern "C" int eprem_gpu_omni_flux_static(eprem_gpu_run *r, double *out) {
   if (!r || !out) return fail(EPREM_GPU_ERR_ARG, "null argument");
+  int current = -1;
+  CK(cudaGetDevice(&current));
+  if (current != r->device)
+    return fail(EPREM_GPU_ERR_ARG, "eprem_gpu_omni_flux_static: make the run's device current");
   const size_t n = r->sn() * r->dims.num_energies;
   if (n > (size_t)EPREM_GPU_FLUX_STATIC_MAX)
     return fail(EPREM_GPU_ERR_ARG,

@@ -343,17 +343,19 @@ int eprem_gpu_omni_flux(eprem_gpu_run *run, double *out_host);
 #define EPREM_GPU_FLUX_STATIC_MAX 1048576
 
 /* The omnidirectional flux of eprem_gpu_omni_flux, computed by the same
- * kernel, but staged in a fixed device buffer that the library holds from
- * the moment it is loaded on a device, so this call allocates no device or
- * pinned host memory.  No counterpart in the reference: it exists for
- * callers that cannot allocate at output time -- a run set or ensemble that
- * sizes its runs to fill the GPU's memory up front (where the first
+ * kernel, but staged in a fixed device buffer, so this call allocates no
+ * device or pinned host memory.  No counterpart in the reference: it exists
+ * for callers that cannot allocate at output time -- a run set or ensemble
+ * that sizes its runs to fill the GPU's memory up front (where the first
  * eprem_gpu_omni_flux call, which allocates its staging buffer then, could
  * fail for lack of memory in the middle of a simulation), or a host program
  * that budgets device memory at start-up and permits no allocation later.
- *   - The first call on each device does a one-time set-up: it looks up the
- *     buffer's device address with that device current.  Make that first
- *     call before any stream capture on the device.
+ *   - The buffer (8 MiB) becomes resident on a device when the first run is
+ *     created there: eprem_gpu_create looks up its address, with that device
+ *     current, before the run allocates anything, and keeps it until the
+ *     process exits.  This call itself loads and allocates nothing.
+ *   - Call it with the run's device current; another current device is
+ *     refused with EPREM_GPU_ERR_ARG.
  *   - S*N*E above EPREM_GPU_FLUX_STATIC_MAX is rejected with
  *     EPREM_GPU_ERR_ARG before anything is launched; use eprem_gpu_omni_flux.
  *   - Nothing in the buffer needs to start at zero: the kernel writes every
