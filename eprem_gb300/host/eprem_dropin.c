@@ -33,10 +33,13 @@
  * when its file index (masFileIndex0 / masFileIndex1) changes, and s_cor and
  * phiOffset are passed on every call.
  *
+ * Output: dataDumpIO brings f down only when an output is due, and with
+ * streamFluxOutput alone only the device's omnidirectional flux (1/M of f).
+ *
  * Scope: one MPI rank holds every stream (the GPU replaces the rank
  * decomposition), one species, analytic or MAS coronal background (the
- * heliospheric MAS coupling is refused with the reference's panic), no drift
- * or shell diffusion.
+ * heliospheric MAS coupling is refused with the reference's panic), shell
+ * diffusion; drift is refused with the reference's panic text.
  */
 #include <float.h>
 #include <stdio.h>
@@ -345,9 +348,56 @@ void rotSunAndSpawnShell(Time_t t_sun_del) {
   spawnNewShell();
 }
 
-/* The driver's output reads eParts: bring it up to date first. */
+/* Whether dataDumpIO (src/unifiedOutput.c:1479-1531) writes anything at
+ * this time, by its own conditions. */
+static int dropin_output_due(void) {
+  const double t = t_global * DAY;
+  return (config.unifiedOutput > 0 && t >= config.unifiedOutputTime) ||
+         (config.numObservers > 0 && t >= config.pointObserverOutputTime) ||
+         (config.epremDomain > 0 && t >= config.epremDomainOutputTime) ||
+         (config.unstructuredDomain > 0 && t >= config.epremDomainOutputTime);
+}
+
+/* streamFluxOutput = 1 with no other output that reads eParts: the observer
+ * files take the omnidirectional flux alone, which computeFlux
+ * (src/unifiedOutput.c:153-180) forms from each row's mu-average of f.  The
+ * device's flux (S*N*E values, 1/M of f) comes down instead of f, and each
+ * eParts row of the output is set to its mu-average J / (2E) -- all that
+ * computeFlux reads of it.  eParts stays marked as older than the device's
+ * f, so any later reader of the whole of f still brings it down. */
+static double *dropin_flux = NULL;
+static int dropin_flux_only(void) {
+  return config.streamFluxOutput == 1 && config.numObservers == 0 && config.epremDomain == 0 &&
+         config.unstructuredDomain == 0;
+}
+
+static void dropin_flux_to_host(void) {
+  const size_t N = TOTAL_NUM_SHELLS, E = NUM_ESTEPS, M = NUM_MUSTEPS;
+  if (!dropin_flux) {
+    dropin_flux = (double *)eprem_gpu_host_alloc(sizeof(double) * dropin_sn * E);
+    if (!dropin_flux) panic("GPU path: host flux buffer allocation failed");
+  }
+  dropin_check(eprem_gpu_omni_flux(dropin_run, dropin_flux), "omnidirectional flux");
+  for (size_t s = 0; s < (size_t)NUM_STREAMS; s++)
+    for (size_t k = 0; k < N; k++) {
+      Scalar_t *row = eParts + SPEM + s * SSPEM + k * E * M;
+      const double *j = dropin_flux + (s * N + k) * E;
+      for (size_t e = 0; e < E; e++) {
+        const Scalar_t iso = j[e] / (2.0 * egrid[e]);
+        for (size_t m = 0; m < M; m++) row[e * M + m] = iso;
+      }
+    }
+}
+
+/* The driver's output reads eParts: bring it up to date first (when the
+ * output is due at all; the driver calls dataDumpIO every step). */
 void dataDumpIO(void) {
-  if (dropin_run) dropin_f_to_host();
+  if (dropin_run && dropin_f_stale && dropin_output_due()) {
+    if (dropin_flux_only())
+      dropin_flux_to_host();
+    else
+      dropin_f_to_host();
+  }
   dataDumpIO_cpu();
 }
 

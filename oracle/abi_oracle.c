@@ -200,6 +200,12 @@ int eprem_gpu_ripple_f(eprem_gpu_run *r, const double *tmpl, size_t stream_pitch
   return EPREM_GPU_OK;
 }
 
+int eprem_gpu_omni_flux(eprem_gpu_run *r, double *out) {
+  if (!r || !out) return abi_fail(EPREM_GPU_ERR_ARG, "null argument");
+  orc_omni_flux(&r->d, &r->g, r->f, out);
+  return EPREM_GPU_OK;
+}
+
 int eprem_gpu_upload_nodes(eprem_gpu_run *r, const double *nodes, uint64_t mask) {
   const size_t sn = (size_t)r->d.num_streams * r->d.num_nodes;
   for (int k = 0; k < EPREM_NODE_NFIELDS; k++)

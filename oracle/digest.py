@@ -105,10 +105,11 @@ def var_lines(name, a):
     return lines
 
 
-def digest_run(rundir):
-    """Digest text of every obs*.nc capture in rundir (granularity=global)."""
+def digest_run(rundir, prefix="obs"):
+    """Digest text of every <prefix>*.nc capture in rundir (granularity=global;
+    prefix "flux" for the streamFluxOutput files, src/unifiedOutput.c:115-122)."""
     lines = ["# eprem_digest granularity=global"]
-    for cap in sorted(glob.glob(os.path.join(rundir, "obs*.nc.cap"))):
+    for cap in sorted(glob.glob(os.path.join(rundir, prefix + "*.nc.cap"))):
         lines.append("file " + os.path.basename(cap)[:-4])
         vs = read_capture(cap)
         for name in sorted(vs):

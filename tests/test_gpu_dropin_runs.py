@@ -122,3 +122,21 @@ def test_gpu_run_arrays_match_oracle_run(runs, case):
             worst[name] = max(worst.get(name, 0.0), err)
             assert err <= tol, (os.path.basename(cap), name, err)
     assert "Dist" in worst
+
+
+def test_gpu_flux_output_run_matches_reference(tmp_path):
+    """streamFluxOutput on the GPU: dataDumpIO brings down the device's flux
+    (S*N*E values) instead of f; the flux files of the testsuite's wind case
+    (streamFluxOutput=1, domain dump off) within 1e-12 of the reference's
+    own run, every other variable within 1e-10."""
+    from test_flux_output_run import compare_flux_runs, flux_config, run_case
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref",
+                           f"REF={REF}"])
+    from eprem_gb300 import build
+    build.build()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "eprem_gb300", "host"), "link",
+                           f"REF={REF}"])
+    text = flux_config()
+    ref = run_case(os.path.join(ROOT, "oracle", "_ref", "eprem_ref"), "wind", tmp_path, text)
+    gpu = run_case(GPU_EXE, "wind", tmp_path, text)
+    assert compare_flux_runs(gpu, ref, 1e-12) > 0.0
