@@ -87,6 +87,11 @@ class Params(C.Structure):
     ]
 
 
+class DriftParams(C.Structure):
+    """eprem_drift_params_t"""
+    _fields_ = [("lnpmin", C.c_double), ("charge", C.c_double), ("mass", C.c_double)]
+
+
 class Grids(C.Structure):
     _fields_ = [
         ("egrid", C.POINTER(C.c_double)),

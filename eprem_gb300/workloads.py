@@ -237,7 +237,13 @@ def build_grids(w: Workload):
     dmu = 2.0 / (1.0 * M)
     mugrid = np.array([0.5 * ((-1.0 + (m + 1.0) * dmu) + (-1.0 + m * dmu)) for m in range(M)])
     return {"egrid": egrid, "vgrid": vgrid, "vgrid_i": vgrid_i, "mugrid": mugrid,
-            "rigidity": rig, "dlnp": dlnp, "dmu": dmu}
+            "rigidity": rig, "dlnp": dlnp, "dmu": dmu, "lnpmin": lnpmin}
+
+
+def drift_params(w: Workload, g: dict) -> abi.DriftParams:
+    """eprem_drift_params_t of the workload (useDrift): lnpmin of its momentum
+    grid and the species' charge and mass."""
+    return abi.DriftParams(g["lnpmin"], w.charge, w.mass)
 
 
 def grids_struct(g) -> tuple[abi.Grids, list]:

@@ -40,6 +40,10 @@ struct eprem_gpu_run {
   orc_mas_t mas;
   int32_t *news; /* shell diffusion: NEWS links, NULL when off */
   double kperxkpar;
+  int drift_on;          /* drift: curl formed by updateMhd                  */
+  eprem_drift_params_t drift;
+  int32_t *drift_news;   /* drift: NEWS links once known                     */
+  double *curl;          /* [3][S*N]                                         */
 };
 
 static char abi_err[320] = "";
@@ -227,11 +231,21 @@ int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
   char err[256] = "";
   const char *env = getenv("EPREM_ORACLE_THREADS");
   const int nt = env ? atoi(env) : 1;
-  const int rc =
-      r->news ? orc_update_energetic_particles_news(&r->d, &r->p, &r->g, r->f, r->nodes, r->news,
-                                                    r->kperxkpar, &r->stats, nt > 0 ? nt : 1, err)
-              : orc_update_energetic_particles(&r->d, &r->p, &r->g, r->f, r->nodes, &r->stats,
-                                               nt > 0 ? nt : 1, err);
+  const int drift = r->drift_on && r->drift_news;
+  int rc;
+  if (drift) {
+    if (r->news && memcmp(r->news, r->drift_news, 4 * sizeof(int32_t) * r->d.num_streams))
+      return abi_fail(EPREM_GPU_ERR_ARG, "shell diffusion and drift need the same links");
+    rc = orc_update_energetic_particles_perp(&r->d, &r->p, &r->g, r->f, r->nodes, r->drift_news,
+                                             r->news != NULL, r->kperxkpar, &r->drift, r->curl,
+                                             &r->stats, nt > 0 ? nt : 1, err);
+  } else {
+    rc = r->news ? orc_update_energetic_particles_news(&r->d, &r->p, &r->g, r->f, r->nodes,
+                                                       r->news, r->kperxkpar, &r->stats,
+                                                       nt > 0 ? nt : 1, err)
+                 : orc_update_energetic_particles(&r->d, &r->p, &r->g, r->f, r->nodes,
+                                                  &r->stats, nt > 0 ? nt : 1, err);
+  }
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, err);
 }
 void *eprem_gpu_host_alloc(size_t bytes) { return malloc(bytes ? bytes : 1); }
@@ -281,9 +295,31 @@ int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *s) {
 
 int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
   rec_call(r, REC_MHD, t_global);
+  if (r->mas_on && r->drift_on)
+    return abi_fail(EPREM_GPU_ERR_UNSUPPORTED, "drift with the MAS background");
   const int rc = r->mas_on ? orc_mas_update_mhd(&r->d, &r->p, r->nodes, &r->mas, t_global)
-                           : orc_update_mhd(&r->d, &r->p, r->nodes, t_global);
+                 : r->drift_on ? orc_update_mhd_curl(&r->d, &r->p, r->nodes, t_global, r->curl)
+                               : orc_update_mhd(&r->d, &r->p, r->nodes, t_global);
   return rc == EPREM_GPU_OK ? rc : abi_fail(rc, "updateMhd");
+}
+
+int eprem_gpu_set_drift(eprem_gpu_run *r, const int32_t *news, const eprem_drift_params_t *dp) {
+  if (!dp) {
+    r->drift_on = 0;
+    return EPREM_GPU_OK;
+  }
+  if (r->mas_on) return abi_fail(EPREM_GPU_ERR_UNSUPPORTED, "drift with the MAS background");
+  const size_t sn = (size_t)r->d.num_streams * r->d.num_nodes;
+  if (!r->curl) r->curl = (double *)calloc(3 * sn, sizeof(double));
+  r->drift = *dp;
+  r->drift_on = 1;
+  if (news) {
+    const size_t n = 4 * (size_t)r->d.num_streams;
+    free(r->drift_news);
+    r->drift_news = (int32_t *)malloc(n * sizeof(int32_t));
+    memcpy(r->drift_news, news, n * sizeof(int32_t));
+  }
+  return EPREM_GPU_OK;
 }
 int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
   rec_call(r, REC_MOVE, dt);

@@ -855,7 +855,8 @@ static int orc_validate(const eprem_dims_t *d, const eprem_params_t *p, char *er
  * perpendicular to B, dl * sqrt(1 - (e_n . e_B)^2).  dlper: [S][N][4] in the
  * order north, east, west, south. */
 static void orc_shell_lengths(const eprem_dims_t *d, const eprem_params_t *p,
-                              const double *nodes, const int32_t *news, double *dlper) {
+                              const double *nodes, const int32_t *news, double *dlper,
+                              double *dlen) {
   const int S = d->num_streams, N = d->num_nodes;
   const size_t SN = (size_t)S * N;
   const double rs = p->r_scale;
@@ -871,6 +872,7 @@ static void orc_shell_lengths(const eprem_dims_t *d, const eprem_params_t *p,
         double ex = NODE(EPREM_NODE_RX, o, k) * rs - rx, ey = NODE(EPREM_NODE_RY, o, k) * rs - ry,
                ez = NODE(EPREM_NODE_RZ, o, k) * rs - rz;
         double dl = sqrt(ex * ex + ey * ey + ez * ez);
+        dlen[((size_t)s * N + k) * 4 + dir] = dl;
         ex /= dl;
         ey /= dl;
         ez /= dl;
@@ -930,9 +932,96 @@ static int orc_shell_diffuse(const eprem_dims_t *d, const eprem_params_t *p,
   return rc;
 }
 
+/* driftVelocity (src/energeticParticles.c:210-246) for energy e: the
+ * spherical curl(B)/B^2 times (1/om1) p v / 3, p = exp(lnpmin + e dlnp),
+ * om1 = charge OM / mass, to Cartesian at position r (sphToCartVector,
+ * src/geometry.c:89-125). */
+#define ORC_Q 4.80320425e-10
+#define ORC_OM (ORC_MHD_B_NORM * ORC_Q * ORC_AU / (ORC_MP * ORC_C * ORC_C))
+static void orc_drift_velocity(const eprem_drift_params_t *dp, const eprem_grids_t *g, int e,
+                               const double curl[3], double x, double y, double z,
+                               double out[3]) {
+  double pm = exp(dp->lnpmin + e * g->dlnp);
+  double om1 = dp->charge * ORC_OM / dp->mass;
+  double factor = (1.0 / om1) * (pm * g->vgrid[e] / 3.0);
+  double vr = factor * curl[0], vt = factor * curl[1], vp = factor * curl[2];
+  double rmag = sqrt(x * x + y * y + z * z);
+  if ((rmag - fabs(z)) < ORC_VERYSMALL) {
+    out[0] = 0.0;
+    out[1] = 0.0;
+  } else {
+    out[0] = x / rmag * vr + x * z / (rmag * sqrt(rmag * rmag - z * z)) * vt -
+             y / sqrt(rmag * rmag - z * z) * vp;
+    out[1] = y / rmag * vr + y * z / (rmag * sqrt(rmag * rmag - z * z)) * vt +
+             x / sqrt(rmag * rmag - z * z) * vp;
+  }
+  out[2] = z / rmag * vr - sqrt(rmag * rmag - z * z) / rmag * vt;
+}
+
+/* DriftShellData (src/energeticParticles.c:561-801), one sub-step of length
+ * dt over all streams, nodes 1..N-1: per node and energy, each stream hands
+ * del = min(vdp dt / dl, THRESH) of its f to every NEWS neighbour with
+ * vdp = (v_d . (r_nbr - r)) rScale / dl > 0 (dl the neighbour distance of
+ * ShellData), all hand-overs of one node and energy summed in the
+ * reference's order (source streams ascending; per source north, east, west,
+ * south, each with its gain to the neighbour and then the source's loss)
+ * before f changes. */
+static int orc_drift_shell(const eprem_dims_t *d, const eprem_params_t *p,
+                           const eprem_grids_t *g, double *f, const double *nodes,
+                           const int32_t *news, const double *dlen, const double *curl,
+                           const eprem_drift_params_t *dp, double dt, char *errbuf) {
+  const int S = d->num_streams, N = d->num_nodes, E = d->num_energies, M = d->num_mu;
+  const size_t SN = (size_t)S * N;
+  const double thresh = 0.025;
+  double *delta = (double *)malloc(sizeof(double) * (size_t)S * M);
+  int rc = EPREM_GPU_OK;
+  for (int k = 1; k < N && !rc; k++)
+    for (int e = 0; e < E && !rc; e++) {
+      for (size_t i = 0; i < (size_t)S * M; i++) delta[i] = 0.0;
+      for (int s = 0; s < S; s++) {
+        const double x = NODE(EPREM_NODE_RX, s, k), y = NODE(EPREM_NODE_RY, s, k),
+                     z = NODE(EPREM_NODE_RZ, s, k);
+        const double cv[3] = {curl[0 * SN + (size_t)s * N + k], curl[1 * SN + (size_t)s * N + k],
+                              curl[2 * SN + (size_t)s * N + k]};
+        double vd[3];
+        orc_drift_velocity(dp, g, e, cv, x, y, z, vd);
+        const double *fs = &f[FIDX(s, k, e, 0)];
+        for (int dir = 0; dir < 4; dir++) {
+          const int o = news[s * 4 + dir];
+          double enx = NODE(EPREM_NODE_RX, o, k) - x, eny = NODE(EPREM_NODE_RY, o, k) - y,
+                 enz = NODE(EPREM_NODE_RZ, o, k) - z;
+          const double dl = dlen[((size_t)s * N + k) * 4 + dir];
+          double vdp = (vd[0] * enx + vd[1] * eny + vd[2] * enz) * p->r_scale / dl;
+          if (vdp > 0.0) {
+            double del = vdp * dt / dl;
+            if (del > thresh) del = thresh;
+            for (int m = 0; m < M; m++) {
+              delta[(size_t)o * M + m] += del * fs[m];
+              delta[(size_t)s * M + m] -= del * fs[m];
+            }
+          }
+        }
+      }
+      for (int s = 0; s < S && !rc; s++)
+        for (int m = 0; m < M; m++) {
+          double v = f[FIDX(s, k, e, m)] += delta[(size_t)s * M + m];
+          if (isnan(v) || isinf(v)) {
+            rc = isnan(v) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF;
+            if (errbuf)
+              snprintf(errbuf, 256, "%s in DriftShellData (stream %d, node %d)",
+                       isnan(v) ? "NaN value" : "Inf value", s, k);
+            break;
+          }
+        }
+    }
+  free(delta);
+  return rc;
+}
+
 static int orc_update_core(const eprem_dims_t *d, const eprem_params_t *p, const eprem_grids_t *g,
                            double *f, double *nodes, int s0, int s1, const int32_t *news,
-                           double kperxkpar, eprem_ep_stats_t *stats, int nthreads,
+                           int shell_on, double kperxkpar, const eprem_drift_params_t *drift,
+                           const double *curl, eprem_ep_stats_t *stats, int nthreads,
                            char *errbuf) {
   int rc = orc_validate(d, p, errbuf);
   if (rc) return rc;
@@ -965,10 +1054,11 @@ static int orc_update_core(const eprem_dims_t *d, const eprem_params_t *p, const
   /* Without shell diffusion one pass runs every sub-step; with it, one pass
    * per sub-step, each followed by the diffusion over all streams. */
   const int passes = news ? p->num_ep_steps : 1;
-  double *dlper = NULL;
+  double *dlper = NULL, *dlen = NULL;
   if (news) {
     dlper = (double *)malloc(sizeof(double) * 4 * (size_t)d->num_streams * d->num_nodes);
-    orc_shell_lengths(d, p, nodes, news, dlper);
+    dlen = (double *)malloc(sizeof(double) * 4 * (size_t)d->num_streams * d->num_nodes);
+    orc_shell_lengths(d, p, nodes, news, dlper, dlen);
   }
   const double dt = p->t_del / (1.0 * p->num_ep_steps);
   int diff_rc = EPREM_GPU_OK;
@@ -987,10 +1077,13 @@ static int orc_update_core(const eprem_dims_t *d, const eprem_params_t *p, const
     int failed = 0;
     for (int t = 0; t < nthreads; t++) failed |= jobs[t].status != EPREM_GPU_OK;
     if (failed) break;
-    if (news)
+    if (news && shell_on)
       diff_rc = orc_shell_diffuse(d, p, g, f, nodes, news, kperxkpar, dlper, dt, diff_err);
+    if (news && drift && !diff_rc)
+      diff_rc = orc_drift_shell(d, p, g, f, nodes, news, dlen, curl, drift, dt, diff_err);
   }
   free(dlper);
+  free(dlen);
   rc = EPREM_GPU_OK;
   for (int t = 0; t < nthreads; t++) {
     eprem_ep_stats_t *js = &jobs[t].stats;
@@ -1022,15 +1115,29 @@ int orc_update_energetic_particles_range(const eprem_dims_t *d, const eprem_para
                                          const eprem_grids_t *g, double *f, double *nodes,
                                          int s0, int s1, eprem_ep_stats_t *stats, int nthreads,
                                          char *errbuf) {
-  return orc_update_core(d, p, g, f, nodes, s0, s1, NULL, 0.0, stats, nthreads, errbuf);
+  return orc_update_core(d, p, g, f, nodes, s0, s1, NULL, 0, 0.0, NULL, NULL, stats, nthreads,
+                         errbuf);
 }
 
 int orc_update_energetic_particles_news(const eprem_dims_t *d, const eprem_params_t *p,
                                         const eprem_grids_t *g, double *f, double *nodes,
                                         const int32_t *news, double kperxkpar,
                                         eprem_ep_stats_t *stats, int nthreads, char *errbuf) {
-  return orc_update_core(d, p, g, f, nodes, 0, d->num_streams, news, kperxkpar, stats, nthreads,
-                         errbuf);
+  return orc_update_core(d, p, g, f, nodes, 0, d->num_streams, news, 1, kperxkpar, NULL, NULL,
+                         stats, nthreads, errbuf);
+}
+
+int orc_update_energetic_particles_perp(const eprem_dims_t *d, const eprem_params_t *p,
+                                        const eprem_grids_t *g, double *f, double *nodes,
+                                        const int32_t *news, int shell_on, double kperxkpar,
+                                        const eprem_drift_params_t *drift, const double *curl,
+                                        eprem_ep_stats_t *stats, int nthreads, char *errbuf) {
+  if (drift && !curl) {
+    if (errbuf) snprintf(errbuf, 256, "drift needs curl(B)/B^2");
+    return EPREM_GPU_ERR_ARG;
+  }
+  return orc_update_core(d, p, g, f, nodes, 0, d->num_streams, news, shell_on, kperxkpar, drift,
+                         curl, stats, nthreads, errbuf);
 }
 
 int orc_update_energetic_particles(const eprem_dims_t *d, const eprem_params_t *p,
@@ -1062,10 +1169,87 @@ static double orc_shock_factor(const eprem_params_t *p, double r, double t_globa
   return 1 + (factor - 1) * falloff;
 }
 
+/* parkerB (src/flow.c:443-472) at (r AU, theta), ideal shock included. */
+static void orc_parker_b(const eprem_params_t *p, double r, double theta, double Vr, int isn,
+                         double t_global, double B[3]) {
+  B[0] = p->mhd_bs_au / (r * r);
+  B[1] = 0.0;
+  B[2] = -1.0 * r * B[0] * (p->omega_sun / (Vr + ORC_VERYSMALL)) * sin(theta);
+  if ((p->ideal_shock > 0) && (isn > 0)) {
+    B[0] *= orc_shock_factor(p, r, t_global);
+    B[1] *= orc_shock_factor(p, r, t_global);
+    B[2] *= orc_shock_factor(p, r, t_global);
+  }
+}
+
+/* curlBoverB2 (src/flow.c:479-616): curl(B)/B^2 of the Parker field by
+ * centred differences at (r +- 0.001 AU, theta +- pi/100, phi +- pi/100),
+ * angles folded back into range; spherical components (r, theta, phi). */
+static void orc_curl_bover_b2(const eprem_params_t *p, double x, double y, double z, double Vr,
+                              int isn, double t_global, double curl[3]) {
+  const double rcw = 0.001, tcw = ORC_PI / 100.0, pcw = ORC_PI / 100.0;
+  double rr = p->r_scale * sqrt(x * x + y * y + z * z);
+  double th = acos(z * p->r_scale / rr);
+  double ph = atan2(y, x);
+  double rp = rr + rcw, rm = rr - rcw;
+  double tp = th + tcw, tp_ph = ph;
+  if (tp > ORC_PI) {
+    tp = 2.0 * ORC_PI - tp;
+    tp_ph += ORC_PI;
+    if (tp_ph > (2.0 * ORC_PI)) tp_ph -= (2.0 * ORC_PI);
+  }
+  double tm = th - tcw, tm_ph = ph;
+  if (tm < 0.0) {
+    tm *= -1.0;
+    tm_ph += ORC_PI;
+    if (tm_ph > (2.0 * ORC_PI)) tm_ph -= (2.0 * ORC_PI);
+  }
+  (void)tp_ph;
+  (void)tm_ph;  /* parkerB depends on r and theta only */
+  double B_rm[3], B_rp[3], B_tm[3], B_tp[3], B_pm[3], B_pp[3];
+  orc_parker_b(p, rm, th, Vr, isn, t_global, B_rm);
+  orc_parker_b(p, rp, th, Vr, isn, t_global, B_rp);
+  orc_parker_b(p, rr, tm, Vr, isn, t_global, B_tm);
+  orc_parker_b(p, rr, tp, Vr, isn, t_global, B_tp);
+  orc_parker_b(p, rr, th, Vr, isn, t_global, B_pm);
+  orc_parker_b(p, rr, th, Vr, isn, t_global, B_pp);
+  double m_rm = sqrt(B_rm[0] * B_rm[0] + B_rm[1] * B_rm[1] + B_rm[2] * B_rm[2]);
+  double m_rp = sqrt(B_rp[0] * B_rp[0] + B_rp[1] * B_rp[1] + B_rp[2] * B_rp[2]);
+  double m_tm = sqrt(B_tm[0] * B_tm[0] + B_tm[1] * B_tm[1] + B_tm[2] * B_tm[2]);
+  double m_tp = sqrt(B_tp[0] * B_tp[0] + B_tp[1] * B_tp[1] + B_tp[2] * B_tp[2]);
+  double m_pm = sqrt(B_pm[0] * B_pm[0] + B_pm[1] * B_pm[1] + B_pm[2] * B_pm[2]);
+  double m_pp = sqrt(B_pp[0] * B_pp[0] + B_pp[1] * B_pp[1] + B_pp[2] * B_pp[2]);
+  double A, B;
+  A = (0.5 / tcw) * (B_tp[2] * sin(tp) / (m_tp * m_tp) - B_tm[2] * sin(tm) / (m_tm * m_tm));
+  B = (0.5 / pcw) * (B_pp[1] / (m_pp * m_pp) - B_pm[1] / (m_pm * m_pm));
+  curl[0] = (1.0 / (rr * sin(th))) * (A - B);
+  A = (1.0 / sin(th)) * (0.5 / pcw) * (B_pp[0] / (m_pp * m_pp) - B_pm[0] / (m_pm * m_pm));
+  B = (0.5 / rcw) * (rp * B_rp[2] / (m_rp * m_rp) - rm * B_rm[2] / (m_rm * m_rm));
+  curl[1] = (1.0 / rr) * (A - B);
+  A = (0.5 / rcw) * (rp * B_rp[1] / (m_rp * m_rp) - rm * B_rm[1] / (m_rm * m_rm));
+  B = (0.5 / tcw) * (B_tp[0] / (m_tp * m_tp) - B_tm[0] / (m_tm * m_tm));
+  curl[2] = (1.0 / rr) * (A - B);
+}
+
+static int orc_update_mhd_core(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                               double t_global, double *curl);
+
 /* updateMhd with mhdGridStatus == MHD_DEFAULT (src/flow.c:36-154), including
  * mhdDensity (:241-275), mhdV (:356-403), mhdB (:281-350). */
 int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
                    double t_global) {
+  return orc_update_mhd_core(d, p, nodes, t_global, NULL);
+}
+
+/* The same with useDrift on: curl(B)/B^2 of every node (mhdCurlBoverB2,
+ * src/flow.c:127-128) into curl[3][S*N] (r, theta, phi). */
+int orc_update_mhd_curl(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                        double t_global, double *curl) {
+  return orc_update_mhd_core(d, p, nodes, t_global, curl);
+}
+
+static int orc_update_mhd_core(const eprem_dims_t *d, const eprem_params_t *p, double *nodes,
+                               double t_global, double *curl) {
   const int N = d->num_nodes;
   const size_t SN = (size_t)d->num_streams * N;
   const double rs = p->r_scale;
@@ -1130,6 +1314,11 @@ int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p, double *nodes
       NODE(EPREM_NODE_BVEC_X, s, k) = Br * sin(theta) * cos(phi) + Bt * cos(theta) * cos(phi) - Bp * sin(phi);
       NODE(EPREM_NODE_BVEC_Y, s, k) = Br * sin(theta) * sin(phi) + Bt * cos(theta) * sin(phi) + Bp * cos(phi);
       NODE(EPREM_NODE_BVEC_Z, s, k) = Br * cos(theta) - Bt * sin(theta);
+      if (curl) {
+        double cv[3];
+        orc_curl_bover_b2(p, x, y, z, Vr, isn, t_global, cv);
+        for (int c = 0; c < 3; c++) curl[(size_t)c * SN + (size_t)s * N + k] = cv[c];
+      }
       if (k == 0) {
         NODE(EPREM_NODE_DUPAR, s, k) = 0.0;
         NODE(EPREM_NODE_DLNB, s, k) = 0.0;

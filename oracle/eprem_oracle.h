@@ -76,6 +76,20 @@ int orc_update_energetic_particles_news(const eprem_dims_t *d, const eprem_param
 /* updateMhd for the analytic background (src/flow.c:36-154). */
 int orc_update_mhd(const eprem_dims_t *d, const eprem_params_t *p,
                    double *nodes, double t_global);
+/* The same with useDrift on: also curl(B)/B^2 of every node (mhdCurlBoverB2
+ * with curlBoverB2, src/flow.c:127-128, :479-616), curl[3][S*N] (r, theta,
+ * phi components). */
+int orc_update_mhd_curl(const eprem_dims_t *d, const eprem_params_t *p,
+                        double *nodes, double t_global, double *curl);
+/* updateEnergeticParticles with the perpendicular steps after each
+ * sub-step: DiffuseShellData when shell_on, then DriftShellData
+ * (src/energeticParticles.c:561-801) when drift is non-NULL, with the
+ * curl(B)/B^2 of orc_update_mhd_curl. */
+int orc_update_energetic_particles_perp(const eprem_dims_t *d, const eprem_params_t *p,
+                                        const eprem_grids_t *g, double *f, double *nodes,
+                                        const int32_t *news, int shell_on, double kperxkpar,
+                                        const eprem_drift_params_t *drift, const double *curl,
+                                        eprem_ep_stats_t *stats, int nthreads, char *errbuf);
 
 /* moveNodes (src/simCore.c:737-785) with delrFlow (src/flow.c:162-196). */
 int orc_move_nodes(const eprem_dims_t *d, const eprem_params_t *p,

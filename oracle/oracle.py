@@ -2,7 +2,9 @@
 
 * ``Oracle``    -> oracle/liboracle.so, the CPU restatement (eprem_oracle.c);
 * ``Reference`` -> oracle/_ref/libeprem_ref.so, the reference's own C compiled
-  from its source tree (only present where that tree exists).
+  from its source tree (only present where that tree exists), or
+  oracle/_ref/native/libeprem_ref_native.so, the same compiled with the
+  reference's own optimisation flags (the timed CPU baseline).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module, and only to check or time against it.
@@ -20,6 +22,8 @@ from eprem_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libeprem_ref.so")
+# the reference compiled with its own flags (-O3 -march=native), for timing
+NATIVE_LIB = os.path.join(HERE, "_ref", "native", "libeprem_ref_native.so")
 DP = C.POINTER(C.c_double)
 
 
@@ -48,7 +52,7 @@ def build(ref: bool = False) -> None:
     root = reference_root()
     if root:
         subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref", "ref-dropin",
-                               f"REF={root}"])
+                               "ref-native", f"REF={root}"])
 
 
 def _dp(a: np.ndarray):
@@ -70,6 +74,13 @@ class Oracle:
             C.POINTER(C.c_int32), C.c_double, C.POINTER(abi.EpStats), C.c_int, C.c_char_p]
         lib.orc_update_energetic_particles_news.restype = C.c_int
         lib.orc_update_mhd.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
+        lib.orc_update_mhd_curl.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP,
+                                            C.c_double, DP]
+        lib.orc_update_energetic_particles_perp.argtypes = [
+            C.POINTER(abi.Dims), C.POINTER(abi.Params), C.POINTER(abi.Grids), DP, DP,
+            C.POINTER(C.c_int32), C.c_int, C.c_double, C.POINTER(abi.DriftParams), DP,
+            C.POINTER(abi.EpStats), C.c_int, C.c_char_p]
+        lib.orc_update_energetic_particles_perp.restype = C.c_int
         lib.orc_move_nodes.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Params), DP, C.c_double]
         lib.orc_omni_flux.argtypes = [C.POINTER(abi.Dims), C.POINTER(abi.Grids), DP, DP]
         lib.orc_omni_flux.restype = None
@@ -120,8 +131,27 @@ class Oracle:
             C.byref(st), nthreads, err)
         return rc, st, err.value.decode()
 
-    def update_mhd(self, dims, params, nodes, t_global):
+    def update_mhd(self, dims, params, nodes, t_global, curl=None):
+        """curl: a (3, S*N) array to receive curl(B)/B^2 (useDrift), or None."""
+        if curl is not None:
+            return self.lib.orc_update_mhd_curl(C.byref(dims), C.byref(params), _dp(nodes),
+                                                t_global, _dp(curl))
         return self.lib.orc_update_mhd(C.byref(dims), C.byref(params), _dp(nodes), t_global)
+
+    def update_energetic_particles_perp(self, dims, params, grids_s, f, nodes, news,
+                                        kperxkpar=None, drift=None, curl=None, nthreads=1):
+        """The update with the perpendicular steps: shell diffusion when
+        kperxkpar is given, drift when drift (abi.DriftParams) and curl are."""
+        st = abi.EpStats()
+        st.min_tau = np.finfo(np.float64).max
+        err = C.create_string_buffer(256)
+        nw = np.ascontiguousarray(news, dtype=np.int32)
+        rc = self.lib.orc_update_energetic_particles_perp(
+            C.byref(dims), C.byref(params), C.byref(grids_s), _dp(f), _dp(nodes),
+            nw.ctypes.data_as(C.POINTER(C.c_int32)), int(kperxkpar is not None),
+            float(kperxkpar or 0.0), C.byref(drift) if drift is not None else None,
+            _dp(curl) if curl is not None else None, C.byref(st), nthreads, err)
+        return rc, st, err.value.decode()
 
     def move_nodes(self, dims, params, nodes, dt):
         return self.lib.orc_move_nodes(C.byref(dims), C.byref(params), _dp(nodes), dt)
@@ -167,7 +197,16 @@ class Reference:
                                       C.POINTER(abi.MasSlice), C.c_double, C.c_double]
         lib.ref_mas_move_nodes.argtypes = [C.c_double]
         lib.ref_shell_diffusion.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_int32)]
+        lib.ref_drift.argtypes = [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         self.lib = lib
+
+    def drift(self, num_streams):
+        """Switch DriftShellData on; returns the reference's NEWS links and
+        its lnpmin."""
+        news = np.zeros((num_streams, 4), dtype=np.int32)
+        lnpmin = C.c_double()
+        self.lib.ref_drift(1, news.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(lnpmin))
+        return news, lnpmin.value
 
     def shell_diffusion(self, kperxkpar, num_streams):
         """Switch on DiffuseShellData; returns the reference's NEWS links

@@ -260,15 +260,32 @@ int ref_store(double *f, double *nodes) {
  * 46-94), returned in news as stream indices face*R*C + row*C + col, four per
  * stream in the order north, east, west, south.  initCopyAll also places the
  * nodes on the unit sphere; ref_load sets them afterwards. */
-int ref_shell_diffusion(int on, double kperxkpar, int32_t *news) {
-  initNEWS(INNER_SHELL);
-  initCopyAll();
+static int ref_news_ready = 0;
+static void ref_news(int32_t *news) {
+  if (!ref_news_ready) {
+    initNEWS(INNER_SHELL);
+    initCopyAll();
+    ref_news_ready = 1;
+  }
   for (int s = 0; s < ref_S; s++) {
     const Node_t *n = &grid[(size_t)s * LOCAL_NUM_SHELLS + INNER_ACTIVE_SHELL];
     const Neighbor_t *nb[4] = {&n->n, &n->e, &n->w, &n->s};
     for (int d = 0; d < 4; d++)
       news[s * 4 + d] = (int32_t)((nb[d]->face * FACE_ROWS + nb[d]->row) * FACE_COLS + nb[d]->col);
   }
+}
+
+/* useDrift on or off, with the grid's NEWS links (news) and the momentum
+ * grid's lnpmin (the reference's global) handed back. */
+int ref_drift(int on, int32_t *news, double *lnpmin_out) {
+  ref_news(news);
+  config.useDrift = on;
+  *lnpmin_out = lnpmin;
+  return 0;
+}
+
+int ref_shell_diffusion(int on, double kperxkpar, int32_t *news) {
+  ref_news(news);
   config.useShellDiffusion = on;
   config.kperxkpar = kperxkpar;
   return 0;
@@ -286,7 +303,7 @@ int ref_update_energetic_particles(double tg, eprem_ep_stats_t *st) {
   ref_abort_armed = 1;
   int code = setjmp(ref_abort_jmp);
   if (code == 0) {
-    if (config.useShellDiffusion > 0) ShellData();
+    if (config.useShellDiffusion > 0 || config.useDrift > 0) ShellData();
     updateEnergeticParticles();
   }
   ref_abort_armed = 0;

@@ -31,7 +31,16 @@ CASES = {
     "shell_3x2_capped_alg3": lambda: W.custom(3, 2, 16, 6, 6, num_ep_steps=2,
                                               adiabatic_focus_alg=3, adiabatic_change_alg=3),
 }
-SHELL = {"shell_1x1_faces": 0.5, "shell_2x2_faces": 0.05, "shell_3x2_capped_alg3": 50.0}
+SHELL = {"shell_1x1_faces": 0.5, "shell_2x2_faces": 0.05, "shell_3x2_capped_alg3": 50.0,
+         "drift_shell_3x2": 0.05}
+# drift (DriftShellData with curlBoverB2 from the analytic updateMhd), alone,
+# with shell diffusion, and through the ideal shock
+CASES.update({
+    "drift_2x2_faces": lambda: W.custom(2, 2, 24, 10, 8, num_ep_steps=3),
+    "drift_shell_3x2": lambda: W.custom(3, 2, 16, 8, 6, num_ep_steps=2),
+    "drift_cone_shock": lambda: W.testsuite_like("cone", 1, 1, 40),
+})
+DRIFT = {"drift_2x2_faces", "drift_shell_3x2", "drift_cone_shock"}
 
 
 def _reference_run(name, q):
@@ -39,6 +48,9 @@ def _reference_run(name, q):
     ref = O.Reference()
     g = ref.setup(w)
     news = ref.shell_diffusion(SHELL[name], w.dims().num_streams) if name in SHELL else None
+    lnpmin = None
+    if name in DRIFT:
+        news, lnpmin = ref.drift(w.dims().num_streams)
     nodes0 = W.initial_nodes(w)
     f0 = np.zeros(w.cells)
     ref.load(f0, nodes0)
@@ -56,7 +68,7 @@ def _reference_run(name, q):
     f_out = np.zeros_like(f_in)
     nodes_out = np.zeros_like(nodes_in)
     ref.store(f_out, nodes_out)
-    q.put((g, nodes0, nodes_in, f_in, f_out, nodes_out, outs, news))
+    q.put((g, nodes0, nodes_in, f_in, f_out, nodes_out, outs, news, lnpmin))
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -65,7 +77,8 @@ def test_oracle_bit_exact_with_reference(name, oracle_lib):
     q = ctx.Queue()
     p = ctx.Process(target=_reference_run, args=(name, q))
     p.start()
-    g_ref, nodes0, nodes_in_ref, f_in, f_out_ref, nodes_out_ref, outs, news = q.get(timeout=300)
+    g_ref, nodes0, nodes_in_ref, f_in, f_out_ref, nodes_out_ref, outs, news, lnpmin = q.get(
+        timeout=300)
     p.join()
     w = CASES[name]()
     g = oracle_lib.grids(w.num_energies, w.num_mu, w.e_min, w.e_max, w.mass, w.charge,
@@ -74,15 +87,25 @@ def test_oracle_bit_exact_with_reference(name, oracle_lib):
         assert np.array_equal(np.asarray(g[k]), np.asarray(g_ref[k])), k
     d = w.dims()
     nodes = nodes0.copy()
-    oracle_lib.update_mhd(d, w.params, nodes, 0.0)
+    curl = np.zeros((3, d.num_streams * d.num_nodes)) if name in DRIFT else None
+    oracle_lib.update_mhd(d, w.params, nodes, 0.0, curl)
     oracle_lib.move_nodes(d, w.params, nodes, w.params.t_del)
-    oracle_lib.update_mhd(d, w.params, nodes, w.params.t_del)
+    oracle_lib.update_mhd(d, w.params, nodes, w.params.t_del, curl)
     assert np.array_equal(nodes, nodes_in_ref)
     gs, keep = W.grids_struct(g)
     f = f_in.copy()
+    if name in DRIFT:
+        assert lnpmin == W.build_grids(w)["lnpmin"]
+        dp = W.drift_params(w, W.build_grids(w))
+        assert np.any(curl != 0.0)
     for call in range(2):
-        shell = {} if news is None else {"news": news, "kperxkpar": SHELL[name]}
-        rc, st, err = oracle_lib.update_energetic_particles(d, w.params, gs, f, nodes, **shell)
+        if name in DRIFT:
+            rc, st, err = oracle_lib.update_energetic_particles_perp(
+                d, w.params, gs, f, nodes, news, SHELL.get(name), dp, curl)
+        else:
+            shell = {} if news is None else {"news": news, "kperxkpar": SHELL[name]}
+            rc, st, err = oracle_lib.update_energetic_particles(d, w.params, gs, f, nodes,
+                                                                **shell)
         assert rc == outs[call][0] == 0, err
         assert (st.max_subcycles_change, st.max_subcycles_focusing) == outs[call][1:3]
         assert st.min_tau == outs[call][3]
