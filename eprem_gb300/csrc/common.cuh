@@ -26,6 +26,7 @@ constexpr double kVerySmall = 1.0e-33;
 constexpr double kTau = kAu / kC;
 constexpr double kDay = kTau / (24.0 * 60.0 * 60.0);
 constexpr double kMhdDensityNorm = 1.0;
+constexpr double kQ = 4.80320425e-10;  // proton charge (esu), src/baseTypes.h:61
 
 // Device status: first failure wins.
 struct DevStatus {
@@ -48,6 +49,8 @@ struct EnergyConsts {
   float dvi32;           // vgrid_i[e+1] - vgrid_i[e-1] (0 at the ends), from FP64
   int seed_k;            // FP32 streaming seeds are held as seed * 2^seed_k, so that
                          // the energy-only factor of sepSeedFunction is near 1
+  double drift_factor;   // (1/om1) p v / 3 of driftVelocity (src/energeticParticles.c:
+                         // 210-246), p = exp(lnpmin + E dlnp); 0 without drift
 };
 
 // Per-node coefficients of the FP32 focusing / change kernels, fixed for one
@@ -69,6 +72,7 @@ struct RunView {
   int precision;
   void *f;                 // Real*
   short *fexp;             // [S][N][E] FP32 form: row exponents, f = f_stored * 2^-fexp
+  double *curl;            // [3][S*N] curl(B)/B^2 (r, theta, phi) with drift on, else null
   double *nodes;           // [NF][S*N]
   const double *mugrid;    // [M]
   const EnergyConsts *ec;  // [E]

@@ -13,11 +13,14 @@
 using namespace eprem;
 
 // ---- autotuner ---------------------------------------------------------------
-// Times the FP32 streaming-kernel shapes on a scratch copy of the run's first
-// streams (the kernel that takes 90 % of a step) and keeps the fastest.  The
-// copy has its own status block, so the run's statistics are untouched.
+// Times the FP32 streaming kernels on a scratch copy of the run's first
+// streams (the kernel that takes 90 % of a step) and keeps the fastest: every
+// kind that fits the run (compile-time guards, packed, scalar) in every CTA
+// shape of its mu bin (threads per CTA, list nodes per thread, and so the
+// cluster size for the run's stream length).  The copy has its own status
+// block, so the run's statistics are untouched.
 namespace {
-constexpr int kTuneVariants[] = {5, 4, 3};
+constexpr int kTuneKinds[] = {5, 4, 3};
 
 int tune_stream(eprem_gpu_run *r, int *chosen) {
   const eprem_params_t &p = r->params;
@@ -55,7 +58,10 @@ int tune_stream(eprem_gpu_run *r, int *chosen) {
   int best_variant = 0;
   StreamPlan best_plan{};
   uint64_t dummy = 0;
-  for (int variant : kTuneVariants) {
+  std::vector<int> variants;
+  for (int shape = 1; shape <= stream2_shape_count(r->dims.num_mu); ++shape)
+    for (int kind : kTuneKinds) variants.push_back(kind + 8 * shape);
+  for (int variant : variants) {
     if (e != cudaSuccess) break;
     StreamPlan pl{};
     if (plan_stream(EPREM_FP32, r->dims.num_nodes, r->dims.num_mu, r->m0, variant, &pl)) continue;
@@ -128,7 +134,9 @@ struct eprem_gpu_ensemble {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> launches_per_step;
-  int chains = 1;  // serial chains side by side; 0: one branch per run
+  int chains = -1;  // < 0 lock-step with merged streaming; 0 one branch per run; k serial chains
+  // lock-step: the slab lists of the merged streaming launches
+  std::vector<int4 *> d_items;
 };
 
 static void ensemble_drop_graph(eprem_gpu_ensemble *e) {
@@ -136,6 +144,8 @@ static void ensemble_drop_graph(eprem_gpu_ensemble *e) {
   if (e->graph) cudaGraphDestroy(e->graph);
   e->exec = nullptr;
   e->graph = nullptr;
+  for (int4 *p : e->d_items) cudaFree(p);
+  e->d_items.clear();
 }
 
 extern "C" int eprem_gpu_ensemble_destroy(eprem_gpu_ensemble *e) {
@@ -165,8 +175,9 @@ extern "C" int eprem_gpu_ensemble_create(eprem_gpu_run *const *runs, int n,
                   "ensemble steps use the analytic background; MAS runs step one by one");
     if (runs[i]->surr)
       return fail(EPREM_GPU_ERR_UNSUPPORTED, "surrogate-form runs step one by one");
-    if (runs[i]->shell_on)
-      return fail(EPREM_GPU_ERR_UNSUPPORTED, "runs with shell diffusion step one by one");
+    if (runs[i]->shell_on || runs[i]->drift_on)
+      return fail(EPREM_GPU_ERR_UNSUPPORTED,
+                  "runs with shell diffusion or drift step one by one");
     for (int j = 0; j < i; j++)
       if (runs[j] == runs[i]) return fail(EPREM_GPU_ERR_ARG, "run listed twice in ensemble");
   }
@@ -234,7 +245,161 @@ extern "C" int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *e, int *chosen_va
   return EPREM_GPU_OK;
 }
 
+// Lock-step capture: every run's per-call set-up, then EP sub-step by EP
+// sub-step the streaming of all runs -- one launch per group of runs that
+// share a packed streaming kernel (mu bin, CTA shape, cluster size, guards),
+// the group's (run, stream, energy) slabs ordered by their estimated work,
+// longest first, so the slabs of small runs fill the tails of large ones --
+// and each run's node phase; all on the ensemble's stream.  Each slab and
+// row is computed by the same code as in a run's own update: the results are
+// the runs' own, bit for bit.  Needs the same numEpSteps in every run.
+namespace {
+struct S2Group {
+  StreamPlan plan;
+  std::vector<int> runs;  // ensemble indices
+};
+bool same_plan(const StreamPlan &a, const StreamPlan &b) {
+  return a.mmax == b.mmax && a.threads == b.threads && a.npt == b.npt && a.cluster == b.cluster &&
+         a.packed == b.packed && a.filled == b.filled && a.reg_coef == b.reg_coef;
+}
+}  // namespace
+
+static int ensemble_capture_lockstep(eprem_gpu_ensemble *e) {
+  const int n = (int)e->runs.size();
+  // the slabs' work estimates need each run's stream geometry: one geometry
+  // pass (its values are the ones the step itself forms, up to the step's
+  // node motion) before the capture
+  std::vector<std::vector<double>> ds_min(n);
+  std::vector<std::vector<int>> list_size(n);
+  for (int i = 0; i < n; i++) {
+    eprem_gpu_run *r = e->runs[i];
+    const eprem_params_t &p = r->params;
+    if (launch_geometry(r->v, r->stream, r->norm_radius, r->neg_beta, p.mfp_type,
+                        p.mfp_type == 2 ? p.mfp_b_power : p.mfp_radial_power, p.mhd_bs_au,
+                        &r->launches))
+      return cuda_fail(cudaGetLastError(), "ensemble geometry launch");
+    const int S = r->dims.num_streams;
+    ds_min[i].resize(S);
+    list_size[i].resize(S);
+    CK(cudaMemcpyAsync(ds_min[i].data(), r->d_ds_min, S * sizeof(double),
+                       cudaMemcpyDeviceToHost, r->stream));
+    CK(cudaMemcpyAsync(list_size[i].data(), r->d_list_size, S * sizeof(int),
+                       cudaMemcpyDeviceToHost, r->stream));
+    CK(cudaStreamSynchronize(r->stream));
+  }
+  std::vector<S2Group> groups;
+  std::vector<int> solo;
+  for (int i = 0; i < n; i++) {
+    eprem_gpu_run *r = e->runs[i];
+    const StreamPlan &pl = r->splan;
+    if (!r->v.use_stream || pl.reg_coef != 2 || !pl.packed) {
+      solo.push_back(i);
+      continue;
+    }
+    bool found = false;
+    for (auto &g : groups)
+      if (same_plan(g.plan, pl) && (int)g.runs.size() < kMultiRuns) {
+        g.runs.push_back(i);
+        found = true;
+        break;
+      }
+    if (!found) groups.push_back({pl, {i}});
+  }
+  std::vector<MultiRunViews> views(groups.size());
+  std::vector<int> n_items(groups.size());
+  for (size_t gi = 0; gi < groups.size(); gi++) {
+    std::vector<std::pair<double, int4>> items;
+    for (int j = 0; j < (int)groups[gi].runs.size(); j++) {
+      eprem_gpu_run *r = e->runs[groups[gi].runs[j]];
+      views[gi].v[j] = r->v;
+      views[gi].m0[j] = r->m0;
+      const double dt = r->v.dt;
+      for (int s = 0; s < r->dims.num_streams; s++)
+        for (int en = 0; en < r->dims.num_energies; en++) {
+          const double dtMin = 0.4 * ds_min[groups[gi].runs[j]][s] * r->h_ec[en].vgrid_i;
+          const double nst = dtMin > 0.0 ? floor(dt / dtMin + 1.0) : 1.0;
+          const double cost = nst * list_size[groups[gi].runs[j]][s] * r->dims.num_mu;
+          items.push_back({cost, make_int4(j, s, en, 0)});
+        }
+    }
+    std::stable_sort(items.begin(), items.end(),
+                     [](const auto &a, const auto &b) { return a.first > b.first; });
+    std::vector<int4> flat(items.size());
+    for (size_t k = 0; k < items.size(); k++) flat[k] = items[k].second;
+    int4 *d = nullptr;
+    CK(cudaMalloc(&d, flat.size() * sizeof(int4)));
+    e->d_items.push_back(d);
+    CK(cudaMemcpy(d, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    n_items[gi] = (int)flat.size();
+  }
+  std::vector<bool> saved(n);
+  std::vector<cudaStream_t> own(n);
+  for (int i = 0; i < n; i++) {
+    saved[i] = e->runs[i]->timing;
+    own[i] = e->runs[i]->stream;
+    e->runs[i]->timing = false;       // no event bookkeeping inside a graph
+    e->runs[i]->stream = e->origin;   // every launch on the ensemble's stream
+  }
+  std::vector<uint64_t> l0(n);
+  for (int i = 0; i < n; i++) l0[i] = e->runs[i]->launches;
+  CK(cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeRelaxed));
+  int rc = EPREM_GPU_OK;
+  cudaError_t err = cudaSuccess;
+  const int nsub = e->runs[0]->params.num_ep_steps;
+  for (int i = 0; i < n && !rc && err == cudaSuccess; i++) {
+    eprem_gpu_run *r = e->runs[i];
+    const double td = r->params.t_del;
+    if (launch_move_nodes(r->v, td, r->stream, &r->launches) ||
+        launch_update_mhd(r->v, r->mhd, td, r->stream, &r->launches, e->d_time + i))
+      err = cudaGetLastError();
+    else
+      rc = ep_begin(r, r->v);
+  }
+  for (int step = 0; step < nsub && !rc && err == cudaSuccess; step++) {
+    for (size_t gi = 0; gi < groups.size() && !rc; gi++)
+      if (launch_stream2_multi(groups[gi].plan, views[gi], e->d_items[gi], n_items[gi],
+                               e->origin, &e->runs[groups[gi].runs[0]]->launches))
+        err = cudaGetLastError();
+    for (int i : solo)
+      if (!rc && err == cudaSuccess) rc = ep_stream_phase(e->runs[i], e->runs[i]->v);
+    for (int i = 0; i < n && !rc && err == cudaSuccess; i++)
+      rc = ep_node_phase(e->runs[i], e->runs[i]->v);
+  }
+  for (int i = 0; i < n && !rc && err == cudaSuccess; i++) {
+    eprem_gpu_run *r = e->runs[i];
+    if (launch_advance_time(e->d_time + i, r->params.t_del, r->stream, &r->launches))
+      err = cudaGetLastError();
+  }
+  for (int i = 0; i < n; i++) {
+    e->runs[i]->timing = saved[i];
+    e->runs[i]->stream = own[i];
+    e->launches_per_step[i] = e->runs[i]->launches - l0[i];
+    e->runs[i]->launches = l0[i];  // counted again at every replay
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(e->origin, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (err == cudaSuccess) err = end;
+  if (err == cudaSuccess) err = cudaGraphInstantiate(&e->exec, g, 0);
+  if (err != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    e->exec = nullptr;
+    return cuda_fail(err, "ensemble step capture");
+  }
+  e->graph = g;
+  return EPREM_GPU_OK;
+}
+
 static int ensemble_capture(eprem_gpu_ensemble *e) {
+  if (e->chains < 0) {
+    bool same = true;
+    for (eprem_gpu_run *r : e->runs)
+      same = same && r->params.num_ep_steps == e->runs[0]->params.num_ep_steps;
+    if (same) return ensemble_capture_lockstep(e);
+  }
   const int n = (int)e->runs.size();
   std::vector<bool> saved(n);
   for (int i = 0; i < n; i++) saved[i] = e->runs[i]->timing;
@@ -242,7 +407,7 @@ static int ensemble_capture(eprem_gpu_ensemble *e) {
   int rc = EPREM_GPU_OK;
   cudaError_t err = cudaEventRecord(e->fork, e->origin);
   // chain of each run: largest run first onto the chain with the fewest cells
-  const int nch = (e->chains <= 0 || e->chains > n) ? n : e->chains;
+  const int nch = (e->chains == 0 || e->chains > n) ? n : (e->chains < 0 ? 1 : e->chains);
   std::vector<int> order(n), chain_of(n, 0);
   for (int i = 0; i < n; i++) order[i] = i;
   auto cells = [&](int i) { return (double)e->runs[i]->cells(); };
@@ -301,7 +466,7 @@ static int ensemble_capture(eprem_gpu_ensemble *e) {
 
 extern "C" int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *e, int chains) {
   if (!e) return fail(EPREM_GPU_ERR_ARG, "null ensemble");
-  if (chains < 0) return fail(EPREM_GPU_ERR_ARG, "chains must be >= 0");
+  if (chains < 0) chains = -1;
   if (chains != e->chains) {
     if (e->origin) CK(cudaStreamSynchronize(e->origin));
     ensemble_drop_graph(e);
@@ -313,8 +478,9 @@ extern "C" int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *e, int chains) 
 extern "C" int eprem_gpu_ensemble_step(eprem_gpu_ensemble *e) {
   if (!e) return fail(EPREM_GPU_ERR_ARG, "null ensemble");
   for (eprem_gpu_run *r : e->runs)  // switched on after the ensemble was made
-    if (r->shell_on)
-      return fail(EPREM_GPU_ERR_UNSUPPORTED, "runs with shell diffusion step one by one");
+    if (r->shell_on || r->drift_on)
+      return fail(EPREM_GPU_ERR_UNSUPPORTED,
+                  "runs with shell diffusion or drift step one by one");
   if (!e->exec) {
     const int rc = ensemble_capture(e);
     if (rc) return rc;

@@ -118,6 +118,7 @@ static int validate(const eprem_dims_t *d, const eprem_params_t *p, const eprem_
 namespace {
 int flux_static_buffer(int device, double **out);
 }
+static int mas_mark_used(eprem_gpu_run *r);
 
 template <typename T>
 static cudaError_t dalloc(T **p, size_t n) {
@@ -217,6 +218,8 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   }
   std::vector<float> mu32(M);
   for (int m = 0; m < M; m++) mu32[m] = (float)grids->mugrid[m];
+  for (int i = 0; i < E; i++) ec[i].drift_factor = 0.0;
+  r->h_ec = ec;
   e = cudaMemcpyAsync(r->d_ec, ec.data(), E * sizeof(EnergyConsts), cudaMemcpyHostToDevice, r->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(r->d_mugrid, grids->mugrid, M * sizeof(double), cudaMemcpyHostToDevice, r->stream);
@@ -232,6 +235,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
     eprem_gpu_destroy(r);
     return fail(rc, "cannot reserve shared memory for the stream-list kernel");
   }
+  r->grid_dlnp = grids->dlnp;
   r->norm_radius = p.bf_r0 / p.r_scale;
   r->neg_beta = -p.bf_beta;
   RunView &v = r->v;
@@ -293,6 +297,7 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
 extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   if (!r) return EPREM_GPU_OK;
   if (r->stream) cudaStreamSynchronize(r->stream);
+  if (r->copy_stream) cudaStreamSynchronize(r->copy_stream);  // slice copies may be queued
   cudaFree(r->d_f);
   cudaFree(r->d_fexp);
   cudaFree(r->d_shell_fexp);
@@ -321,9 +326,17 @@ extern "C" int eprem_gpu_destroy(eprem_gpu_run *r) {
   cudaFree(r->d_shell_ent);
   cudaFree(r->d_shell_del);
   cudaFree(r->d_shell_f);
+  cudaFree(r->d_curl);
+  cudaFree(r->d_drift_news);
+  cudaFree(r->d_drift_ent);
+  cudaFree(r->d_drift_del);
   for (cudaEvent_t ev : r->ev_pool) cudaEventDestroy(ev);
   for (auto &slot : r->mas_allocs)
     for (void *p : slot) cudaFree(p);
+  for (cudaEvent_t ev : r->mas_ready_ev)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : r->mas_used_ev)
+    if (ev) cudaEventDestroy(ev);
   if (r->h_status) cudaFreeHost(r->h_status);
   if (r->stream) cudaStreamDestroy(r->stream);
   delete r;
@@ -528,8 +541,11 @@ static RunView stream_range_view(const eprem_gpu_run *r, int s0, int s1) {
   return u;
 }
 
-// updateEnergeticParticles on the streams of view v, on the run's stream.
-static int ep_update(eprem_gpu_run *r, const RunView &v) {
+// updateEnergeticParticles on the streams of view v, on the run's stream, in
+// three pieces (ensembles interleave the sub-steps of several runs):
+// ep_begin once per call, then per EP sub-step ep_stream_phase and
+// ep_node_phase.
+int eprem::ep_begin(eprem_gpu_run *r, const RunView &v) {
   const eprem_params_t &p = r->params;
   int rc = timed(r, EPREM_KERNEL_GEOMETRY, [&] {
     return launch_geometry(v, r->stream, r->norm_radius, r->neg_beta, p.mfp_type,
@@ -547,50 +563,86 @@ static int ep_update(eprem_gpu_run *r, const RunView &v) {
                [&] { return launch_node32_setup(v, r->stream, &r->launches); });
     if (rc) return cuda_fail(cudaGetLastError(), "focusing/change set-up launch");
   }
-  // shell diffusion couples the streams: only a whole-run view reaches here
-  // with it on (the stream-range entries route around it)
-  // (each step swaps the run's two f buffers, which v, the run's own view, sees)
-  const bool shell = r->shell_on && &v == &r->v;
-  if (r->shell_on && !shell) return fail(EPREM_GPU_ERR_UNSUPPORTED, "shell diffusion on a stream range");
-  if (shell) {
+  // shell diffusion and drift couple the streams: only a whole-run view
+  // reaches here with them on (the stream-range entries route around them)
+  if (r->shell_on && &v != &r->v)
+    return fail(EPREM_GPU_ERR_UNSUPPORTED, "shell diffusion on a stream range");
+  if (r->drift_on && &v != &r->v) return fail(EPREM_GPU_ERR_UNSUPPORTED, "drift on a stream range");
+  if (r->shell_on) {
     rc = timed(r, EPREM_KERNEL_SHELL, [&] {
       return launch_shell_coef(v, r->d_news, r->kperxkpar, r->d_shell_del, r->stream,
                                &r->launches);
     });
     if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion set-up launch");
   }
-  for (int step = 0; step < p.num_ep_steps; step++) {
-    if (v.use_stream)
-      rc = timed(r, EPREM_KERNEL_STREAM,
-                 [&] { return launch_stream(v, r->splan, r->m0, r->stream, &r->launches); });
-    else if (v.check_seed)
-      rc = timed(r, EPREM_KERNEL_SEED_CHECK,
-                 [&] { return launch_seed_check(v, r->stream, &r->launches); });
-    if (rc) return cuda_fail(cudaGetLastError(), "streaming launch");
-    if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {
-      rc = timed(r, EPREM_KERNEL_NODE, [&] { return split_node_phase(r); });
-      if (rc) return rc == EPREM_GPU_ERR_CUDA ? cuda_fail(cudaGetLastError(), "split node phase") : rc;
-    } else if (v.use_focus || v.use_change) {
-      rc = timed(r, EPREM_KERNEL_NODE, [&] {
-        return r->nplan.fast32 ? launch_node32(v, r->nplan, r->stream, &r->launches)
-                               : launch_node(v, r->nplan, r->stream, &r->launches);
-      });
-      if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
-    }
-    // DiffuseShellData after every stream's sub-step (src/energeticParticles.c:178-182)
-    if (shell) {
-      rc = timed(r, EPREM_KERNEL_SHELL, [&] {
-        return launch_shell_diffuse(v, r->d_shell_ent, r->shell_L, r->d_shell_del, r->d_shell_f,
-                                    r->d_shell_fexp, r->stream, &r->launches);
-      });
-      if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion launch");
-      std::swap(r->d_f, r->d_shell_f);  // the new f is the other buffer
-      std::swap(r->d_fexp, r->d_shell_fexp);
-      r->v.f = r->d_f;
-      r->v.fexp = r->d_fexp;
-    }
+  if (r->drift_on && r->drift_links) {
+    rc = timed(r, EPREM_KERNEL_SHELL, [&] {
+      return launch_drift_coef(v, r->d_drift_news, r->d_drift_del, r->stream, &r->launches);
+    });
+    if (rc) return cuda_fail(cudaGetLastError(), "drift set-up launch");
   }
   return EPREM_GPU_OK;
+}
+
+int eprem::ep_stream_phase(eprem_gpu_run *r, const RunView &v) {
+  int rc = EPREM_GPU_OK;
+  if (v.use_stream)
+    rc = timed(r, EPREM_KERNEL_STREAM,
+               [&] { return launch_stream(v, r->splan, r->m0, r->stream, &r->launches); });
+  else if (v.check_seed)
+    rc = timed(r, EPREM_KERNEL_SEED_CHECK,
+               [&] { return launch_seed_check(v, r->stream, &r->launches); });
+  return rc ? cuda_fail(cudaGetLastError(), "streaming launch") : EPREM_GPU_OK;
+}
+
+int eprem::ep_node_phase(eprem_gpu_run *r, const RunView &v) {
+  int rc = EPREM_GPU_OK;
+  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE) {
+    rc = timed(r, EPREM_KERNEL_NODE, [&] { return split_node_phase(r); });
+    if (rc) return rc == EPREM_GPU_ERR_CUDA ? cuda_fail(cudaGetLastError(), "split node phase") : rc;
+  } else if (v.use_focus || v.use_change) {
+    rc = timed(r, EPREM_KERNEL_NODE, [&] {
+      return r->nplan.fast32 ? launch_node32(v, r->nplan, r->stream, &r->launches)
+                             : launch_node(v, r->nplan, r->stream, &r->launches);
+    });
+    if (rc) return cuda_fail(cudaGetLastError(), "focusing/change launch");
+  }
+  // (each perpendicular step swaps the run's two f buffers, which v, the
+  // run's own view, sees)
+  // DiffuseShellData after every stream's sub-step (src/energeticParticles.c:178-182)
+  if (r->shell_on) {
+    rc = timed(r, EPREM_KERNEL_SHELL, [&] {
+      return launch_shell_diffuse(v, r->d_shell_ent, r->shell_L, r->d_shell_del, r->d_shell_f,
+                                  r->d_shell_fexp, r->stream, &r->launches);
+    });
+    if (rc) return cuda_fail(cudaGetLastError(), "shell diffusion launch");
+    std::swap(r->d_f, r->d_shell_f);  // the new f is the other buffer
+    std::swap(r->d_fexp, r->d_shell_fexp);
+    r->v.f = r->d_f;
+    r->v.fexp = r->d_fexp;
+  }
+  // DriftShellData after the shell diffusion (src/energeticParticles.c:186-190)
+  if (r->drift_on && r->drift_links) {
+    rc = timed(r, EPREM_KERNEL_SHELL, [&] {
+      return launch_shell_diffuse(v, r->d_drift_ent, r->drift_L, r->d_drift_del, r->d_shell_f,
+                                  r->d_shell_fexp, r->stream, &r->launches, true);
+    });
+    if (rc) return cuda_fail(cudaGetLastError(), "drift launch");
+    std::swap(r->d_f, r->d_shell_f);
+    std::swap(r->d_fexp, r->d_shell_fexp);
+    r->v.f = r->d_f;
+    r->v.fexp = r->d_fexp;
+  }
+  return EPREM_GPU_OK;
+}
+
+static int ep_update(eprem_gpu_run *r, const RunView &v) {
+  int rc = ep_begin(r, v);
+  for (int step = 0; step < r->params.num_ep_steps && !rc; step++) {
+    rc = ep_stream_phase(r, v);
+    if (!rc) rc = ep_node_phase(r, v);
+  }
+  return rc;
 }
 
 extern "C" int eprem_gpu_update_energetic_particles(eprem_gpu_run *r, double t_global) {
@@ -615,8 +667,8 @@ extern "C" int eprem_gpu_update_energetic_particles_host(eprem_gpu_run *r, const
   const size_t per_stream = (size_t)r->dims.num_nodes * r->dims.num_energies * r->dims.num_mu;
   const size_t pitch = stream_pitch ? stream_pitch : per_stream;
   if (pitch < per_stream) return fail(EPREM_GPU_ERR_ARG, "stream_pitch below N*E*M");
-  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE || r->shell_on) {
-    // those phases, and shell diffusion, work on the whole run
+  if (r->node_mode != EPREM_NODE_PHASE_REFERENCE || r->shell_on || r->drift_on) {
+    // those phases, shell diffusion and drift work on the whole run
     int rc = eprem_gpu_upload_f_pitched(r, f_in, pitch);
     if (!rc) rc = ep_update(r, r->v);
     if (!rc) rc = eprem_gpu_download_f_pitched(r, f_out, pitch);
@@ -730,6 +782,9 @@ extern "C" int eprem_gpu_read_stats(eprem_gpu_run *r, eprem_ep_stats_t *stats) {
 
 extern "C" int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  if (r->mas_on && r->drift_on)
+    return fail(EPREM_GPU_ERR_UNSUPPORTED,
+                "drift with the MAS background (masGetNode does not form curl(B)/B^2)");
   if (r->mas_on) {
     if (!r->mas_selected)
       return fail(EPREM_GPU_ERR_STATE, "MAS background: no time slices selected");
@@ -737,7 +792,7 @@ extern "C" int eprem_gpu_update_mhd(eprem_gpu_run *r, double t_global) {
           return launch_mas_update_mhd(r->v, r->mv, r->params.t_del, r->stream, &r->launches);
         }))
       return cuda_fail(cudaGetLastError(), "updateMhd (MAS) launch");
-    return EPREM_GPU_OK;
+    return mas_mark_used(r);
   }
   if (timed(r, EPREM_KERNEL_MHD,
             [&] { return launch_update_mhd(r->v, r->mhd, t_global, r->stream, &r->launches); }))
@@ -755,6 +810,13 @@ extern "C" int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp
   r->mas_allocs.assign(mp->max_slices, {});
   r->mas_slots.assign(mp->max_slices, MasSlotDev{});
   r->mas_loaded.assign(mp->max_slices, 0);
+  for (cudaEvent_t ev : r->mas_ready_ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : r->mas_used_ev) cudaEventDestroy(ev);
+  r->mas_ready_ev.assign(mp->max_slices, nullptr);
+  r->mas_used_ev.assign(mp->max_slices, nullptr);
+  r->mas_pending.assign(mp->max_slices, 0);
+  r->mas_used.assign(mp->max_slices, 0);
+  r->mas_sel[0] = r->mas_sel[1] = -1;
   r->mv.radial_max = mp->radial_max;
   r->mv.v_min = mp->v_min;
   r->mv.cor_rotate_fake = mp->cor_rotate_fake;
@@ -764,37 +826,100 @@ extern "C" int eprem_gpu_mas_init(eprem_gpu_run *r, const eprem_mas_params_t *mp
   return EPREM_GPU_OK;
 }
 
-extern "C" int eprem_gpu_mas_load_slice(eprem_gpu_run *r, int slot, const eprem_mas_slice_t *s) {
+// One slice into device slot `slot`.  The slot's device arrays are kept
+// from load to load while the slice's dimensions stay the same (a MAS run
+// keeps one grid), so later loads allocate nothing.  async: the copies run
+// on the run's copy stream after the slot's last reader, and selecting the
+// slot makes the run's stream wait for them; otherwise they run on the run's
+// stream and the call returns once they are done.
+static int mas_store(eprem_gpu_run *r, int slot, const eprem_mas_slice_t *s, bool async) {
   if (!r || !s) return fail(EPREM_GPU_ERR_ARG, "null argument");
   if (!r->mas_ready) return fail(EPREM_GPU_ERR_STATE, "eprem_gpu_mas_init first");
   if (slot < 0 || slot >= (int)r->mas_slots.size()) return fail(EPREM_GPU_ERR_ARG, "slot out of range");
-  CK(cudaStreamSynchronize(r->stream));
-  for (void *p : r->mas_allocs[slot]) cudaFree(p);
-  r->mas_allocs[slot].clear();
+  if (async && (slot == r->mas_sel[0] || slot == r->mas_sel[1]))
+    return fail(EPREM_GPU_ERR_STATE, "an asynchronous load needs a slot that is not selected");
+  for (int f = 0; f < EPREM_MAS_NFIELDS; f++) {
+    if (!s->data[f]) return fail(EPREM_GPU_ERR_ARG, "null MAS field");
+    for (int a = 0; a < 3; a++)
+      if (s->dims[f][a] < 2 || !s->mesh[f][a])
+        return fail(EPREM_GPU_ERR_ARG, "MAS meshes need >= 2 points");
+  }
+  MasSlotDev &dev = r->mas_slots[slot];
+  bool same = !r->mas_allocs[slot].empty();
+  for (int f = 0; f < EPREM_MAS_NFIELDS && same; f++)
+    for (int a = 0; a < 3; a++) same = same && dev.dims[f][a] == s->dims[f][a];
+  if (!r->mas_ready_ev[slot]) {
+    CK(cudaEventCreateWithFlags(&r->mas_ready_ev[slot], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&r->mas_used_ev[slot], cudaEventDisableTiming));
+  }
+  if (async && !r->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &ev : r->stage_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  if (!same) {  // first load of the slot, or a new grid: (re)allocate, nothing in flight
+    CK(cudaStreamSynchronize(r->stream));
+    if (r->copy_stream) CK(cudaStreamSynchronize(r->copy_stream));
+    for (void *p : r->mas_allocs[slot]) cudaFree(p);
+    r->mas_allocs[slot].clear();
+    dev = MasSlotDev{};
+    for (int f = 0; f < EPREM_MAS_NFIELDS; f++) {
+      size_t n = 1;
+      for (int a = 0; a < 3; a++) {
+        float *m = nullptr;
+        CK(cudaMalloc(&m, s->dims[f][a] * sizeof(float)));
+        r->mas_allocs[slot].push_back(m);
+        dev.mesh[f][a] = m;
+        dev.dims[f][a] = s->dims[f][a];
+        n *= (size_t)s->dims[f][a];
+      }
+      float *v = nullptr;
+      CK(cudaMalloc(&v, n * sizeof(float)));
+      r->mas_allocs[slot].push_back(v);
+      dev.data[f] = v;
+    }
+  }
   r->mas_loaded[slot] = 0;
-  MasSlotDev dev{};
+  cudaStream_t cs = async ? r->copy_stream : r->stream;
+  if (async && r->mas_used[slot]) CK(cudaStreamWaitEvent(cs, r->mas_used_ev[slot], 0));
   for (int f = 0; f < EPREM_MAS_NFIELDS; f++) {
     size_t n = 1;
     for (int a = 0; a < 3; a++) {
-      const int d = s->dims[f][a];
-      if (d < 2 || !s->mesh[f][a]) return fail(EPREM_GPU_ERR_ARG, "MAS meshes need >= 2 points");
-      n *= (size_t)d;
-      float *m = nullptr;
-      CK(cudaMalloc(&m, d * sizeof(float)));
-      r->mas_allocs[slot].push_back(m);
-      CK(cudaMemcpy(m, s->mesh[f][a], d * sizeof(float), cudaMemcpyHostToDevice));
-      dev.mesh[f][a] = m;
-      dev.dims[f][a] = d;
+      CK(cudaMemcpyAsync(const_cast<float *>(dev.mesh[f][a]), s->mesh[f][a],
+                         s->dims[f][a] * sizeof(float), cudaMemcpyHostToDevice, cs));
+      n *= (size_t)s->dims[f][a];
     }
-    if (!s->data[f]) return fail(EPREM_GPU_ERR_ARG, "null MAS field");
-    float *v = nullptr;
-    CK(cudaMalloc(&v, n * sizeof(float)));
-    r->mas_allocs[slot].push_back(v);
-    CK(cudaMemcpy(v, s->data[f], n * sizeof(float), cudaMemcpyHostToDevice));
-    dev.data[f] = v;
+    CK(cudaMemcpyAsync(const_cast<float *>(dev.data[f]), s->data[f], n * sizeof(float),
+                       cudaMemcpyHostToDevice, cs));
   }
-  r->mas_slots[slot] = dev;
+  if (async) {
+    CK(cudaEventRecord(r->mas_ready_ev[slot], cs));
+    r->mas_pending[slot] = 1;
+  } else {
+    CK(cudaStreamSynchronize(cs));
+    r->mas_pending[slot] = 0;
+  }
   r->mas_loaded[slot] = 1;
+  return EPREM_GPU_OK;
+}
+
+extern "C" int eprem_gpu_mas_load_slice(eprem_gpu_run *r, int slot, const eprem_mas_slice_t *s) {
+  return mas_store(r, slot, s, false);
+}
+
+extern "C" int eprem_gpu_mas_load_slice_async(eprem_gpu_run *r, int slot,
+                                              const eprem_mas_slice_t *s) {
+  return mas_store(r, slot, s, true);
+}
+
+// After a launch that reads the selected slots: mark them read (an async
+// load into either waits for this point of the run's stream).
+static int mas_mark_used(eprem_gpu_run *r) {
+  for (int i = 0; i < 2; i++) {
+    const int sl = r->mas_sel[i];
+    if (sl < 0) continue;
+    CK(cudaEventRecord(r->mas_used_ev[sl], r->stream));
+    r->mas_used[sl] = 1;
+  }
   return EPREM_GPU_OK;
 }
 
@@ -806,10 +931,17 @@ extern "C" int eprem_gpu_mas_select(eprem_gpu_run *r, int slot0, int slot1, doub
   if (slot0 < 0 || slot0 >= n || slot1 < 0 || slot1 >= n || !r->mas_loaded[slot0] ||
       !r->mas_loaded[slot1])
     return fail(EPREM_GPU_ERR_ARG, "MAS slot not loaded");
+  for (int sl : {slot0, slot1})
+    if (r->mas_pending[sl]) {  // an asynchronous load: the run's stream waits for its copies
+      CK(cudaStreamWaitEvent(r->stream, r->mas_ready_ev[sl], 0));
+      r->mas_pending[sl] = 0;
+    }
   r->mv.s0 = r->mas_slots[slot0];
   r->mv.s1 = r->mas_slots[slot1];
   r->mv.s_cor = s_cor;
   r->mv.phi_offset = phi_offset;
+  r->mas_sel[0] = slot0;
+  r->mas_sel[1] = slot1;
   r->mas_selected = true;
   return EPREM_GPU_OK;
 }
@@ -828,7 +960,7 @@ extern "C" int eprem_gpu_mas_move_nodes(eprem_gpu_run *r, double dt) {
   if (timed(r, EPREM_KERNEL_MOVE,
             [&] { return launch_mas_move_nodes(r->v, r->mv, dt, r->stream, &r->launches); }))
     return cuda_fail(cudaGetLastError(), "masMoveNodes launch");
-  return EPREM_GPU_OK;
+  return mas_mark_used(r);
 }
 
 extern "C" int eprem_gpu_move_nodes(eprem_gpu_run *r, double dt) {
@@ -850,9 +982,103 @@ extern "C" int eprem_gpu_set_time_step(eprem_gpu_run *r, double t_del) {
   return EPREM_GPU_OK;
 }
 
+// The second f buffer (and its row exponents) that a perpendicular step
+// writes before it becomes the run's f.
+static int ensure_second_f(eprem_gpu_run *r) {
+  if (r->d_shell_f) return EPREM_GPU_OK;
+  const size_t elem = r->dims.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
+  CK(cudaMalloc(&r->d_shell_f, elem * r->cells() + 16));  // as d_f, tail zeroed as there
+  CK(cudaMemset(r->d_shell_f, 0, elem * r->cells() + 16));
+  if (r->dims.precision == EPREM_FP32) {
+    CK(cudaMalloc(&r->d_shell_fexp, sizeof(short) * r->sn() * r->dims.num_energies + 16));
+    CK(cudaMemset(r->d_shell_fexp, 0, sizeof(short) * r->sn() * r->dims.num_energies));
+  }
+  return EPREM_GPU_OK;
+}
+
+// Per target stream, the NEWS hand-overs it receives in the reference's
+// order (source streams ascending, per source north, east, west, south);
+// with per_direction_loss (DriftShellData) each direction of the target's
+// own row adds its loss right after that direction's gain, else
+// (DiffuseShellData) one summed loss follows the target's four directions.
+// Rows padded with -1 to the longest; *L its length.
+static std::vector<int> news_gather_lists(const int32_t *news, int S, bool per_direction_loss,
+                                          int *L) {
+  std::vector<std::vector<int>> lists(S);
+  for (int i = 0; i < S; i++) {
+    for (int d = 0; d < 4; d++) {
+      lists[news[i * 4 + d]].push_back(i * 8 + d);
+      if (per_direction_loss) lists[i].push_back(i * 8 + 4 + d);
+    }
+    if (!per_direction_loss) lists[i].push_back(i * 8 + 4);
+  }
+  size_t n = 0;
+  for (const auto &l : lists) n = std::max(n, l.size());
+  std::vector<int> ent(n * S, -1);
+  for (int j = 0; j < S; j++) std::copy(lists[j].begin(), lists[j].end(), ent.begin() + j * n);
+  *L = (int)n;
+  return ent;
+}
+
+extern "C" int eprem_gpu_set_drift(eprem_gpu_run *r, const int32_t *news,
+                                   const eprem_drift_params_t *dp) {
+  if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  CK(cudaStreamSynchronize(r->stream));  // earlier launches may read what changes here
+  if (!dp) {
+    r->drift_on = false;
+    r->v.curl = nullptr;
+    return EPREM_GPU_OK;
+  }
+  if (r->mas_on)
+    return fail(EPREM_GPU_ERR_UNSUPPORTED,
+                "drift with the MAS background (masGetNode does not form curl(B)/B^2)");
+  if (!(dp->mass > 0.0) || !std::isfinite(dp->charge) || dp->charge == 0.0 ||
+      !std::isfinite(dp->lnpmin))
+    return fail(EPREM_GPU_ERR_ARG, "drift: charge non-zero, mass > 0 and lnpmin finite");
+  const int S = r->dims.num_streams, E = r->dims.num_energies;
+  if (news)
+    for (int i = 0; i < 4 * S; i++)
+      if (news[i] < 0 || news[i] >= S) return fail(EPREM_GPU_ERR_ARG, "NEWS neighbour out of range");
+  // driftVelocity's energy factor (src/energeticParticles.c:222-226), host libm
+  const double mhd_b_norm = sqrt(kMp * kMhdDensityNorm) * kC;  // MHD_B_NORM
+  const double om = mhd_b_norm * kQ * kAu / (kMp * kC * kC);    // OM, src/baseTypes.h:98
+  const double om1 = dp->charge * om / dp->mass;
+  for (int e = 0; e < E; e++) {
+    const double p = exp(dp->lnpmin + e * r->grid_dlnp);
+    r->h_ec[e].drift_factor = (1.0 / om1) * (p * r->h_ec[e].vgrid / 3.0);
+  }
+  CK(cudaMemcpy(r->d_ec, r->h_ec.data(), E * sizeof(EnergyConsts), cudaMemcpyHostToDevice));
+  if (!r->d_curl) {
+    CK(cudaMalloc(&r->d_curl, sizeof(double) * 3 * r->sn()));
+    CK(cudaMemset(r->d_curl, 0, sizeof(double) * 3 * r->sn()));
+  }
+  r->v.curl = r->d_curl;
+  r->drift_on = true;
+  if (news) {
+    int L = 0;
+    const std::vector<int> ent = news_gather_lists(news, S, true, &L);
+    if (!r->d_drift_news) {
+      CK(cudaMalloc(&r->d_drift_news, sizeof(int) * 4 * (size_t)S));
+      const size_t elem = r->dims.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
+      CK(cudaMalloc(&r->d_drift_del, elem * 4 * r->sn() * E));
+    }
+    const int rc = ensure_second_f(r);
+    if (rc) return rc;
+    cudaFree(r->d_drift_ent);
+    r->d_drift_ent = nullptr;
+    CK(cudaMalloc(&r->d_drift_ent, sizeof(int) * ent.size()));
+    CK(cudaMemcpy(r->d_drift_news, news, sizeof(int) * 4 * (size_t)S, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(r->d_drift_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice));
+    r->drift_L = L;
+    r->drift_links = true;
+  }
+  return EPREM_GPU_OK;
+}
+
 extern "C" int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *news,
                                              double kperxkpar) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
+  int rc = EPREM_GPU_OK;
   if (!news) {
     r->shell_on = false;
     return EPREM_GPU_OK;
@@ -866,27 +1092,15 @@ extern "C" int eprem_gpu_set_shell_diffusion(eprem_gpu_run *r, const int32_t *ne
   // Per target stream, its incoming terms in the reference's order: source
   // streams ascending and, per source, north, east, west, south, then the
   // source's own loss (entry source * 8 + 4); rows padded to the longest.
-  std::vector<std::vector<int>> lists(S);
-  for (int i = 0; i < S; i++) {
-    for (int d = 0; d < 4; d++) lists[news[i * 4 + d]].push_back(i * 8 + d);
-    lists[i].push_back(i * 8 + 4);
-  }
-  size_t L = 0;
-  for (const auto &l : lists) L = std::max(L, l.size());
-  std::vector<int> ent(L * S, -1);
-  for (int j = 0; j < S; j++) std::copy(lists[j].begin(), lists[j].end(), ent.begin() + j * L);
+  int L = 0;
+  const std::vector<int> ent = news_gather_lists(news, S, false, &L);
   CK(cudaStreamSynchronize(r->stream));  // earlier launches may read the old lists
   if (!r->d_news) {
-    const size_t elem = r->dims.precision == EPREM_FP32 ? sizeof(float) : sizeof(double);
     CK(cudaMalloc(&r->d_news, sizeof(int) * 4 * (size_t)S));
     CK(cudaMalloc(&r->d_shell_del, sizeof(double) * 5 * r->sn() * r->dims.num_energies));
-    CK(cudaMalloc(&r->d_shell_f, elem * r->cells() + 16));  // as d_f, tail zeroed as there
-    CK(cudaMemset(r->d_shell_f, 0, elem * r->cells() + 16));
-    if (r->dims.precision == EPREM_FP32) {
-      CK(cudaMalloc(&r->d_shell_fexp, sizeof(short) * r->sn() * r->dims.num_energies + 16));
-      CK(cudaMemset(r->d_shell_fexp, 0, sizeof(short) * r->sn() * r->dims.num_energies));
-    }
   }
+  rc = ensure_second_f(r);
+  if (rc) return rc;
   cudaFree(r->d_shell_ent);
   r->d_shell_ent = nullptr;
   CK(cudaMalloc(&r->d_shell_ent, sizeof(int) * ent.size()));

@@ -20,13 +20,25 @@ struct StreamPlan {
   int reg_coef;  // coefficients in registers (1), shared memory (0); 2: stream2.cu
   int packed;    // stream2.cu: fp32x2 arithmetic on pairs of mu cells
   int filled;    // stream2.cu: M fills the bin, m0 = M/2 (guards known at compile time)
+  int npt;       // stream2.cu: list nodes per thread
 };
 int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan);
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches);
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 // stream2.cu -- FP32 streaming, two list nodes per thread (plan.reg_coef == 2)
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan);
+// shape: 0 automatic, k >= 1 the k-th CTA shape of M's bin (stream2_shape_count)
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan);
+int stream2_shape_count(int M);
+// The packed kinds over the slabs of several runs of one plan: the runs'
+// views (a kernel parameter) and items[i] = (run index, stream, energy, 0)
+constexpr int kMultiRuns = 64;
+struct MultiRunViews {
+  RunView v[kMultiRuns];
+  int m0[kMultiRuns];
+};
+int launch_stream2_multi(const StreamPlan &pl, const MultiRunViews &mv, const int4 *items,
+                         int n_items, cudaStream_t st, uint64_t *launches);
 // once per updateEnergeticParticles call, before the stream2 launches
 int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches);
 int launch_stream2(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
@@ -70,9 +82,13 @@ int launch_ripple_f(const RunView &r, const double *tmpl, cudaStream_t st, uint6
 // shell.cu -- cross-field (shell) diffusion (DiffuseShellData, ShellData)
 int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void *del,
                       cudaStream_t st, uint64_t *launches);
-// xout: the FP32 form's output row exponents (null in FP64)
+// xout: the FP32 form's output row exponents (null in FP64); drift: the
+// gather of DriftShellData (lists and fractions of launch_drift_coef)
 int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
-                         short *xout, cudaStream_t st, uint64_t *launches);
+                         short *xout, cudaStream_t st, uint64_t *launches, bool drift = false);
+// DriftShellData's fractions, Real[N][E][S][4], from r.curl and the positions
+int launch_drift_coef(const RunView &r, const int *news, void *del, cudaStream_t st,
+                      uint64_t *launches);
 // FP32 form: rows [row0, row0 + nrows) of view r between an FP64 staging
 // buffer and the device's rows with their exponents
 int launch_convert_f(const RunView &r, size_t row0, size_t nrows, double *stage, int to_device,
@@ -113,6 +129,8 @@ int launch_surr_apply(const RunView &r, size_t row0, size_t nrows, const float *
                       uint64_t *launches);
 int launch_surr_residual(const float *xs, const float *ts, size_t n, const float *mu32,
                          float *res, cudaStream_t st);
+int launch_surr_calib(const float *xs, const float *ts, const float *Y, int ldy, size_t n,
+                      const float *mu32, float *res, float *err, cudaStream_t st);
 int launch_to_bf16(const float *in, void *out, size_t n, cudaStream_t st);
 int launch_gelu_bf16(const float *Z, void *H, size_t n, cudaStream_t st);
 int launch_mse_grad(const float *Y, const float *T, size_t rows, float *dY, void *dYb,

@@ -29,6 +29,58 @@ __device__ double shock_factor(const MhdParams &p, double r, double tg) {
   return 1 + (factor - 1) * falloff;
 }
 
+// parkerB (src/flow.c:443-472) at (r AU, theta), ideal shock included.
+__device__ void parker_b(const MhdParams &p, double r, double theta, double Vr, int isn,
+                         double tg, double B[3]) {
+  B[0] = p.mhd_bs_au / (r * r);
+  B[1] = 0.0;
+  B[2] = -1.0 * r * B[0] * (p.omega_sun / (Vr + kVerySmall)) * sin(theta);
+  if (p.ideal_shock > 0 && isn > 0) {
+    const double sf = shock_factor(p, r, tg);
+    B[0] *= sf;
+    B[1] *= sf;
+    B[2] *= sf;
+  }
+}
+
+// curlBoverB2 (src/flow.c:479-616): curl(B)/B^2 of the Parker field by
+// centred differences at (r +- 0.001 AU, theta +- pi/100, phi +- pi/100),
+// theta folded back into [0, pi]; the field has no phi dependence, so the
+// phi offsets leave r and theta, and their differences vanish as there.
+// Spherical components (r, theta, phi), the reference's operation order.
+__device__ void curl_bover_b2(const MhdParams &p, double x, double y, double z, double Vr,
+                              int isn, double tg, double curl[3]) {
+  const double rcw = 0.001, tcw = kPi / 100.0, pcw = kPi / 100.0;
+  const double rr = p.r_scale * sqrt(x * x + y * y + z * z);
+  const double th = acos(z * p.r_scale / rr);
+  const double rp = rr + rcw, rm = rr - rcw;
+  double tp = th + tcw;
+  if (tp > kPi) tp = 2.0 * kPi - tp;
+  double tm = th - tcw;
+  if (tm < 0.0) tm *= -1.0;
+  double B_rm[3], B_rp[3], B_tm[3], B_tp[3], B_pc[3];
+  parker_b(p, rm, th, Vr, isn, tg, B_rm);
+  parker_b(p, rp, th, Vr, isn, tg, B_rp);
+  parker_b(p, rr, tm, Vr, isn, tg, B_tm);
+  parker_b(p, rr, tp, Vr, isn, tg, B_tp);
+  parker_b(p, rr, th, Vr, isn, tg, B_pc);  // both phi offsets
+  const double m_rm = sqrt(B_rm[0] * B_rm[0] + B_rm[1] * B_rm[1] + B_rm[2] * B_rm[2]);
+  const double m_rp = sqrt(B_rp[0] * B_rp[0] + B_rp[1] * B_rp[1] + B_rp[2] * B_rp[2]);
+  const double m_tm = sqrt(B_tm[0] * B_tm[0] + B_tm[1] * B_tm[1] + B_tm[2] * B_tm[2]);
+  const double m_tp = sqrt(B_tp[0] * B_tp[0] + B_tp[1] * B_tp[1] + B_tp[2] * B_tp[2]);
+  const double m_pc = sqrt(B_pc[0] * B_pc[0] + B_pc[1] * B_pc[1] + B_pc[2] * B_pc[2]);
+  double A, B;
+  A = (0.5 / tcw) * (B_tp[2] * sin(tp) / (m_tp * m_tp) - B_tm[2] * sin(tm) / (m_tm * m_tm));
+  B = (0.5 / pcw) * (B_pc[1] / (m_pc * m_pc) - B_pc[1] / (m_pc * m_pc));
+  curl[0] = (1.0 / (rr * sin(th))) * (A - B);
+  A = (1.0 / sin(th)) * (0.5 / pcw) * (B_pc[0] / (m_pc * m_pc) - B_pc[0] / (m_pc * m_pc));
+  B = (0.5 / rcw) * (rp * B_rp[2] / (m_rp * m_rp) - rm * B_rm[2] / (m_rm * m_rm));
+  curl[1] = (1.0 / rr) * (A - B);
+  A = (0.5 / rcw) * (rp * B_rp[1] / (m_rp * m_rp) - rm * B_rm[1] / (m_rm * m_rm));
+  B = (0.5 / tcw) * (B_tp[0] / (m_tp * m_tp) - B_tm[0] / (m_tm * m_tm));
+  curl[2] = (1.0 / rr) * (A - B);
+}
+
 // tg_dev, when given, holds the run's time on the device (graph replays of an
 // ensemble step); tg is then the offset added to it.
 __global__ void k_update_mhd(RunView r, MhdParams p, double tg, const double *tg_dev) {
@@ -93,6 +145,11 @@ __global__ void k_update_mhd(RunView r, MhdParams p, double tg, const double *tg
     F(EPREM_NODE_BVEC_X) = Br * st * cp + Bt * ct * cp - Bp * sp;
     F(EPREM_NODE_BVEC_Y) = Br * st * sp + Bt * ct * sp + Bp * cp;
     F(EPREM_NODE_BVEC_Z) = Br * ct - Bt * st;
+    if (r.curl) {  // useDrift: mhdCurlBoverB2 (src/flow.c:127-128)
+      double cv[3];
+      curl_bover_b2(p, x, y, z, Vr, isn, tg, cv);
+      for (int c = 0; c < 3; c++) r.curl[(size_t)c * r.node_stride + g] = cv[c];
+    }
     if (k == 0) {  // rank-0 INNER_ACTIVE_SHELL (src/flow.c:131-137)
       F(EPREM_NODE_DUPAR) = 0.0;
       F(EPREM_NODE_DLNB) = 0.0;

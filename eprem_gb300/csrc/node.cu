@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       const double vel1 = mul(mul(0.5, sub(1.0, mul(m1, m1))), add(a, mul(m1, n_b[g])));
       const double va = mul(0.5, add(vel1, vel0));
       vf[(size_t)g * F + e * (M + 1) + j + 1] = va;
-      atomic_max_pos(&vmax_bits[g], fabs(va));
+      // the reference's `if (fabs(va) > vel_abs_max)` passes over a NaN
+      if (!isnan(va)) atomic_max_pos(&vmax_bits[g], fabs(va));
     }
     __syncthreads();
     for (int it = tid; it < Gv * E; it += kNodeThreads) {
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_node(RunView r, int G) {
       const double b = add(mul(mul(mu, mu), sub(n_c[g], n_b[g])),
                            mul(mul(0.5, sub(1.0, mul(mu, mu))), n_b[g]));
       const double vel = mul(n_d[g], add(mul(a, r.ec[e].vgrid_i), b));
-      atomic_max_pos(&vmax_bits[g], fabs(vel));
+      if (!isnan(vel)) atomic_max_pos(&vmax_bits[g], fabs(vel));
       if (e >= 1) {
         const double velm = mul(n_d[g], add(mul(a, r.ec[e - 1].vgrid_i), b));
         vf[(size_t)g * F + e * M + m] = mul(0.5, add(vel, velm));

@@ -242,8 +242,9 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
             const float vel = 0.5f * (1.f - mu * mu) * (a + mu * b);
             if (m >= 1) {
               const float q = sc * 0.5f * (vel + vel_prev);
-              qp[m] = fmaxf(q, 0.f);
-              qn[m] = fminf(q, 0.f);
+              // a NaN face speed reaches f, as in the reference's upwind flux
+              qp[m] = q < 0.f ? 0.f : q;
+              qn[m] = q > 0.f ? 0.f : q;
             }
             vel_prev = vel;
           }

@@ -37,6 +37,7 @@ struct eprem_gpu_run {
   eprem::NodePlan nplan{};
   int m0 = 0;
   double norm_radius = 0, neg_beta = 0;
+  double grid_dlnp = 0;  // dlnp of the momentum grid
   void *d_f = nullptr;
   short *d_fexp = nullptr;  // FP32 form: row exponents [S][N][E]
   double *d_nodes = nullptr, *d_mugrid = nullptr;
@@ -65,6 +66,14 @@ struct eprem_gpu_run {
   void *d_shell_del = nullptr;    // Real[N][E][S][5]
   void *d_shell_f = nullptr;      // Real[S][N][E][M]
   short *d_shell_fexp = nullptr;  // FP32 form: its row exponents
+  // drift (eprem_gpu_set_drift): curl(B)/B^2 per node, the drift NEWS links,
+  // per-target gather lists (S x drift_L) and per-call fractions
+  bool drift_on = false, drift_links = false;
+  double *d_curl = nullptr;       // [3][S*N]
+  int *d_drift_news = nullptr, *d_drift_ent = nullptr;
+  int drift_L = 0;
+  void *d_drift_del = nullptr;    // Real[N][E][S][4]
+  std::vector<eprem::EnergyConsts> h_ec;  // host copy of d_ec
   uint64_t launches = 0;
   // optional per-launch timing: events recorded around each kernel launch
   bool timing = false;
@@ -82,6 +91,10 @@ struct eprem_gpu_run {
   std::vector<std::vector<void *>> mas_allocs;
   std::vector<eprem::MasSlotDev> mas_slots;
   std::vector<char> mas_loaded;
+  // per slot: copy done (async loads, on copy_stream) and last read (on stream)
+  std::vector<cudaEvent_t> mas_ready_ev, mas_used_ev;
+  std::vector<char> mas_pending, mas_used;
+  int mas_sel[2] = {-1, -1};
   eprem::MasView mv{};
   size_t cells() const {
     return (size_t)dims.num_streams * dims.num_nodes * dims.num_energies * dims.num_mu;
@@ -117,5 +130,11 @@ inline int timed(eprem_gpu_run *r, int kind, Fn &&launch) {
 int check_status(eprem_gpu_run *r, bool reset_stats, eprem_ep_stats_t *stats);
 // The node phase of one EP sub-step in the split and surrogate forms.
 int split_node_phase(eprem_gpu_run *r);
+// updateEnergeticParticles in pieces, on the run's stream: the per-call
+// set-up, then per EP sub-step the streaming (or seed check) and the node
+// phase with the perpendicular steps.
+int ep_begin(eprem_gpu_run *r, const RunView &v);
+int ep_stream_phase(eprem_gpu_run *r, const RunView &v);
+int ep_node_phase(eprem_gpu_run *r, const RunView &v);
 
 }  // namespace eprem

@@ -78,6 +78,67 @@ __global__ void k_shell_coef(RunView r, const int *news, double kperxkpar, Real 
   }
 }
 
+// DriftShellData's hand-over fractions (src/energeticParticles.c:561-801):
+// one thread per node (s, k >= 1); per energy the drift velocity of
+// driftVelocity (:210-246: drift_factor times curl(B)/B^2, to Cartesian by
+// sphToCartVector, src/geometry.c:89-125) and per NEWS direction
+// vdp = (v_d . (r_nbr - r)) rScale / dl with dl the neighbour distance of
+// ShellData (:254-413); del = min(vdp dt / dl, 0.025) where vdp > 0, else 0
+// (no hand-over).  del[((k*E + e)*S + s)*4 + d], in the f type.  The
+// reference's expressions and order, no fused multiply-adds.
+template <typename Real>
+__global__ void k_drift_coef(RunView r, const int *news, Real *del) {
+  const size_t SN = (size_t)r.S * r.N;
+  const double *rx = node_field(r, EPREM_NODE_RX), *ry = node_field(r, EPREM_NODE_RY),
+               *rz = node_field(r, EPREM_NODE_RZ);
+  const double rs = r.r_scale;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < SN;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(g / r.N), k = (int)(g % r.N);
+    if (k == 0) continue;
+    const double x = rx[g], y = ry[g], z = rz[g];
+    const double xs = __dmul_rn(x, rs), ys = __dmul_rn(y, rs), zs = __dmul_rn(z, rs);
+    double en[4][3], dl[4];
+    for (int d = 0; d < 4; d++) {
+      const size_t o = (size_t)news[s * 4 + d] * r.N + k;
+      const double ex = __dsub_rn(__dmul_rn(rx[o], rs), xs), ey = __dsub_rn(__dmul_rn(ry[o], rs), ys),
+                   ez = __dsub_rn(__dmul_rn(rz[o], rs), zs);
+      dl[d] = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)));
+      en[d][0] = __dsub_rn(rx[o], x);
+      en[d][1] = __dsub_rn(ry[o], y);
+      en[d][2] = __dsub_rn(rz[o], z);
+    }
+    const double cr = r.curl[g], ct = r.curl[r.node_stride + g], cp = r.curl[2 * r.node_stride + g];
+    const double rmag = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    const double rho2 = __dsub_rn(__dmul_rn(rmag, rmag), __dmul_rn(z, z));
+    const bool axis = __dsub_rn(rmag, fabs(z)) < kVerySmall;
+    for (int e = 0; e < r.E; e++) {
+      const double fac = r.ec[e].drift_factor;
+      const double vr = __dmul_rn(fac, cr), vt = __dmul_rn(fac, ct), vp = __dmul_rn(fac, cp);
+      double vx = 0.0, vy = 0.0;
+      if (!axis) {
+        vx = __dsub_rn(__dadd_rn(__dmul_rn(x / rmag, vr), __dmul_rn(__dmul_rn(x, z) / __dmul_rn(rmag, sqrt(rho2)), vt)),
+                       __dmul_rn(y / sqrt(rho2), vp));
+        vy = __dadd_rn(__dadd_rn(__dmul_rn(y / rmag, vr), __dmul_rn(__dmul_rn(y, z) / __dmul_rn(rmag, sqrt(rho2)), vt)),
+                       __dmul_rn(x / sqrt(rho2), vp));
+      }
+      const double vz = __dsub_rn(__dmul_rn(z / rmag, vr), __dmul_rn(sqrt(rho2) / rmag, vt));
+      Real *out = del + (((size_t)k * r.E + e) * r.S + s) * 4;
+      for (int d = 0; d < 4; d++) {
+        const double dot = __dadd_rn(__dadd_rn(__dmul_rn(vx, en[d][0]), __dmul_rn(vy, en[d][1])),
+                                     __dmul_rn(vz, en[d][2]));
+        const double vdp = __dmul_rn(dot, rs) / dl[d];
+        double dd = 0.0;
+        if (vdp > 0.0) {
+          dd = __dmul_rn(vdp, r.dt) / dl[d];
+          if (dd > 0.025) dd = 0.025;
+        }
+        out[d] = (Real)dd;
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ double sd_fma(double a, double b, double acc) {
   return __dadd_rn(acc, __dmul_rn(a, b));
 }
@@ -136,10 +197,16 @@ __device__ __forceinline__ void st_vec(Real *p, const Real (&x)[V]) {
 // so a gain a f_i stays below 2^120 in an exponent no higher than
 // fexp_i + 17 - log2(a).  Every term is taken to that exponent (exact powers
 // of two) before the sum; xout receives it.
-template <typename Real, int C, int V>
+// DRIFT: the same gather for DriftShellData, whose lists hold a loss per
+// direction (code = source * 8 + 4 + direction, right after that direction's
+// gain) with the fractions four per source ([N][E][S][4]).
+template <typename Real, int C, int V, bool DRIFT>
 __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
     k_shell_diffuse(RunView r, const int *__restrict__ ent, int L, const Real *__restrict__ del,
                     Real *__restrict__ out, short *__restrict__ xout) {
+  constexpr int NCOEF = DRIFT ? 4 : 5;  // fractions per source
+  auto coef_of = [](int code) { return DRIFT ? (code & 3) : (code & 7); };
+  auto is_gain = [](int code) { return (code & 7) < 4; };
   const Real *__restrict__ f = static_cast<const Real *>(r.f);
   const int M = r.M, S = r.S, E = r.E;
   const int MV = M / V;      // V-cell groups per row
@@ -151,7 +218,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
   for (int sl = blockIdx.x; sl < nslices; sl += gridDim.x) {
     const int k = sl / E, e = sl - (sl / E) * E;
     const size_t row = (size_t)sl * M;                 // (k*E + e)*M within a stream
-    const Real *__restrict__ dsl = del + (size_t)sl * S * 5;
+    const Real *__restrict__ dsl = del + (size_t)sl * S * NCOEF;
     int s0 = s_first, m0 = m_first;
     for (int c = threadIdx.x; c < groups; c += 2 * blockDim.x) {
       int s[2], m[2];
@@ -184,8 +251,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
           int b = xt[u];
           for (int p = 0; k > 0 && p < L; ++p) {
             const int cd = __ldg(ent + s[u] * L + p);
-            if (cd < 0 || (cd & 7) >= 4) continue;
-            const float a = (float)__ldg(dsl + (cd >> 3) * 5 + (cd & 7));
+            if (cd < 0 || !is_gain(cd)) continue;
+            const float a = (float)__ldg(dsl + (cd >> 3) * NCOEF + coef_of(cd));
             if (!(a > 0.f)) continue;
             const int xi = r.fexp[((size_t)(cd >> 3) * r.N + k) * E + e];
             b = min(b, xi + 17 - ilogb_f(a));
@@ -210,7 +277,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
             for (int j = 0; j < V; j++) fi[u][q][j] = Real(0);
             if (code[u][q] >= 0) {
               const int i = code[u][q] >> 3;
-              a[u][q] = __ldg(dsl + i * 5 + (code[u][q] & 7));
+              a[u][q] = __ldg(dsl + i * NCOEF + coef_of(code[u][q]));
               ld_vec<V>(f + (size_t)i * per_stream + row + (size_t)m[u] * V, fi[u][q]);
               if constexpr (sizeof(Real) == 4)  // the source row taken to the new exponent
                 a[u][q] = ldexp_f(a[u][q], xn[u] - r.fexp[((size_t)i * r.N + k) * E + e]);
@@ -221,7 +288,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
 #pragma unroll
           for (int q = 0; q < C; q++)
             if (code[u][q] >= 0) {
-              const bool gain = (code[u][q] & 7) < 4;
+              const bool gain = is_gain(code[u][q]);
 #pragma unroll
               for (int j = 0; j < V; j++)
                 acc[u][j] = gain ? sd_fma(a[u][q], fi[u][q][j], acc[u][j])
@@ -245,8 +312,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2)
           for (int j = 0; j < V; j++) {
             v[j] = v[j] + acc[u][j];
             if (nonfinite(v[j]))
-              set_error(r, isnan(v[j]) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, 6, s[u], k, e,
-                        m[u] * V + j);
+              set_error(r, isnan(v[j]) ? EPREM_GPU_ERR_NAN : EPREM_GPU_ERR_INF, DRIFT ? 7 : 6,
+                        s[u], k, e, m[u] * V + j);
           }
         }
         st_vec<V>(out + gi, v);
@@ -267,29 +334,48 @@ int launch_shell_coef(const RunView &r, const int *news, double kperxkpar, void 
   return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
-template <typename Real>
+template <typename Real, bool DRIFT>
 static void shell_diffuse_as(const RunView &r, const int *ent, int L, const void *del,
                              void *out, short *xout, int blocks, cudaStream_t st) {
   const Real *d = (const Real *)del;
   Real *o = (Real *)out;
   const bool pairs = r.M % 2 == 0;
   if (L <= 5 && pairs)
-    k_shell_diffuse<Real, 5, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
+    k_shell_diffuse<Real, 5, 2, DRIFT><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else if (L <= 5)
-    k_shell_diffuse<Real, 5, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
+    k_shell_diffuse<Real, 5, 1, DRIFT><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else if (pairs)
-    k_shell_diffuse<Real, 8, 2><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
+    k_shell_diffuse<Real, 8, 2, DRIFT><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
   else
-    k_shell_diffuse<Real, 8, 1><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
+    k_shell_diffuse<Real, 8, 1, DRIFT><<<blocks, 256, 0, st>>>(r, ent, L, d, o, xout);
 }
 
 int launch_shell_diffuse(const RunView &r, const int *ent, int L, const void *del, void *out,
-                         short *xout, cudaStream_t st, uint64_t *launches) {
+                         short *xout, cudaStream_t st, uint64_t *launches, bool drift) {
   const int blocks = std::min(r.N * r.E, 152 * 8);
+  if (r.precision == EPREM_FP32) {
+    if (drift)
+      shell_diffuse_as<float, true>(r, ent, L, del, out, xout, blocks, st);
+    else
+      shell_diffuse_as<float, false>(r, ent, L, del, out, xout, blocks, st);
+  } else {
+    if (drift)
+      shell_diffuse_as<double, true>(r, ent, L, del, out, nullptr, blocks, st);
+    else
+      shell_diffuse_as<double, false>(r, ent, L, del, out, nullptr, blocks, st);
+  }
+  ++*launches;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
+int launch_drift_coef(const RunView &r, const int *news, void *del, cudaStream_t st,
+                      uint64_t *launches) {
+  const size_t SN = (size_t)r.S * r.N;
+  const int blocks = (int)std::min<size_t>((SN + 127) / 128, 152 * 8);
   if (r.precision == EPREM_FP32)
-    shell_diffuse_as<float>(r, ent, L, del, out, xout, blocks, st);
+    k_drift_coef<float><<<blocks, 128, 0, st>>>(r, news, (float *)del);
   else
-    shell_diffuse_as<double>(r, ent, L, del, out, nullptr, blocks, st);
+    k_drift_coef<double><<<blocks, 128, 0, st>>>(r, news, (double *)del);
   ++*launches;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

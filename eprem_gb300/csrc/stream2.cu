@@ -14,8 +14,8 @@
 //     half has its own loop, so the upwind direction is never a branch;
 //   * warp-edge lanes publish only the half their neighbour needs (lane 31's
 //     last node for mu >= 0, lane 0's first node for mu < 0).
-// A CTA of T threads holds NPT*T >= 1024 nodes for mu bins up to 48, so a
-// 1000-node stream fits one CTA.  Two kernels: k_stream2, the scalar shape
+// A CTA of T threads holds NPT*T list nodes (shapes per mu bin below; a
+// 1000-node stream fits one CTA of the default shapes).  Two kernels: k_stream2, the scalar shape
 // (any M and split), and k_stream2_pairs, the packed fp32x2 shapes, with f
 // held as float2 pairs (an odd half padded with a zero cell).
 #include <cooperative_groups.h>
@@ -27,17 +27,22 @@ namespace cg = cooperative_groups;
 
 namespace eprem {
 
-// Threads per CTA and list nodes per thread for each mu bin: NPT * T >= 1024
-// where registers allow (a 1000-node stream in one CTA), the f halves of all
-// NPT nodes plus ~45 scalars inside the register cap of T threads.
-template <int MMAX> struct Stream2Shape;
-template <> struct Stream2Shape<8> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<16> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<24> { static constexpr int T = 512, NPT = 2; };
-template <> struct Stream2Shape<32> { static constexpr int T = 256, NPT = 4; };
-template <> struct Stream2Shape<40> { static constexpr int T = 256, NPT = 4; };
-template <> struct Stream2Shape<48> { static constexpr int T = 256, NPT = 3; };
-template <> struct Stream2Shape<64> { static constexpr int T = 256, NPT = 2; };
+// CTA shapes (threads T, list nodes per thread NPT) per mu bin, the bin's
+// default first.  A thread holds NPT nodes x MMAX cells in registers: NPT * T
+// list nodes per CTA, clusters of CTAs for longer streams.  Fewer nodes per
+// thread leave registers for more warps per SM; more nodes per thread amortise
+// the shuffles and halo exchange over more cells.  plan_stream2 picks a shape
+// from N (or the one a variant names), the autotuner times them all.
+// Measured on a GB300 (96 streams x 50 E x 40 mu, FP32 FMA-peak fractions of
+// the compile-time-guard kernel): N = 1000 -- 256x4 0.42, 128x4 in clusters
+// of 2 0.40, 256x3 in clusters of 2 0.24, 384x3 and 512x2 (register spills)
+// 0.24; N = 1500 -- 128x4 in clusters of 3 0.39, 256x3 in clusters of 2
+// 0.37, 256x4 in clusters of 2 (27 % of the slots idle) 0.29.  Shapes that
+// spill are not kept; where two shapes waste as few slots, the earlier wins.
+#define EPREM_S2_SHAPES(X)                                                             \
+  X(8, 512, 2) X(16, 512, 2) X(24, 512, 2) X(24, 256, 4) X(24, 128, 4) X(32, 256, 4)  \
+  X(32, 128, 4) X(32, 256, 3) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3) X(48, 256, 3) \
+  X(48, 128, 3) X(64, 256, 2) X(64, 128, 2)
 
 // The common exponent of a (stream, energy) slab (FP32 row exponents): the
 // largest true value of its rows, and of the seeds the sub-step can write,
@@ -79,16 +84,14 @@ __device__ __forceinline__ Pow2Pair pow2_pair(int k) {
 }
 __device__ __forceinline__ float scale2(float x, Pow2Pair p) { return (x * p.a) * p.b; }
 
-template <int MMAX>
+template <int MMAX, int T>
 constexpr size_t stream2_smem_bytes() {
-  return sizeof(float) * 2 * 2 * (Stream2Shape<MMAX>::T / 32 + 1) * (MMAX / 2);
+  return sizeof(float) * 2 * 2 * (T / 32 + 1) * (MMAX / 2);
 }
 
 // The scalar shape: any M up to MMAX and any split m0 (odd halves included).
-template <int MMAX>
-__global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView r, int m0) {
-  constexpr int T = Stream2Shape<MMAX>::T;
-  constexpr int NPT = Stream2Shape<MMAX>::NPT;
+template <int MMAX, int T, int NPT>
+__global__ void __launch_bounds__(T, 1) k_stream2(RunView r, int m0) {
   constexpr int W = T / 32;
   constexpr int H = MMAX / 2;  // register slots per direction (mu < 0, mu >= 0)
   constexpr unsigned FULL = 0xffffffffu;
@@ -348,10 +351,11 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2(RunView 
 // held at zero: its upwind value stays 0 (0 + c (0 - 0), the neighbours'
 // padding is zero too), it adds nothing to the isotropisation sum, and it is
 // zeroed again after the seed boundary and the relaxation set it.
-template <int MMAX, bool FILLED>
-__global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(RunView r, int m0) {
-  constexpr int T = Stream2Shape<MMAX>::T;
-  constexpr int NPT = Stream2Shape<MMAX>::NPT;
+// One (stream s, energy e) slab of run r, on a CTA (or cluster) of T
+// threads: the body of k_stream2_pairs and of k_stream2_pairs_multi.
+template <int MMAX, int T, int NPT, bool FILLED>
+__device__ __forceinline__ void stream2_pairs_slab(const RunView &r, const int s, const int e,
+                                                   int m0) {
   constexpr int W = T / 32;
   constexpr int H = MMAX / 2;  // cells per direction
   constexpr int P = H / 2;     // pairs per direction
@@ -364,8 +368,6 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int crank = (int)cluster.block_rank();
-  const int s = blockIdx.y;
-  const int e = r.E - 1 - (int)blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int N = r.N;
   const int M = FILLED ? MMAX : r.M;
@@ -684,6 +686,25 @@ __global__ void __launch_bounds__((Stream2Shape<MMAX>::T), 1) k_stream2_pairs(Ru
   if (C > 1) cluster.sync();
 }
 
+template <int MMAX, int T, int NPT, bool FILLED>
+__global__ void __launch_bounds__(T, 1) k_stream2_pairs(RunView r, int m0) {
+  stream2_pairs_slab<MMAX, T, NPT, FILLED>(r, blockIdx.y, r.E - 1 - (int)blockIdx.z, m0);
+}
+
+// The same kernel over the slabs of several runs in one launch (batched
+// ensembles): cluster i of the launch takes slab items[i] = (run, stream,
+// energy), the items in decreasing order of estimated work, so the slabs of
+// small runs fill the tail of the large ones.  Every slab is computed as the
+// one-run launch computes it.
+template <int MMAX, int T, int NPT, bool FILLED>
+__global__ void __launch_bounds__(T, 1)
+    k_stream2_pairs_multi(const __grid_constant__ MultiRunViews mv, const int4 *items) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int4 it = items[blockIdx.x / cluster.num_blocks()];
+  // the run's view stays in the parameter bank (indexed constant loads)
+  stream2_pairs_slab<MMAX, T, NPT, FILLED>(mv.v[it.x], it.y, it.z, mv.m0[it.x]);
+}
+
 // Per (stream, energy, list node): mult = ds_i min(tau / dtProp, 1), the
 // relaxation factor exp(-dtProp / tau) and 1 - it, and the seed times
 // 2^seed_k (the energy's own power of two, so that seeds far below the float
@@ -765,41 +786,70 @@ int launch_stream2_coef(const RunView &r, cudaStream_t st, uint64_t *launches) {
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, StreamPlan *plan) {
+namespace {
+struct S2Shape {
+  int mmax, T, npt;
+};
+constexpr S2Shape kS2Shapes[] = {
+#define EPREM_S2_ROW(MM, TT, NN) {MM, TT, NN},
+    EPREM_S2_SHAPES(EPREM_S2_ROW)
+#undef EPREM_S2_ROW
+};
+}  // namespace
+
+// shape: 0 automatic, k >= 1 the k-th shape of the mu bin.  Automatic: the
+// bin's default when one CTA holds the stream, else the shape whose cluster
+// wastes the fewest list-node slots (ties to the earlier shape).
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
-  int T, npt;
-  switch (mmax) {
-    case 8: T = Stream2Shape<8>::T; npt = Stream2Shape<8>::NPT; break;
-    case 16: T = Stream2Shape<16>::T; npt = Stream2Shape<16>::NPT; break;
-    case 24: T = Stream2Shape<24>::T; npt = Stream2Shape<24>::NPT; break;
-    case 32: T = Stream2Shape<32>::T; npt = Stream2Shape<32>::NPT; break;
-    case 40: T = Stream2Shape<40>::T; npt = Stream2Shape<40>::NPT; break;
-    case 48: T = Stream2Shape<48>::T; npt = Stream2Shape<48>::NPT; break;
-    default: T = Stream2Shape<64>::T; npt = Stream2Shape<64>::NPT; break;
-  }
-  plan->mmax = mmax;
-  plan->threads = T;
-  plan->reg_coef = 2;  // marks the several-nodes-per-thread kernel
-  plan->packed = packed ? 1 : 0;
-  plan->filled = 0;
   // packed: odd halves take one padding cell (mmax/2 is even, so it fits)
   if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
+  const S2Shape *pick = nullptr;
+  int k = 0;
+  double best = 0.0;
+  for (const S2Shape &sh : kS2Shapes) {
+    if (sh.mmax != mmax) continue;
+    ++k;
+    const int per = sh.T * sh.npt, cl = (N + per - 1) / per;
+    if (cl > 8) continue;
+    if (shape) {
+      if (k == shape) pick = &sh;
+      continue;
+    }
+    if (k == 1 && cl == 1) { pick = &sh; break; }
+    const double use = (double)N / ((double)cl * per);
+    if (!pick || use > best + 1e-9) { pick = &sh; best = use; }
+  }
+  if (!pick) return EPREM_GPU_ERR_ARG;
+  plan->mmax = mmax;
+  plan->threads = pick->T;
+  plan->npt = pick->npt;
+  plan->reg_coef = 2;  // marks the several-nodes-per-thread kernels
+  plan->packed = packed ? 1 : 0;
   plan->filled = filled ? 1 : 0;
-  plan->cluster = (N + npt * T - 1) / (npt * T);
-  return plan->cluster > 8 ? EPREM_GPU_ERR_ARG : 0;
+  plan->cluster = (N + pick->T * pick->npt - 1) / (pick->T * pick->npt);
+  return 0;
 }
 
-template <int MMAX>
+int stream2_shape_count(int M) {
+  int mmax = 0;
+  for (int b : {8, 16, 24, 32, 40, 48, 64})
+    if (M <= b) { mmax = b; break; }
+  int k = 0;
+  for (const S2Shape &sh : kS2Shapes) k += sh.mmax == mmax;
+  return k;
+}
+
+template <int MMAX, int T, int NPT>
 static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int m0,
                                     cudaStream_t st) {
-  constexpr int T = Stream2Shape<MMAX>::T;
-  constexpr size_t dyn = stream2_smem_bytes<MMAX>();
-  void (*kern)(RunView, int) = !pl.packed  ? k_stream2<MMAX>
-                               : pl.filled ? k_stream2_pairs<MMAX, true>
-                                           : k_stream2_pairs<MMAX, false>;
+  constexpr size_t dyn = stream2_smem_bytes<MMAX, T>();
+  void (*kern)(RunView, int) = !pl.packed  ? k_stream2<MMAX, T, NPT>
+                               : pl.filled ? k_stream2_pairs<MMAX, T, NPT, true>
+                                           : k_stream2_pairs<MMAX, T, NPT, false>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(pl.cluster, r.S, r.E);
   cfg.blockDim = dim3(T, 1, 1);
@@ -815,18 +865,51 @@ static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int 
   return cudaLaunchKernelEx(&cfg, kern, r, m0);
 }
 
+template <int MMAX, int T, int NPT>
+static cudaError_t launch_stream2_multi_t(const StreamPlan &pl, const MultiRunViews &mv,
+                                          const int4 *items, int n_items, cudaStream_t st) {
+  constexpr size_t dyn = stream2_smem_bytes<MMAX, T>();
+  void (*kern)(const MultiRunViews, const int4 *) =
+      pl.filled ? k_stream2_pairs_multi<MMAX, T, NPT, true>
+                : k_stream2_pairs_multi<MMAX, T, NPT, false>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(pl.cluster * n_items, 1, 1);
+  cfg.blockDim = dim3(T, 1, 1);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = pl.cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, mv, items);
+}
+
+int launch_stream2_multi(const StreamPlan &pl, const MultiRunViews &mv, const int4 *items,
+                         int n_items, cudaStream_t st, uint64_t *launches) {
+  if (!pl.packed || n_items <= 0) return EPREM_GPU_ERR_ARG;
+  cudaError_t err = cudaErrorInvalidValue;
+#define EPREM_S2_MCASE(MM, TT, NN)                                          \
+  if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)                    \
+    err = launch_stream2_multi_t<MM, TT, NN>(pl, mv, items, n_items, st); \
+  else
+  EPREM_S2_SHAPES(EPREM_S2_MCASE) {}
+#undef EPREM_S2_MCASE
+  *launches += 1;
+  return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
 int launch_stream2(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st,
                    uint64_t *launches) {
-  cudaError_t err;
-  switch (pl.mmax) {
-    case 8: err = launch_stream2_t<8>(r, pl, m0, st); break;
-    case 16: err = launch_stream2_t<16>(r, pl, m0, st); break;
-    case 24: err = launch_stream2_t<24>(r, pl, m0, st); break;
-    case 32: err = launch_stream2_t<32>(r, pl, m0, st); break;
-    case 40: err = launch_stream2_t<40>(r, pl, m0, st); break;
-    case 48: err = launch_stream2_t<48>(r, pl, m0, st); break;
-    default: err = launch_stream2_t<64>(r, pl, m0, st); break;
-  }
+  cudaError_t err = cudaErrorInvalidValue;
+#define EPREM_S2_CASE(MM, TT, NN)                                   \
+  if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)            \
+    err = launch_stream2_t<MM, TT, NN>(r, pl, m0, st);             \
+  else
+  EPREM_S2_SHAPES(EPREM_S2_CASE) {}
+#undef EPREM_S2_CASE
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

@@ -450,6 +450,46 @@ int launch_surr_apply(const RunView &r, size_t row0, size_t nrows, const float *
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
+// The acceptance check's statistic and the true error of the network's output on
+// collected rows, whose plain step (the target) is known: for row i the
+// residual of the network's projected output (as k_surr_apply forms it) and
+// its distance from the plain step, max over mu of |f_net - f_plain|
+// relative to the plain row's mean.
+__global__ void k_surr_calib(const float *xs, const float *ts, const float *Y, int ldy,
+                             size_t n, const float *mu32, float *res, float *err) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *x = xs + i * kSurIn;
+  const float *t = ts + i * kSurM;
+  const float *y = Y + i * ldy;
+  float fin[kSurM], fout[kSurM];
+  double sin_ = 0.0, sout = 0.0, splain = 0.0;
+#pragma unroll
+  for (int m = 0; m < kSurM; ++m) {
+    fin[m] = expf(x[m]);
+    fout[m] = expf(x[m] + y[m]);
+    sin_ += (double)fin[m];
+    sout += (double)fout[m];
+    splain += (double)expf(x[m] + t[m]);
+  }
+  const float scale = (float)(sin_ / sout);
+  float dmax = 0.f;
+#pragma unroll
+  for (int m = 0; m < kSurM; ++m) {
+    fout[m] *= scale;
+    dmax = fmaxf(dmax, fabsf(fout[m] - expf(x[m] + t[m])));
+  }
+  const float e = 1.f - x[42];
+  res[i] = cn_residual(fin, fout, sinhf(x[40]), sinhf(x[41]), -logf(e), mu32);
+  err[i] = (float)(dmax / (splain / kSurM));
+}
+
+int launch_surr_calib(const float *xs, const float *ts, const float *Y, int ldy, size_t n,
+                      const float *mu32, float *res, float *err, cudaStream_t st) {
+  k_surr_calib<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xs, ts, Y, ldy, n, mu32, res, err);
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
 int launch_surr_residual(const float *xs, const float *ts, size_t n, const float *mu32,
                          float *res, cudaStream_t st) {
   k_surr_residual<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xs, ts, n, mu32, res);

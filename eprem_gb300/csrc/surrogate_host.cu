@@ -418,6 +418,62 @@ extern "C" int eprem_gpu_surrogate_calibrate(eprem_gpu_surrogate *s, double quan
   return EPREM_GPU_OK;
 }
 
+// Tolerance of the residual check from the rows' true error: the network
+// runs on up to `rows` collected rows (whose plain step is known), and the
+// tolerance is the largest residual below which every row is within
+// `target` of its plain step (max over mu, relative to the row's mean).
+// *kept: the fraction of those rows the check then keeps; *within: the
+// fraction within target at all (what an exact check would keep).
+extern "C" int eprem_gpu_surrogate_calibrate_error(eprem_gpu_surrogate *s, double target,
+                                                   int64_t rows, double *tol_out,
+                                                   double *kept, double *within) {
+  if (!s || !s->n) return fail(EPREM_GPU_ERR_STATE, "calibrate: no samples");
+  const size_t n = std::min(s->n, rows > 0 ? (size_t)rows : s->n);
+  float *res = nullptr, *err = nullptr;
+  CK(cudaMalloc(&res, n * sizeof(float)));
+  cudaError_t e = cudaMalloc(&err, n * sizeof(float));
+  for (size_t r0 = 0; r0 < n && e == cudaSuccess; r0 += s->R) {
+    const size_t nr = std::min(s->R, n - r0);
+    const int nn = (int)nr;
+    if (launch_to_bf16(s->xs + r0 * kSIn, s->X, nr * kSIn, s->st) ||
+        launch_gemm_bf16(s->X, kSIn, s->w1t, kSIn, s->p + kOffB1, s->Z, kSHid, nn, kSHid, kSIn,
+                         s->d_err, s->st) ||
+        launch_gelu_bf16(s->Z, s->Ha, nr * kSHid, s->st) ||
+        launch_gemm_bf16(s->Ha, kSHid, s->w2t, kSHid, s->p + kOffB2, s->Z, kSHid, nn, kSHid,
+                         kSHid, s->d_err, s->st) ||
+        launch_gelu_bf16(s->Z, s->Hb, nr * kSHid, s->st) ||
+        launch_gemm_bf16(s->Hb, kSHid, s->w3t, kSHid, s->p + kOffB3, s->Y, kSOut, nn, kSOut,
+                         kSHid, s->d_err, s->st) ||
+        launch_surr_calib(s->xs + r0 * kSIn, s->ts + r0 * kSM, s->Y, kSOut, nr, s->mu32,
+                          res + r0, err + r0, s->st))
+      e = cudaGetLastError();
+  }
+  std::vector<float> hr(n), he(n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hr.data(), res, n * sizeof(float), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(he.data(), err, n * sizeof(float), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  cudaFree(res);
+  cudaFree(err);
+  if (e != cudaSuccess) return cuda_fail(e, "calibrate_error");
+  const int rc = surr_read_err(s);
+  if (rc) return rc;
+  // the smallest residual of a row beyond target bounds the tolerance
+  float bound = INFINITY;
+  size_t ok = 0;
+  for (size_t i = 0; i < n; i++) {
+    const bool good = he[i] <= (float)target;  // false for NaN
+    ok += good;
+    if (!good) bound = std::min(bound, std::isnan(hr[i]) ? -INFINITY : hr[i]);
+  }
+  size_t keep = 0;
+  for (size_t i = 0; i < n; i++) keep += hr[i] < bound;  // false for NaN
+  s->tol = std::isinf(bound) && bound > 0 ? INFINITY : std::nextafter(bound, -INFINITY);
+  if (tol_out) *tol_out = s->tol;
+  if (kept) *kept = (double)keep / (double)n;
+  if (within) *within = (double)ok / (double)n;
+  return EPREM_GPU_OK;
+}
+
 extern "C" int eprem_gpu_surrogate_set_tolerance(eprem_gpu_surrogate *s, double tol) {
   if (!s) return fail(EPREM_GPU_ERR_ARG, "null surrogate");
   s->tol = (float)tol;

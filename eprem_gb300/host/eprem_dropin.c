@@ -39,7 +39,7 @@
  * Scope: one MPI rank holds every stream (the GPU replaces the rank
  * decomposition), one species, analytic or MAS coronal background (the
  * heliospheric MAS coupling is refused with the reference's panic), shell
- * diffusion; drift is refused with the reference's panic text.
+ * diffusion and drift (drift with the analytic background only).
  */
 #include <float.h>
 #include <stdio.h>
@@ -135,7 +135,7 @@ static void dropin_init(void) {
   if (N_PROCS != 1) panic("GPU path: run with one MPI rank (every stream lives on the GPU)");
   if (config.masHelCouple > 0)
     panic("GPU path: heliospheric MAS coupling is not supported by this build");
-  if (config.useDrift > 0) panic("GPU path: drift is not supported by this build");
+
   eprem_dims_t d;
   d.num_streams = NUM_STREAMS;
   d.num_nodes = TOTAL_NUM_SHELLS;
@@ -192,6 +192,15 @@ static void dropin_init(void) {
   g.dlnp = dlnp;
   g.dmu = dmu;
   dropin_check(eprem_gpu_create(&d, &p, &g, &dropin_run), "eprem_gpu_create");
+  /* useDrift: curl(B)/B^2 from every updateMhd from here on; the drift
+   * itself once the grid's links exist (dropin_perp_setup) */
+  if (config.useDrift > 0) {
+    eprem_drift_params_t dp;
+    dp.lnpmin = lnpmin;
+    dp.charge = config.charge[0];
+    dp.mass = config.mass[0];
+    dropin_check(eprem_gpu_set_drift(dropin_run, NULL, &dp), "drift");
+  }
   dropin_t_del = config.tDel;
   dropin_sn = (size_t)d.num_streams * d.num_nodes;
   dropin_nodes = (double *)eprem_gpu_host_alloc(sizeof(double) * EPREM_NODE_NFIELDS * dropin_sn);
@@ -266,16 +275,16 @@ static void dropin_f_to_host(void) {
                "download f");
 }
 
-/* useShellDiffusion: hand the run the NEWS links gridStructInit gave every
- * shell (initNEWS + initCopyAll, src/cubeShellInit.c:46-94) as stream
- * indices.  The driver's first updateMhd comes before gridStructInit
+/* useShellDiffusion / useDrift: hand the run the NEWS links gridStructInit
+ * gave every shell (initNEWS + initCopyAll, src/cubeShellInit.c:46-94) as
+ * stream indices.  The driver's first updateMhd comes before gridStructInit
  * (src/eprem.c:470-480), so this waits for the first particle update.  The
  * run forms ShellData's lengths itself at each update; the driver's own
  * ShellData call (src/eprem.c:647-650) only fills host fields nothing here
  * reads. */
 static int dropin_shell_ready = 0;
 static void dropin_shell_setup(void) {
-  if (dropin_shell_ready || config.useShellDiffusion <= 0) return;
+  if (dropin_shell_ready || (config.useShellDiffusion <= 0 && config.useDrift <= 0)) return;
   int32_t *news = (int32_t *)malloc(sizeof(int32_t) * 4 * (size_t)NUM_STREAMS);
   if (!news) panic("GPU path: allocation failed");
   for (Index_t face = 0; face < NUM_FACES; face++)
@@ -287,8 +296,16 @@ static void dropin_shell_setup(void) {
         for (int k = 0; k < 4; k++)
           news[s * 4 + k] = (int32_t)((nb[k]->face * FACE_ROWS + nb[k]->row) * FACE_COLS + nb[k]->col);
       }
-  dropin_check(eprem_gpu_set_shell_diffusion(dropin_run, news, config.kperxkpar),
-               "shell diffusion");
+  if (config.useShellDiffusion > 0)
+    dropin_check(eprem_gpu_set_shell_diffusion(dropin_run, news, config.kperxkpar),
+                 "shell diffusion");
+  if (config.useDrift > 0) {
+    eprem_drift_params_t dp;
+    dp.lnpmin = lnpmin;
+    dp.charge = config.charge[0];
+    dp.mass = config.mass[0];
+    dropin_check(eprem_gpu_set_drift(dropin_run, news, &dp), "drift");
+  }
   free(news);
   dropin_shell_ready = 1;
 }
@@ -465,6 +482,8 @@ void updateMhd(void) {
   dropin_init();
   dropin_sync_step();
   const uint64_t all = EPREM_NODE_MASK_ALL;
+  if (mhdGridStatus == MHD_MAS && config.useDrift > 0)
+    panic("GPU path: drift with the MAS background is not supported by this build");
   if (mhdGridStatus == MHD_MAS) {
     dropin_mas_sync();
     dropin_check(eprem_gpu_mas_use(dropin_run, 1), "updateMhd");

@@ -37,6 +37,11 @@ EXPORTS = [
     ("eprem_gpu_update_mhd", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_set_time_step", C.c_int, [C.c_void_p, C.c_double]),
+    ("eprem_gpu_surrogate_calibrate_error", C.c_int,
+     [C.c_void_p, C.c_double, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+      C.POINTER(C.c_double)]),
+    ("eprem_gpu_set_drift", C.c_int,
+     [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(abi.DriftParams)]),
     ("eprem_gpu_set_shell_diffusion", C.c_int,
      [C.c_void_p, C.POINTER(C.c_int32), C.c_double]),
     ("eprem_gpu_update_energetic_particles_host", C.c_int,
@@ -58,6 +63,7 @@ EXPORTS = [
     ("eprem_gpu_alu_peak", C.c_int, [C.c_int, DP]),
     ("eprem_gpu_mas_init", C.c_int, [C.c_void_p, C.POINTER(abi.MasParams)]),
     ("eprem_gpu_mas_load_slice", C.c_int, [C.c_void_p, C.c_int, C.POINTER(abi.MasSlice)]),
+    ("eprem_gpu_mas_load_slice_async", C.c_int, [C.c_void_p, C.c_int, C.POINTER(abi.MasSlice)]),
     ("eprem_gpu_mas_select", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]),
     ("eprem_gpu_mas_move_nodes", C.c_int, [C.c_void_p, C.c_double]),
     ("eprem_gpu_mas_use", C.c_int, [C.c_void_p, C.c_int]),
@@ -270,6 +276,23 @@ class EpremRun:
         self._check(self.lib.eprem_gpu_set_shell_diffusion(
             self.handle, nw.ctypes.data_as(C.POINTER(C.c_int32)), kperxkpar))
 
+    def set_drift(self, news, drift_params):
+        """useDrift: curl(B)/B^2 formed by every analytic update_mhd and
+        DriftShellData after every sub-step.  drift_params: abi.DriftParams
+        (None: off); news: num_streams x 4 NEWS links (None keeps earlier
+        ones)."""
+        if drift_params is None:
+            self._check(self.lib.eprem_gpu_set_drift(self.handle, None, None))
+            return
+        ptr = None
+        if news is not None:
+            nw = np.ascontiguousarray(news, dtype=np.int32)
+            if nw.shape != (self.dims.num_streams, 4):
+                raise ValueError("news must be num_streams x 4")
+            self._drift_news = nw
+            ptr = nw.ctypes.data_as(C.POINTER(C.c_int32))
+        self._check(self.lib.eprem_gpu_set_drift(self.handle, ptr, C.byref(drift_params)))
+
     # -- MAS background ------------------------------------------------------
     def mas_init(self, mas_params: abi.MasParams):
         """Switch updateMhd to the MAS background (masGetNode)."""
@@ -277,6 +300,12 @@ class EpremRun:
 
     def mas_load_slice(self, slot: int, slice_struct: abi.MasSlice):
         self._check(self.lib.eprem_gpu_mas_load_slice(self.handle, slot, C.byref(slice_struct)))
+
+    def mas_load_slice_async(self, slot: int, slice_struct: abi.MasSlice):
+        """Queue the slice's copy on the run's copy stream (the arrays behind
+        slice_struct must stay alive until the slot is next selected)."""
+        self._check(self.lib.eprem_gpu_mas_load_slice_async(self.handle, slot,
+                                                            C.byref(slice_struct)))
 
     def mas_select(self, slot0: int, slot1: int, s_cor: float, phi_offset: float = 0.0):
         self._check(self.lib.eprem_gpu_mas_select(self.handle, slot0, slot1, s_cor, phi_offset))
@@ -471,6 +500,15 @@ class Surrogate:
         self._check(self.lib.eprem_gpu_surrogate_calibrate(self.handle, float(quantile),
                                                            float(margin), C.byref(tol)))
         return tol.value
+
+    def calibrate_error(self, target: float, rows: int = 0):
+        """Tolerance from the rows' true error against their plain step:
+        (tolerance, fraction kept by the check, fraction within target)."""
+        tol, kept, within = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.eprem_gpu_surrogate_calibrate_error(
+            self.handle, float(target), int(rows), C.byref(tol), C.byref(kept),
+            C.byref(within)))
+        return tol.value, kept.value, within.value
 
     def set_tolerance(self, tol: float):
         self._check(self.lib.eprem_gpu_surrogate_set_tolerance(self.handle, float(tol)))

@@ -126,15 +126,17 @@ typedef struct {
                                        1,000,000).  The reference has no cap. */
   int32_t stream_variant;           /* streaming-kernel shape in the FP32 form
                                        (tuning; results agree to rounding):
-                                       0 automatic (the first of 5, 4, 3
-                                       that fits these sizes);
-                                       1 one node per thread, coefficients in
-                                       registers; 2 one node per thread,
-                                       coefficients in shared memory;
+                                       kind + 8 * shape.  kind 0 automatic
+                                       (the first of 5, 4, 3 that fits);
                                        3 several nodes per thread; 4 as 3
                                        with packed fp32x2 arithmetic; 5 as 4
                                        with compile-time cell guards (M = 8,
-                                       16, ..., 64 and m0 = M/2)            */
+                                       16, ..., 64 and m0 = M/2).  shape 0
+                                       automatic, k >= 1 the k-th CTA shape
+                                       (threads, nodes per thread, cluster)
+                                       of the run's mu bin.  A shape whose
+                                       stream needs a cluster of more than
+                                       8 CTAs is refused.                  */
 } eprem_params_t;
 
 /* ---- 1-D grids built by initEnergeticParticlesGrids
@@ -332,6 +334,35 @@ int eprem_gpu_set_time_step(eprem_gpu_run *run, double t_del);
  * EPREM_GPU_ERR_ARG for a neighbour out of range or kperxkpar < 1e-33. */
 int eprem_gpu_set_shell_diffusion(eprem_gpu_run *run, const int32_t *news, double kperxkpar);
 
+/* Drift: config.useDrift = 1 (src/configuration.c:126).  The drift velocity
+ * of driftVelocity (src/energeticParticles.c:210-246) needs the particles'
+ * momentum grid and charge-to-mass ratio, which eprem_params_t does not
+ * carry. */
+typedef struct {
+  double lnpmin;  /* lnpmin (src/energeticParticlesTypes.c): p(E) = exp(lnpmin + E dlnp) */
+  double charge;  /* config.charge[0] (units of the proton charge)                     */
+  double mass;    /* config.mass[0]   (units of the proton mass)                       */
+} eprem_drift_params_t;
+
+/* Switch drift on (dp non-NULL) or off (dp NULL).  While on, every
+ * eprem_gpu_update_mhd of the analytic background also forms curl(B)/B^2 at
+ * each node (mhdCurlBoverB2 / curlBoverB2, src/flow.c:127-128, :411-616:
+ * centred differences of the Parker field, ideal shock included), and once
+ * the NEWS links are given (news: as for eprem_gpu_set_shell_diffusion; NULL
+ * keeps the links of an earlier call, so the curl can be switched on before
+ * the grid's links exist) every eprem_gpu_update_energetic_particles runs
+ * DriftShellData (src/energeticParticles.c:561-801) after each sub-step,
+ * after the shell diffusion: each node k >= 1 hands
+ * min(v_d . e_n rScale / dl * dt / dl, 0.025) of its f to each NEWS
+ * neighbour its drift velocity points to (dl: the neighbour distance of
+ * ShellData), summed in the reference's order.  The MAS background is
+ * refused (EPREM_GPU_ERR_UNSUPPORTED): inside the MAS domain the reference
+ * leaves curl(B)/B^2 to masGetNode, which does not form it
+ * (src/masInterp.c:941-942).  Drift couples the streams, as the shell
+ * diffusion does. */
+int eprem_gpu_set_drift(eprem_gpu_run *run, const int32_t *news,
+                        const eprem_drift_params_t *dp);
+
 /* Omnidirectional flux J = 2 E <f>_mu per (stream, node, energy), the
  * quantity computeFlux writes (src/unifiedOutput.c:153-180), without its
  * output unit scale.  out: S*N*E doubles, host memory.  Synchronizes. */
@@ -406,8 +437,22 @@ typedef struct {
  * eprem_gpu_mas_move_nodes becomes available (masMoveNodes). */
 int eprem_gpu_mas_init(eprem_gpu_run *run, const eprem_mas_params_t *mp);
 /* Copy one time slice (all seven fields with their meshes) into device slot
- * `slot`; the replacement of masReadData's H2D side (src/readMAS.c:705-830). */
+ * `slot`; the replacement of masReadData's H2D side (src/readMAS.c:705-830).
+ * Returns once the copies are done.  A slot keeps its device arrays from
+ * load to load while the slice's dimensions stay the same, so only a slot's
+ * first load (or a change of grid) allocates. */
 int eprem_gpu_mas_load_slice(eprem_gpu_run *run, int slot, const eprem_mas_slice_t *slice);
+/* The same, queued: masGetInterpData's next slice (src/readMAS.c:645-998)
+ * copied on the run's copy stream while the run's stream computes with the
+ * selected pair -- the slot must not be one of them (EPREM_GPU_ERR_STATE).
+ * The copies start after the last launch that read the slot and the run's
+ * stream waits for them when eprem_gpu_mas_select next names the slot.  The
+ * slice's host arrays must stay valid and unchanged until then, and should
+ * be page-locked (eprem_gpu_host_alloc / eprem_gpu_host_register): from
+ * pageable memory the driver stages the copy and the call may block until it
+ * has. */
+int eprem_gpu_mas_load_slice_async(eprem_gpu_run *run, int slot,
+                                   const eprem_mas_slice_t *slice);
 /* Interpolate between slots slot0 and slot1 with the time factor s_cor
  * (masGetInterpData, src/readMAS.c:645-998) and the phi offset phiOffset. */
 int eprem_gpu_mas_select(eprem_gpu_run *run, int slot0, int slot1, double s_cor,
@@ -448,9 +493,10 @@ int eprem_gpu_alu_peak(int precision, double *tflops);
  * the device without a host copy of f.  Synchronizes. */
 int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double perturbation);
 
-/* Time the streaming-kernel shapes that fit this run (FP32 form: variants 4,
- * 3, 2, 1 of eprem_params_t.stream_variant) on a scratch copy of its first 96
- * streams and keep the fastest; *chosen_variant receives it.  The run's f
+/* Time the streaming-kernel kinds and CTA shapes that fit this run (FP32
+ * form: every kind 3, 4, 5 with every shape of its mu bin, encoded as
+ * eprem_params_t.stream_variant) on a scratch copy of its first 96 streams
+ * and keep the fastest; *chosen_variant receives it.  The run's f
  * and statistics are not touched.  The FP64 form has one shape.  Allocates
  * and frees scratch; synchronizes. */
 int eprem_gpu_autotune(eprem_gpu_run *run, int *chosen_variant);
@@ -462,7 +508,7 @@ int eprem_gpu_set_stream_variant(eprem_gpu_run *run, int variant);
  * eprem_gpu_ensemble_step captures one driver step of every run --
  * moveNodes(tDel), updateMhd(t + tDel), updateEnergeticParticles, t += tDel,
  * the order of src/eprem.c:620-671 -- into one CUDA graph (the runs in
- * sequence, or the chains of eprem_gpu_ensemble_set_chains); each later step
+ * schedule of eprem_gpu_ensemble_set_chains); each later step
  * is one launch of that graph.  Each run's time t lives
  * on the device (set_time / get_time, zero at creation).  Until
  * eprem_gpu_ensemble_synchronize returns, the member runs must not be used
@@ -478,13 +524,17 @@ int eprem_gpu_ensemble_get_time(eprem_gpu_ensemble *ens, double *t_global);
  * its choice to the others of the class; chosen_variants (may be NULL)
  * receives one variant per run.  The next step captures a new graph. */
 int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *ens, int *chosen_variants);
-/* How the graph orders the runs: `chains` serial chains that run side by
- * side, the runs spread over them largest first onto the chain with the
- * fewest cells (1, the default: every run after the previous one; 0: one
- * branch per run, all side by side).  Runs that each fill the GPU step
- * fastest in one chain (8 runs of 0.1-2.6 G cells: one chain 9.30e9
- * cell-updates/s, one branch per run 9.06e9); side-by-side branches are for
- * runs too small to fill it.  The next step captures a new graph. */
+/* How the graph orders the runs.  chains < 0 (the default): lock-step --
+ * every run's moveNodes, updateMhd and per-call set-up, then EP sub-step by
+ * EP sub-step the streaming of all runs, one launch per group of runs that
+ * share a packed streaming kernel (mu bin, CTA shape, cluster size), its
+ * (run, stream, energy) slabs ordered longest first by their estimated
+ * sub-cycle work so small runs fill the tails of large ones, then each run's
+ * node phase (needs the same numEpSteps in every run; otherwise one chain).
+ * chains >= 1: that many serial chains side by side, each run's whole step
+ * in sequence, runs spread over the chains largest first; 0: one branch per
+ * run.  Results are the runs' own in every schedule, bit for bit.  The next
+ * step captures a new graph. */
 int eprem_gpu_ensemble_set_chains(eprem_gpu_ensemble *ens, int chains);
 int eprem_gpu_ensemble_step(eprem_gpu_ensemble *ens);
 int eprem_gpu_ensemble_synchronize(eprem_gpu_ensemble *ens);
@@ -565,6 +615,14 @@ int eprem_gpu_surrogate_evaluate(eprem_gpu_surrogate *s, const float *x, int row
 int eprem_gpu_surrogate_calibrate(eprem_gpu_surrogate *s, double quantile, double margin,
                                   double *tol);
 int eprem_gpu_surrogate_set_tolerance(eprem_gpu_surrogate *s, double tol);
+/* Tolerance from the true error instead: the network runs on up to `rows`
+ * collected rows (0: all), whose plain step is known; the tolerance becomes
+ * the largest residual below which every one of them is within `target` of
+ * its plain step (max over mu of |f_net - f_plain| over the row's mean).
+ * *kept: fraction of those rows the check then keeps; *within: fraction
+ * within target at all (what a check with the plain step itself would keep). */
+int eprem_gpu_surrogate_calibrate_error(eprem_gpu_surrogate *s, double target, int64_t rows,
+                                        double *tol, double *kept, double *within);
 /* Choose the node phase of a run (the surrogate for SURROGATE, else NULL). */
 int eprem_gpu_set_node_phase(eprem_gpu_run *run, int mode, eprem_gpu_surrogate *s);
 /* Rows the surrogate kept and rows recomputed by the plain kernel since the

@@ -140,3 +140,39 @@ def test_gpu_flux_output_run_matches_reference(tmp_path):
     ref = run_case(os.path.join(ROOT, "oracle", "_ref", "eprem_ref"), "wind", tmp_path, text)
     gpu = run_case(GPU_EXE, "wind", tmp_path, text)
     assert compare_flux_runs(gpu, ref, 1e-12) > 0.0
+
+
+def test_gpu_drift_run_matches_oracle_run(tmp_path):
+    """useDrift through the drop-in on the GPU: the testsuite's wind case
+    with useDrift=1, every observer array within 1e-12 of the same driver
+    over the CPU restatement (whose run is byte-identical to the
+    reference's own, test_drift_whole_run.py)."""
+    from test_drift_whole_run import drift_config
+    from test_flux_output_run import run_case
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref-dropin",
+                           f"REF={REF}"])
+    from eprem_gb300 import build
+    build.build()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "eprem_gb300", "host"), "link",
+                           f"REF={REF}"])
+    text = drift_config("wind", False)
+    orc = run_case(ORC_EXE, "wind", tmp_path, text, {"EPREM_ORACLE_THREADS": "8"})
+    gpu = run_case(GPU_EXE, "wind", tmp_path, text)
+    import glob
+    import digest as D
+    caps = sorted(glob.glob(os.path.join(orc, "obs*.nc.cap")))
+    assert caps
+    for cap in caps:
+        ref = D.read_capture(cap)
+        got = D.read_capture(os.path.join(gpu, os.path.basename(cap)))
+        for name, (a, sc, off) in ref.items():
+            b = got[name][0]
+            a64 = np.asarray(D.unpacked(a, sc, off), dtype=np.float64)
+            b64 = np.asarray(D.unpacked(b, sc, off), dtype=np.float64)
+            if name == "Dist":
+                nz = a64 != 0
+                err = float(np.max(np.abs(b64[nz] - a64[nz]) / np.abs(a64[nz]), initial=0.0))
+                assert err <= 1e-12, (os.path.basename(cap), err)
+            else:
+                scale = max(float(np.max(np.abs(a64), initial=0.0)), 1e-300)
+                assert float(np.max(np.abs(b64 - a64), initial=0.0)) / scale <= 1e-10, name

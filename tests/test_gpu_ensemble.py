@@ -28,11 +28,12 @@ def _start(w, orc, precision):
     return run
 
 
-@pytest.mark.parametrize("chains", [0, 1, 2])
+@pytest.mark.parametrize("chains", [-1, 0, 1, 2])
 @pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
 def test_ensemble_step_equals_individual_steps(oracle_lib, precision, chains):
-    """Every graph schedule (one branch per run, one serial chain, two
-    chains) replays the runs' own kernels: bit-equal to stepping them."""
+    """Every graph schedule (lock-step -- here, with unequal numEpSteps, one
+    chain --, one branch per run, one serial chain, two chains) replays the
+    runs' own kernels: bit-equal to stepping them."""
     ws = _members()
     td = ws[0].params.t_del
     t0 = [td, 2 * td, 3 * td]
@@ -59,6 +60,48 @@ def test_ensemble_step_equals_individual_steps(oracle_lib, precision, chains):
         np.testing.assert_array_equal(rb.download_nodes(), rs.download_nodes())
         assert rb.read_stats().as_dict() == rs.read_stats().as_dict()
         assert rb.kernel_launches - nb > 0
+    ens.close()
+    for r in single + batched:
+        r.close()
+
+
+def _lockstep_members():
+    """Runs with the same numEpSteps: two sharing the mu = 8 packed kernel,
+    two sharing the mu = 40 one (one with a cluster of CTAs per slab), one
+    with an ideal shock."""
+    return [W.custom(1, 1, 120, 10, 8, num_ep_steps=2),
+            W.custom(1, 2, 300, 6, 8, num_ep_steps=2),
+            W.custom(2, 2, 80, 8, 40, num_ep_steps=2, ideal_shock=1, ideal_shock_speed=1500e5,
+                     ideal_shock_init_time=0.0, ideal_shock_width=0.0),
+            W.custom(1, 1, 1100, 5, 40, num_ep_steps=2)]
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+def test_lockstep_ensemble_equals_individual_steps(oracle_lib, precision):
+    """The lock-step schedule (the default): sub-step by sub-step, the
+    streaming of runs that share a packed kernel in one launch over all
+    their slabs, longest first -- bit-equal to stepping each run alone."""
+    ws = _lockstep_members()
+    td = ws[0].params.t_del
+    single = [_start(w, oracle_lib, precision) for w in ws]
+    batched = [_start(w, oracle_lib, precision) for w in ws]
+    for run, w in zip(single, ws):
+        t = td
+        for k in range(3):
+            run.move_nodes(w.params.t_del)
+            run.update_mhd(t + w.params.t_del)
+            run.update_energetic_particles(t)
+            t += w.params.t_del
+        run.synchronize()
+    ens = Ensemble(batched)
+    ens.set_time([td] * len(ws))
+    for _ in range(3):
+        ens.step()
+    ens.synchronize()
+    for rs, rb in zip(single, batched):
+        np.testing.assert_array_equal(rb.download_f(), rs.download_f())
+        np.testing.assert_array_equal(rb.download_nodes(), rs.download_nodes())
+        assert rb.read_stats().as_dict() == rs.read_stats().as_dict()
     ens.close()
     for r in single + batched:
         r.close()
@@ -96,7 +139,7 @@ def test_autotune_keeps_a_correct_shape(oracle_lib):
     run.upload_f(f)
     run.upload_nodes(nodes)
     v = run.autotune()
-    assert v in (1, 2, 3, 4, 5)
+    assert v % 8 in (3, 4, 5) and 1 <= v // 8  # a kind and a CTA shape
     # the scratch copy leaves the state alone
     np.testing.assert_array_equal(run.download_f(), f.astype(np.float32).astype(np.float64))
     run.update_energetic_particles(0.0)
@@ -110,7 +153,7 @@ def test_ensemble_autotune_by_size_class(oracle_lib):
     runs = [_start(w, oracle_lib, abi.EPREM_FP32) for w in ws]
     ens = Ensemble(runs)
     chosen = ens.autotune()
-    assert len(chosen) == 3 and all(v in (1, 2, 3, 4, 5) for v in chosen)
+    assert len(chosen) == 3 and all(v % 8 in (3, 4, 5) and v // 8 >= 1 for v in chosen)
     ens.set_time(0.0)
     ens.step()
     ens.synchronize()

@@ -105,3 +105,28 @@ def test_unsupported_species_rejected_at_create():
     with pytest.raises(EpremGpuError) as ei:
         EpremRun(d, w.params, W.build_grids(w))
     assert ei.value.code == abi.EPREM_GPU_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", [abi.EPREM_FP64, abi.EPREM_FP32])
+def test_nan_node_rate_leaves_the_node_as_the_reference_does(oracle_lib, precision):
+    """A node whose DuPar is NaN has NaN face speeds everywhere: the
+    reference's CFL maximum passes over them (fabs(NaN) > max is false), so
+    its sub-cycle counts are zero and focusing and change leave the node as
+    it is -- no panic.  The GPU forms do the same."""
+    w = W.custom(1, 1, 30, 6, 6, num_ep_steps=2)
+    d, g, f, nodes = primed_state(w, oracle_lib)
+    nodes[abi.NODE["DUPAR"], 10] = np.nan
+    f_ref, n_ref = f.copy(), nodes.copy()
+    gs, keep = W.grids_struct(g)
+    rc, st, err = oracle_lib.update_energetic_particles(d, w.params, gs, f_ref, n_ref)
+    assert rc == 0, err
+    run = EpremRun(w.dims(precision), w.params, g)
+    run.upload_f(f)
+    run.upload_nodes(nodes)
+    run.update_energetic_particles(0.0)
+    run.read_stats()
+    out = run.download_f()
+    run.close()
+    assert np.all(np.isfinite(out))
+    tol = 1e-12 if precision == abi.EPREM_FP64 else 1e-3
+    assert np.max(np.abs(out - f_ref) / f_ref) <= tol

@@ -102,3 +102,40 @@ def test_mas_use_switches_back_to_the_analytic_wind(oracle_lib):
     oracle_lib.update_mhd(d, w.params, nodes, 0.0)
     _assert_nodes_close(run.download_nodes(), nodes, "analytic after mas_use(False)")
     run.close()
+
+
+def test_async_slice_loads_equal_synchronous_loads():
+    """Slices queued on the copy stream (eprem_gpu_mas_load_slice_async) give
+    the same background as synchronous loads, bit for bit, including a load
+    into the third slot while the first pair is selected and in use, and a
+    reload of a slot (its arrays kept, no reallocation); loading into a
+    selected slot is refused."""
+    w, grid, f0, f1 = _case(2, 2, 120)
+    f2 = grid.slice_fields(grid.times[2])
+    structs = [W.mas_slice_struct(grid, f) for f in (f0, f1, f2)]
+    runs = []
+    for mode in ("sync", "async"):
+        run = EpremRun(w.dims(), w.params, W.build_grids(w))
+        run.upload_nodes(W.initial_nodes(w))
+        run.mas_init(grid.params)
+        load = run.mas_load_slice if mode == "sync" else run.mas_load_slice_async
+        load(0, structs[0][0])
+        load(1, structs[1][0])
+        run.mas_select(0, 1, 0.4, 0.1)
+        if mode == "async":
+            with pytest.raises(Exception):
+                run.mas_load_slice_async(0, structs[0][0])
+        run.update_mhd(0.0)
+        run.mas_move_nodes(w.params.t_del)
+        load(2, structs[2][0])  # the next slice while the pair is in use
+        run.mas_select(1, 2, 0.2, 0.1)
+        run.update_mhd(w.params.t_del)
+        run.mas_move_nodes(w.params.t_del)
+        load(0, structs[0][0])  # a reload of a slot that was read before
+        run.mas_select(2, 0, 0.7, 0.1)
+        run.update_mhd(2 * w.params.t_del)
+        runs.append(run.download_nodes())
+        run.close()
+    a, b = runs
+    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    assert same.all()
