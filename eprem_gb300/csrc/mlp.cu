@@ -147,9 +147,13 @@ __global__ void __launch_bounds__(kGemmThreads)
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
           : "memory");
     }
-    if (!mbar_wait(mb, phase)) {
-      ok = false;
+    // block-uniform outcome: every thread leaves the loop together
+    ok = __syncthreads_and(mbar_wait(mb, phase) ? 1 : 0) != 0;
+    if (!ok) {
       if (tid == 0) atomicCAS(err, 0, 1);
+      // the MMAs already committed still write TMEM: wait for them once
+      // more (bounded) before the allocation is released below
+      mbar_wait(mb, phase);
     }
     phase ^= 1u;
     tc_fence_after();

@@ -96,8 +96,10 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
       }
       amin = warp_min(amin);
       amax = warp_max(amax);
+      // NaN a (a NaN DuPar or dlnB/ds) takes no part in the maximum, as the
+      // reference's fabs(v) > max passes over NaN: no finite a, no sub-cycle
       double vmax = 0.0;
-      for (int pass = 0; pass < 2; pass++) {
+      for (int pass = 0; pass < 2 && amin <= amax; pass++) {
         const double a = pass ? amax : amin;
         for (int m = 1 + lane; m < M; m += 32) {
           const double vel = focus_vel(r.mugrid[m], a, b);

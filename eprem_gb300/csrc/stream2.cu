@@ -37,8 +37,11 @@ namespace eprem {
 // the compile-time-guard kernel): N = 1000 -- 256x4 0.42, 128x4 in clusters
 // of 2 0.40, 256x3 in clusters of 2 0.24, 384x3 and 512x2 (register spills)
 // 0.24; N = 1500 -- 128x4 in clusters of 3 0.39, 256x3 in clusters of 2
-// 0.37, 256x4 in clusters of 2 (27 % of the slots idle) 0.29.  Shapes that
-// spill are not kept; where two shapes waste as few slots, the earlier wins.
+// 0.37, 384x2 in clusters of 2 (12 warps/SM, 168 registers) 0.34, 256x4 in
+// clusters of 2 (27 % of the slots idle) 0.29.  More warps per SM at fewer
+// registers lost at both sizes: 352x3 and 512x2 (register-capped, spilling)
+// 0.24 at N = 1000.  Shapes that spill are not kept; where two shapes waste
+// as few slots, the earlier wins.
 #define EPREM_S2_SHAPES(X)                                                             \
   X(8, 512, 2) X(16, 512, 2) X(24, 512, 2) X(24, 256, 4) X(24, 128, 4) X(32, 256, 4)  \
   X(32, 128, 4) X(32, 256, 3) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3) X(48, 256, 3) \
@@ -735,7 +738,15 @@ __global__ void k_stream2_coef(RunView r) {
       const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
       // split form: the relaxation runs in the node phase instead
       const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
-      out = make_float4((float)mult, (float)emt, (float)(1.0 - emt),
+      // exp(-dtProp/tau) and 1 - it as multiples of 2^-24: both exact in
+      // float and summing to exactly 1, so f em + iso om keeps the sum over
+      // mu (up to the unbiased rounding of the sums).  Rounded one by one
+      // they missed 1 by up to 3e-8 -- a fixed factor on a node's particle
+      // number at every sub-cycle, which 10^5 sub-cycles (a few driver steps
+      // at hundreds of streaming sub-cycles) took to 1e-3 of the flux.  The
+      // rate itself moves by at most 2^-25 per sub-cycle.
+      const double qe = rint(emt * 16777216.0);
+      out = make_float4((float)mult, (float)(qe * 0x1p-24), (float)((16777216.0 - qe) * 0x1p-24),
                         (float)ldexp(seed_value(r, ec, r.seed_radial[gidx]), ec.seed_k));
     }
     r.scoef[i] = out;
