@@ -309,6 +309,28 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
 // same exponent differences.  The change takes one or two sub-cycles per
 // step, so its cost is the log / exp per cell (hardware approximations, ~1e-6
 // relative on f).
+// ln of a stored value relative to 2^kRowTop, where a normalised row's
+// largest value lies, so that a row's leading cells have |ln| < 1 and keep
+// float's relative precision in the flux-form update: the power of two
+// from the float's exponent field, exact, plus ln of the mantissa in [1, 2)
+// (__logf's absolute error there is about 4e-7; on the stored value itself,
+// near 2^95, its error and the rounding of a ln near 66 reached 1e-5 of f
+// per conversion, a bias that the sub-steps of a run accumulated).  Values
+// below FLT_MIN are the float floor.
+__device__ __forceinline__ float ln_rel(float v) {
+  constexpr float kLn2 = 0.6931471805599453f;
+  const int b = __float_as_int(v < FLT_MIN ? FLT_MIN : v);
+  const float mant = __int_as_float((b & 0x007fffff) | 0x3f800000);
+  return (float)(((b >> 23) & 0xff) - 127 - kRowTop) * kLn2 + __logf(mant);
+}
+// exp(l) 2^k for l = ln_rel of a value: the exponential of the small
+// relative ln, then an exact power of two; the far tail of a row (l below
+// -80) takes 2^-64 into the exponential to stay above float underflow.
+__device__ __forceinline__ float exp_rel(float l, int k) {
+  constexpr float kLn2 = 0.6931471805599453f;
+  return l > -80.f ? ldexp_f(__expf(l), k) : ldexp_f(__expf(l + 64.f * kLn2), k - 64);
+}
+
 __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc) {
   extern __shared__ float sm[];
   constexpr float kLn2 = 0.6931471805599453f;
@@ -321,9 +343,11 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   float *lnf = sm;                                             // [E][T]
   int *xs = reinterpret_cast<int *>(sm + (size_t)E * T);     // [npc][E] row exponents
   int *sh = xs + npc * E;                                      // [npc][E] renormalising shifts
+  // the rows' exponents less kRowTop: ln f = lnf - xs ln 2 with lnf the ln of
+  // a stored value relative to 2^kRowTop (see ln_rel)
   for (int i = tid; i < npc * E; i += blockDim.x) {
     const size_t gg = (size_t)blockIdx.x * npc + i / E;
-    xs[i] = gg < SN ? r.fexp[gg * E + i % E] : 0;
+    xs[i] = (gg < SN ? r.fexp[gg * E + i % E] : 0) - kRowTop;
   }
   bool ok = false;
   NodeCoef32 c{};
@@ -334,7 +358,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   float *col = reinterpret_cast<float *>(r.f) + (ok ? g : 0) * E * M + m;  // stride M
   float *fc = lnf + tid;                                                    // stride T
   if (ok)
-    for (int e = 0; e < E; ++e) fc[e * T] = __logf(col[e * M]);
+    for (int e = 0; e < E; ++e) fc[e * T] = ln_rel(col[e * M]);
   __syncthreads();
   if (ok && c.ns_c > 0) {
     const int *x = xs + j * E;
@@ -391,18 +415,19 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
       float mx = rowp[0];
       for (int mm = 1; mm < M; ++mm) mx = fmaxf(mx, rowp[mm]);
       const float l2 = fminf(fmaxf(floorf(mx * 1.4426950408889634f), -1.0e6f), 1.0e6f);
-      const int x0 = xs[j * E + e];
-      sh[j * E + e] = clamp_exp(x0 + kRowTop - (int)l2) - x0;
+      const int x0 = xs[j * E + e] + kRowTop;
+      sh[j * E + e] = clamp_exp(x0 - (int)l2) - x0;
     }
   __syncthreads();
   if (ok) {
     int code = 0;
     for (int e = 0; e < E; ++e) {
-      const float v = __expf(fc[e * T] + (float)sh[j * E + e] * kLn2);
+      const float v = exp_rel(fc[e * T], sh[j * E + e] + kRowTop);
       if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / r.N), (int)(g % r.N), e, m);
       col[e * M] = v < FLT_MIN ? FLT_MIN : v;
     }
-    for (int e = m; e < E; e += M) r.fexp[g * E + e] = (short)(xs[j * E + e] + sh[j * E + e]);
+    for (int e = m; e < E; e += M)
+      r.fexp[g * E + e] = (short)(xs[j * E + e] + kRowTop + sh[j * E + e]);
   }
 }
 

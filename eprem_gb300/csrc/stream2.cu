@@ -47,6 +47,25 @@ namespace eprem {
   X(32, 128, 4) X(32, 256, 3) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3) X(48, 256, 3) \
   X(48, 128, 3) X(64, 256, 2) X(64, 128, 2)
 
+// The relaxation weight of one sub-cycle, f <- f (1 - om) + iso om with
+// om = 1 - exp(-dtProp/tau).  For the sum over mu to be kept, 1 - om must be
+// exact in float, so om is a multiple of 2^-24; rounding it there once moved
+// the relaxation rate by up to 2^-25 / om (1e-4 at the 1536-stream case,
+// whose om is 3e-4 - 1e-3), a bias that the diffusive tail of the
+// distribution turns into 1e-3 of the flux 15 decades below its peak.  So
+// om alternates between the two multiples around it (omlo and omlo +
+// 2^-24) with an error-diffusion counter: over any run of sub-cycles the
+// weights sum to the exact om times their number within 2^-24, and every
+// single sub-cycle still keeps the sum.  Splitting the weight apart, f +
+// om (iso - f), would do the same at one more packed operation per cell
+// pair.  dith starts at 1/2 in every launch; phi is om 2^24 - omlo 2^24.
+__device__ __forceinline__ float relax_weight(float omlo, float phi, float &dith) {
+  dith += phi;
+  const bool up = dith >= 1.f;
+  dith = up ? dith - 1.f : dith;
+  return up ? omlo + 0x1p-24f : omlo;
+}
+
 // The common exponent of a (stream, energy) slab (FP32 row exponents): the
 // largest true value of its rows, and of the seeds the sub-step can write,
 // brought to [2^kRowTop, 2^(kRowTop+1)).  lg: this thread's largest
@@ -136,7 +155,7 @@ __global__ void __launch_bounds__(T, 1) k_stream2(RunView r, int m0) {
   // per node: mult for each upwind direction (zero where the reference leaves
   // the cell unchanged: first list node for mu >= 0, last for mu < 0),
   // relaxation factor exp(-dtProp/tau) and 1 - it, boundary seed
-  float mhi[NPT], mlo[NPT], em[NPT], om[NPT];
+  float mhi[NPT], mlo[NPT], phi[NPT], omlo[NPT], dith[NPT];
   __shared__ float s_bcv[3];  // seeds of list nodes 0..2, the boundary (CTA rank 0)
   __shared__ int s_red[W + 1];
   const double vdt = ec.vgrid * dtProp;
@@ -149,7 +168,8 @@ __global__ void __launch_bounds__(T, 1) k_stream2(RunView r, int m0) {
   const bool seeds_in = r.check_seed != 0;
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
-    mhi[q] = mlo[q] = em[q] = om[q] = 0.f;
+    mhi[q] = mlo[q] = phi[q] = omlo[q] = 0.f;
+    dith[q] = 0.5f;
     xr[q] = 0;
     sw[q] = 0.f;
 #pragma unroll
@@ -180,8 +200,8 @@ __global__ void __launch_bounds__(T, 1) k_stream2(RunView r, int m0) {
       if ((seeds_in || (r.use_bc && il < 3)) && ls != kNoExp) lg = max(lg, ls - ec.seed_k);
       mhi[q] = (il == 0) ? 0.f : c.x;
       mlo[q] = (il == L - 1) ? 0.f : c.x;
-      em[q] = c.y;
-      om[q] = c.z;
+      phi[q] = c.y;
+      omlo[q] = c.z;
     }
   }
   // the slab's common exponent; rows and seeds brought to it (exact powers of two)
@@ -298,11 +318,12 @@ __global__ void __launch_bounds__(T, 1) k_stream2(RunView r, int m0) {
     }
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
-      const float iso = (inv_m * acc[q]) * om[q];
+      const float om = relax_weight(omlo[q], phi[q], dith[q]), em = 1.f - om;
+      const float iso = (inv_m * acc[q]) * om;
 #pragma unroll
       for (int j = 0; j < H; ++j) {
-        Lf[q][j] = Lf[q][j] * em[q] + iso;
-        Rf[q][j] = Rf[q][j] * em[q] + iso;
+        Lf[q][j] = Lf[q][j] * em + iso;
+        Rf[q][j] = Rf[q][j] * em + iso;
       }
     }
   }
@@ -398,8 +419,8 @@ __device__ __forceinline__ void stream2_pairs_slab(const RunView &r, const int s
   const int i0 = NPT * (crank * T + tid);
   const size_t sN = (size_t)s * N;
   float2 Lf[NPT][P], Rf[NPT][P];  // mu = 2p, 2p+1 and m0 + 2p, m0 + 2p + 1
-  float2 mhi[NPT], mlo[NPT], em[NPT];
-  float om[NPT];
+  float2 mhi[NPT], mlo[NPT];
+  float phi[NPT], omlo[NPT], dith[NPT];
   __shared__ float s_bcv[3];
   __shared__ int s_red[W + 1];
   const double vdt = ec.vgrid * dtProp;
@@ -409,8 +430,9 @@ __device__ __forceinline__ void stream2_pairs_slab(const RunView &r, const int s
   int lg = kNoExp;  // largest floor(log2) of a true value of this thread's rows and seeds
 #pragma unroll
   for (int q = 0; q < NPT; ++q) {
-    mhi[q] = mlo[q] = em[q] = make_float2(0.f, 0.f);
-    om[q] = 0.f;
+    mhi[q] = mlo[q] = make_float2(0.f, 0.f);
+    phi[q] = omlo[q] = 0.f;
+    dith[q] = 0.5f;
     xr[q] = 0;
     sw[q] = 0.f;
 #pragma unroll
@@ -456,8 +478,8 @@ __device__ __forceinline__ void stream2_pairs_slab(const RunView &r, const int s
       const float mh = (il == 0) ? 0.f : c.x, ml = (il == L - 1) ? 0.f : c.x;
       mhi[q] = make_float2(mh, mh);
       mlo[q] = make_float2(ml, ml);
-      em[q] = make_float2(c.y, c.y);
-      om[q] = c.z;
+      phi[q] = c.y;
+      omlo[q] = c.z;
     }
   }
   // the slab's common exponent; rows and seeds brought to it (exact powers of two)
@@ -615,12 +637,13 @@ __device__ __forceinline__ void stream2_pairs_slab(const RunView &r, const int s
     }
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
-      const float iso = (inv_m * (acc[q].x + acc[q].y)) * om[q];
-      const float2 iso2 = make_float2(iso, iso);
+      const float om = relax_weight(omlo[q], phi[q], dith[q]), em = 1.f - om;
+      const float iso = (inv_m * (acc[q].x + acc[q].y)) * om;
+      const float2 iso2 = make_float2(iso, iso), em2 = make_float2(em, em);
 #pragma unroll
       for (int p = 0; p < P; ++p) {
-        Lf[q][p] = __ffma2_rn(Lf[q][p], em[q], iso2);
-        Rf[q][p] = __ffma2_rn(Rf[q][p], em[q], iso2);
+        Lf[q][p] = __ffma2_rn(Lf[q][p], em2, iso2);
+        Rf[q][p] = __ffma2_rn(Rf[q][p], em2, iso2);
       }
     }
     if (!FILLED && (shL | shR)) {  // padding back to zero (uniform branch)
@@ -738,15 +761,12 @@ __global__ void k_stream2_coef(RunView r) {
       const double mult = (dtProp > tau) ? dsi * tau * dtProp_i : dsi * 1.0;
       // split form: the relaxation runs in the node phase instead
       const double emt = r.relax_in_stream ? exp(-dtProp / tau) : 1.0;
-      // exp(-dtProp/tau) and 1 - it as multiples of 2^-24: both exact in
-      // float and summing to exactly 1, so f em + iso om keeps the sum over
-      // mu (up to the unbiased rounding of the sums).  Rounded one by one
-      // they missed 1 by up to 3e-8 -- a fixed factor on a node's particle
-      // number at every sub-cycle, which 10^5 sub-cycles (a few driver steps
-      // at hundreds of streaming sub-cycles) took to 1e-3 of the flux.  The
-      // rate itself moves by at most 2^-25 per sub-cycle.
-      const double qe = rint(emt * 16777216.0);
-      out = make_float4((float)mult, (float)(qe * 0x1p-24), (float)((16777216.0 - qe) * 0x1p-24),
+      // the relaxation weight om = 1 - exp(-dtProp/tau) as its multiple of
+      // 2^-24 below (y: the fraction left over, z: that multiple): see
+      // relax_weight
+      const double om = (1.0 - emt) * 16777216.0;
+      const double lo = floor(om);
+      out = make_float4((float)mult, (float)(om - lo), (float)(lo * 0x1p-24),
                         (float)ldexp(seed_value(r, ec, r.seed_radial[gidx]), ec.seed_k));
     }
     r.scoef[i] = out;
