@@ -7,9 +7,14 @@ updateEnergeticParticles (numEpSteps = 30 sub-steps), src/eprem.c:620-671.
 
 Workload (default): the precision-at-scale case -- 1536 streams x 1000 nodes x
 50 energies (0.1-1000 MeV) x 40 mu, Parker wind, seed power law -- in the
-chosen form (f and stencil arithmetic in FP32, geometry / CFL in FP64).  The
-plain FP64 form is measured beside it on a 96-stream subset with identical
-per-stream work, and the FP32 omnidirectional flux is compared with it.
+chosen form (f and stencil arithmetic in FP32 with a binary exponent per
+row, geometry / CFL in FP64).  The plain FP64 form is measured beside it on
+48 streams sampled from the 1536, stepped from the same state through the
+same steps, and the FP32 omnidirectional flux is compared with it.  Further
+legs: the MHD-coupled (MAS) workload, the batched ensembles (8 runs of
+uneven sizes; 64 runs of the CPU-runnable case's size), the split form and
+the surrogate, and the CPU baseline -- the reference's own C of the path,
+built with its own flags, one process per host core.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -42,7 +47,7 @@ BYTES_PER_CELL_UPDATE = {"fp64": 32.0, "fp32": 16.0}
 # profiles/k_stream_fp64_96streams.txt, profiles/k_focus32_k_change32_fp32_96streams.txt):
 # traffic per launch / 96*1000*50*40 cells; traffic grows with the number of
 # (stream, energy) slabs, so it scales to a full launch by the cells processed.
-NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1570.3949e6 / 192e6,
+NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1600.7276e6 / 192e6,
                            ("stream", "fp64"): 3054.831e6 / 192e6,
                            ("node", "fp32"): 1488.048e6 / 192e6}
 
@@ -70,6 +75,9 @@ def parse():
     ap.add_argument("--ensemble-steps", type=int, default=2)
     ap.add_argument("--ensemble-only", action="store_true",
                     help="measure only the batched ensemble (with --ensemble-runs 64: the full set)")
+    ap.add_argument("--skip-ensemble-small", action="store_true")
+    ap.add_argument("--ensemble-small-runs", type=int, default=64,
+                    help="runs of the CPU-runnable case's size in the small-run ensemble")
     ap.add_argument("--skip-surrogate", action="store_true")
     ap.add_argument("--surrogate-faces", type=int, default=4,
                     help="rows=cols of the surrogate case's grid (6*n*n streams)")
@@ -532,6 +540,14 @@ def ours(args, rank, ws, dist):
     if not args.skip_ensemble and rank == 0:
         from eprem_gb300 import Ensemble
         ensemble = ensemble_case(args, EpremRun, Ensemble, abi, W)
+    ensemble_small = None
+    if not args.skip_ensemble_small and rank == 0:
+        from eprem_gb300 import Ensemble
+        ensemble_small = ensemble_case(
+            args, EpremRun, Ensemble, abi, W,
+            members=W.ensemble_members_small(args.ensemble_small_runs), steps=4,
+            schedules=(-1,),
+            what="a parameter sweep of runs of the CPU-runnable case's size")
 
     # ---- CPU baseline ----------------------------------------------------
     cpu = None
@@ -565,6 +581,7 @@ def ours(args, rank, ws, dist):
             "plain_fp64": plain,
             "mhd_coupled": mas,
             "ensemble": ensemble,
+            "ensemble_small": ensemble_small,
             "alu_peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak},
             "stats_last_step": stats.as_dict(),
         }
@@ -755,7 +772,8 @@ def mas_case(args, EpremRun, abi, W, fp32_peak, hbm_peak):
     return out
 
 
-def ensemble_case(args, EpremRun, Ensemble, abi, W):
+def ensemble_case(args, EpremRun, Ensemble, abi, W, members=None, steps=None,
+                  schedules=(0, 1, -1), what=None):
     """The batched-ensemble workload: the first n of 64 runs with uneven
     sizes and parameters (24-1536 streams, 400-2000 nodes, 20-50 E, 20-40 mu,
     seed index, mean free path and shock speed drawn from a fixed seed) in
@@ -766,7 +784,8 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     the state (nodes, background, seed population), take one untimed step and
     time the same K steps, so both do the same sub-cycles."""
     import torch
-    members = W.ensemble_members(64)[: args.ensemble_runs]
+    if members is None:
+        members = W.ensemble_members(64)[: args.ensemble_runs]
     runs = [EpremRun(w.dims(abi.EPREM_FP32), w.params, W.build_grids(w)) for w in members]
 
     def initial_state():
@@ -784,7 +803,7 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     ens = Ensemble(runs)
     chosen = ens.autotune()
     t_tune = time.perf_counter() - t_tune
-    K = args.ensemble_steps
+    K = steps or args.ensemble_steps
 
     # one after another, per-run entry points, host-timed around device syncs
     initial_state()
@@ -805,7 +824,7 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     # serial chain, and lock-step with merged streaming launches (the
     # default, last); `value` is the default's
     by_chains = {}
-    for chains in (0, 1, -1):
+    for chains in schedules:
         initial_state()
         ens.set_chains(chains)
         ens.set_time([w.params.t_del for w in members])
@@ -839,15 +858,19 @@ def ensemble_case(args, EpremRun, Ensemble, abi, W):
     ens_err = flux_rel_err(j32, r64.omni_flux())
     r64.close()
     out = {
+        "workload": what or "the first runs of the 64-run ensemble of uneven sizes",
         "flux_rel_err_fp32_vs_fp64": ens_err,
         "flux_err_of": (f"member {im} ({wm.name.split(': ')[1]}, the smallest stepped) after "
                         f"{1 + K} graph steps, against its FP64 run from the same state; "
                         f"J > 1e-30 max J"),
         "value": cells * K / (ms * 1e-3), "unit": UNIT,
-        "value_by_schedule": {"branch_per_run": by_chains[0], "one_chain": by_chains[1],
-                              "lockstep_merged_streaming": by_chains[-1]},
-        "runs": len(members), "of_runs": 64, "total_cells": sum(w.cells for w in members),
-        "sizes": [w.name.split(": ")[1] for w in members],
+        "value_by_schedule": {{0: "branch_per_run", 1: "one_chain",
+                               -1: "lockstep_merged_streaming"}[c]: v
+                              for c, v in by_chains.items()},
+        "runs": len(members), "of_runs": 64 if what is None else len(members),
+        "total_cells": sum(w.cells for w in members),
+        "sizes": (sorted(set(w.name.split(": ")[1] for w in members)) if what else
+                  [w.name.split(": ")[1] for w in members]),
         "steps": K, "warmup": 1, "ms_per_step": ms / K,
         "graph_launches_per_step": 1, "kernel_launches_per_step": launches // K,
         "one_by_one_value": cells * K / seq_s,

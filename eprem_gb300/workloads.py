@@ -517,3 +517,28 @@ def ensemble_members(n: int = 64, seed: int = 20240607) -> list[Workload]:
                      1000.0, 0.05, 5.0, p, seed=seed + i)
         out.append(w)
     return out
+
+
+def ensemble_members_small(n: int = 64, seed: int = 20240611) -> list[Workload]:
+    """A parameter sweep of n runs of the CPU-runnable case's size (24 streams
+    x 400 nodes x 20 E x 20 mu, 0.1-100 MeV, 0.05-5 AU): seed-spectrum index
+    -[2.5, 4], lambda_parallel 0.05-1 AU at 1 GV and an ideal shock at
+    800-2500 km/s drawn from splitmix64(seed).  Each run alone holds 480
+    (stream, energy) slabs, about three per SM: too few to fill the GPU,
+    which is where one launch over all runs' slabs pays."""
+    u = 0.5 * (uniform_pm1(seed, 4 * n).reshape(n, 4) + 1.0)
+    out = []
+    for i in range(n):
+        p = _plain_wind_params()
+        p.bf_gamma = 2.5 + 1.5 * u[i, 0]
+        p.lamo = 0.05 + 0.95 * u[i, 1]
+        p.ideal_shock = 1
+        p.ideal_shock_speed = (800.0 + 1700.0 * u[i, 2]) * 1e5
+        p.ideal_shock_jump = 2.9
+        p.ideal_shock_init_time = 0.0
+        p.ideal_shock_theta = PI / 2
+        p.ideal_shock_phi = 2.0 * PI * u[i, 3]
+        p.ideal_shock_width = 2.0 * math.radians(30.0)
+        out.append(Workload(f"small member {i}: 24x400x20x20", 2, 2, 400, 20, 20, 0.1, 100.0,
+                            0.05, 5.0, p, seed=seed + i))
+    return out
