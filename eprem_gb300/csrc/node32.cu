@@ -311,24 +311,29 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
 // relative on f).
 // ln of a stored value relative to 2^kRowTop, where a normalised row's
 // largest value lies, so that a row's leading cells have |ln| < 1 and keep
-// float's relative precision in the flux-form update: the power of two
-// from the float's exponent field, exact, plus ln of the mantissa in [1, 2)
-// (__logf's absolute error there is about 4e-7; on the stored value itself,
-// near 2^95, its error and the rounding of a ln near 66 reached 1e-5 of f
-// per conversion, a bias that the sub-steps of a run accumulated).  Values
-// below FLT_MIN are the float floor.
+// float's relative precision in the flux-form update.  The value is scaled
+// by an exact power of two first: by 2^-95 (__logf's absolute error on
+// [0.5, 2], where the leading cells land, is about 4e-7), or for values
+// more than 2^125 below the top, negligible in their row, by 2^31.  Taken
+// of the stored value itself near 2^95, __logf's error and the rounding of
+// a logarithm near 66 reached 1e-5 of f per conversion, a bias that the
+// sub-steps of a run accumulated.  Values below FLT_MIN are the floor.
 __device__ __forceinline__ float ln_rel(float v) {
   constexpr float kLn2 = 0.6931471805599453f;
-  const int b = __float_as_int(v < FLT_MIN ? FLT_MIN : v);
-  const float mant = __int_as_float((b & 0x007fffff) | 0x3f800000);
-  return (float)(((b >> 23) & 0xff) - 127 - kRowTop) * kLn2 + __logf(mant);
+  v = v < FLT_MIN ? FLT_MIN : v;
+  const bool top = v >= 0x1p-30f;
+  return __logf(v * (top ? 0x1p-95f : 0x1p31f)) + (top ? 0.f : -126.f * kLn2);
 }
-// exp(l) 2^k for l = ln_rel of a value: the exponential of the small
-// relative ln, then an exact power of two; the far tail of a row (l below
-// -80) takes 2^-64 into the exponential to stay above float underflow.
-__device__ __forceinline__ float exp_rel(float l, int k) {
+static_assert(kRowTop == 95, "ln_rel rescales by 2^-95");
+// exp(l) * scale for l = ln_rel of a value and scale = 2^k, the row's
+// exact power of two (0 below the float range): the exponential of the
+// small relative logarithm, then one exact product; the far tail of a row
+// (l below -80) takes 2^-64 into the exponential to stay above float
+// underflow.
+__device__ __forceinline__ float exp_rel(float l, float scale) {
   constexpr float kLn2 = 0.6931471805599453f;
-  return l > -80.f ? ldexp_f(__expf(l), k) : ldexp_f(__expf(l + 64.f * kLn2), k - 64);
+  const bool near = l > -80.f;
+  return __expf(near ? l : l + 64.f * kLn2) * (near ? scale : scale * 0x1p-64f);
 }
 
 __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc) {
@@ -343,11 +348,24 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   float *lnf = sm;                                             // [E][T]
   int *xs = reinterpret_cast<int *>(sm + (size_t)E * T);     // [npc][E] row exponents
   int *sh = xs + npc * E;                                      // [npc][E] renormalising shifts
+  float *sc = reinterpret_cast<float *>(sh + npc * E);         // [npc][E] 2^(sh + kRowTop)
+  float *dnl = sc + npc * E;   // [npc][E] (x_e - x_{e+1}) ln 2
+  float *xd = dnl + npc * E;   // [npc][E] x_e ln 2 (1/v_{e+1} - 1/v_{e-1})
+  float *vw = xd + npc * E;    // [E] 1/v_e + 1/v_{e+1}: face e+1's sum of the two cells' 1/v
   // the rows' exponents less kRowTop: ln f = lnf - xs ln 2 with lnf the ln of
   // a stored value relative to 2^kRowTop (see ln_rel)
   for (int i = tid; i < npc * E; i += blockDim.x) {
     const size_t gg = (size_t)blockIdx.x * npc + i / E;
     xs[i] = (gg < SN ? r.fexp[gg * E + i % E] : 0) - kRowTop;
+  }
+  for (int e = tid; e < E; e += blockDim.x)
+    vw[e] = e + 1 < E ? r.ec[e].vi32 + r.ec[e + 1].vi32 : 0.f;
+  __syncthreads();
+  // each row's exponent terms of the flux form, once per node and energy
+  for (int i = tid; i < npc * E; i += blockDim.x) {
+    const int e = i % E;
+    dnl[i] = e + 1 < E ? (float)(xs[i] - xs[i + 1]) * kLn2 : 0.f;
+    xd[i] = ((float)xs[i] * kLn2) * r.ec[e].dvi32;
   }
   bool ok = false;
   NodeCoef32 c{};
@@ -362,6 +380,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   __syncthreads();
   if (ok && c.ns_c > 0) {
     const int *x = xs + j * E;
+    const float *dn_j = dnl + j * E, *xd_j = xd + j * E;
     const float mu = r.mugrid32[m];
     const float am = -mu * c.dupar;
     const float bm = mu * mu * (c.dlnn - c.dlnb) + 0.5f * (1.f - mu * mu) * c.dlnb;
@@ -370,15 +389,14 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
     // the seeds relative to the first and last rows' exponents
     const float bc0 = c.bc0 + (float)(c.kbc0 + x[0]) * kLn2;
     const float bc1 = c.bc1 + (float)(c.kbc1 + x[E - 1]) * kLn2;
-    const EnergyConsts *ec = r.ec;
+    const float sch = sc * 0.5f;
+    // face e+1 (between energies e and e+1): q = dt_sub/dlnp times the mean of
+    // the two cell velocities cool (am/v + bm) = qa (1/v_e + 1/v_{e+1}) + qb
+    const float qa = sch * cool * am, qb = sch * cool * (2.f * bm);
     for (int s = 0; s < c.ns_c; ++s) {
-      // face e lies between energies e-1 and e: q = dt_sub/dlnp times the
-      // mean of the two cell velocities cool (am/v + bm)
-      float vel_lo = cool * (am * ec[0].vi32 + bm);
-      float vel_hi = cool * (am * ec[1].vi32 + bm);
-      const float q1 = sc * 0.5f * (vel_hi + vel_lo);
+      const float q1 = qa * vw[0] + qb;
       const float f0 = fc[0], f1 = fc[T];
-      float dprev = (float)(x[0] - x[1]) * kLn2;  // c_1 - c_0
+      float dprev = dn_j[0];  // c_1 - c_0
       float gprev = q1 * (q1 >= 0.f ? f0 : f1);
       float cprev = q1 >= 0.f ? q1 * dprev : 0.f;  // -q_p (c_b - c_e) of the next cell
       const float d0 = (q1 <= 0.f) ? q1 * (f1 - f0 + dprev) : q1 * (f0 - bc0);
@@ -386,18 +404,18 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
       fc[0] = f0 - d0;
       float qcur = q1, fe = f1;
       for (int e = 1; e < E - 1; ++e) {
-        vel_lo = vel_hi;
-        vel_hi = cool * (am * ec[e + 1].vi32 + bm);
-        const float qq = sc * 0.5f * (vel_hi + vel_lo);
+        const float qq = qa * vw[e] + qb;
         const float fn = fc[(e + 1) * T];
-        const float dn = (float)(x[e] - x[e + 1]) * kLn2;  // c_{e+1} - c_e
-        const float gnext = qq * (qq >= 0.f ? fe : fn);
-        const float corr =
-            (qq < 0.f ? qq * dn : 0.f) + cprev - ((float)x[e] * kLn2) * (hq * ec[e].dvi32);
+        const float dn = dn_j[e];  // c_{e+1} - c_e
+        const float qdn = qq * dn;
+        const bool up = qq >= 0.f;
+        const float gnext = qq * (up ? fe : fn);
+        // c_e's share of the divergence term: x_e ln2 hq (1/v_{e+1} - 1/v_{e-1})
+        const float corr = (up ? 0.f : qdn) + cprev - hq * xd_j[e];
         fold_prev = fe;
         fc[e * T] = fe - (gnext - gprev) - corr;
         gprev = gnext;
-        cprev = qq >= 0.f ? qq * dn : 0.f;
+        cprev = up ? qdn : 0.f;
         qcur = qq;
         fe = fn;
         dprev = dn;
@@ -416,13 +434,15 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
       for (int mm = 1; mm < M; ++mm) mx = fmaxf(mx, rowp[mm]);
       const float l2 = fminf(fmaxf(floorf(mx * 1.4426950408889634f), -1.0e6f), 1.0e6f);
       const int x0 = xs[j * E + e] + kRowTop;
-      sh[j * E + e] = clamp_exp(x0 - (int)l2) - x0;
+      const int d = clamp_exp(x0 - (int)l2) - x0;
+      sh[j * E + e] = d;
+      sc[j * E + e] = d + kRowTop >= -126 ? pow2f(min(d + kRowTop, 127)) : 0.f;
     }
   __syncthreads();
   if (ok) {
     int code = 0;
     for (int e = 0; e < E; ++e) {
-      const float v = exp_rel(fc[e * T], sh[j * E + e] + kRowTop);
+      const float v = exp_rel(fc[e * T], sc[j * E + e]);
       if (bad_value(v, &code)) set_error(r, code, 3, (int)(g / r.N), (int)(g % r.N), e, m);
       col[e * M] = v < FLT_MIN ? FLT_MIN : v;
     }
@@ -469,7 +489,9 @@ static void launch_focus_t(const RunView &r, cudaStream_t st) {
 static void launch_change(const RunView &r, cudaStream_t st) {
   const int npc = r.M >= kChangeThreads ? 1 : kChangeThreads / r.M;
   const size_t SN = (size_t)r.S * r.N;
-  const size_t smem = (size_t)r.E * npc * r.M * sizeof(float) + 2 * (size_t)npc * r.E * sizeof(int);
+  const size_t smem =
+      (size_t)r.E * npc * r.M * sizeof(float) + 5 * (size_t)npc * r.E * sizeof(int) +
+      (size_t)r.E * sizeof(float);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_change32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_change32<<<(unsigned)((SN + npc - 1) / npc), kChangeThreads, smem, st>>>(r, npc);
