@@ -276,9 +276,10 @@ def timed_steps(run, w, steps, t0):
     return ms, launches, kt, stats, t
 
 
-def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
+def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form, stream_kernel=None):
     """Roofline of the dominant kernel: algorithmic flops per launch over the
-    kernel's mean CUDA-event duration, against the measured FMA peak."""
+    kernel's mean CUDA-event duration, against the measured FMA peak.
+    stream_kernel: the run's streaming kernel (EpremRun.stream_kernel)."""
     kind = max(("stream", "node"), key=lambda k: kt[k][1])
     launches, total_ms = kt[kind]
     fl = flops_of(stats)[kind]
@@ -288,7 +289,8 @@ def roofline(kt, stats, steps, peak_tflops, hbm_peak, cells, form):
     # algorithmic HBM bytes: one read + one write of f per operator pass
     bytes_per_launch = cells * BYTES_PER_CELL_UPDATE[form] / 2.0
     return {
-        "kernel": ({"fp32": "k_stream2_pairs", "fp64": "k_stream"}[form] if kind == "stream"
+        "kernel": ((stream_kernel or {"fp32": "k_stream2", "fp64": "k_stream"}[form])
+                   if kind == "stream"
                    else {"fp32": "k_focus32+k_change32", "fp64": "k_node"}[form]),
         "bound": "fp64" if form == "fp64" else "fp32",
         "achieved": round(achieved, 3), "peak": round(peak_tflops, 3), "unit": "TFLOP/s",
@@ -456,7 +458,8 @@ def ours(args, rank, ws, dist):
     j32_s = run.omni_flux().reshape(w.num_streams, -1)[idx].reshape(-1)
     cell_updates = w.cells * w.params.num_ep_steps * args.steps
     value = cell_updates * ws / (ms_max * 1e-3)
-    roof = roofline(kt, stats, args.steps, fp32_peak, peaks.get("hbm_gbs"), w.cells, "fp32")
+    roof = roofline(kt, stats, args.steps, fp32_peak, peaks.get("hbm_gbs"), w.cells, "fp32",
+                    run.stream_kernel)
 
     # ---- end to end through the C ABI with host buffers ------------------
     nodes_host = torch.empty(nodes.size, dtype=torch.float64, pin_memory=True).numpy()
@@ -501,6 +504,7 @@ def ours(args, rank, ws, dist):
         for _ in range(steps_done - 1):
             tt = step(r64, tt, w)
         ms64, l64, kt64, st64, _ = timed_steps(r64, w, 1, tt)
+        k64 = r64.stream_kernel
         j64 = r64.omni_flux()
         flux_err = flux_rel_err(j32_s, j64)
         d32 = abi.Dims(n, w.num_nodes, 1, w.num_energies, w.num_mu, abi.EPREM_FP32)
@@ -518,7 +522,7 @@ def ours(args, rank, ws, dist):
             "ms_per_step": ms64,
             "fp32_same_streams_value": cu / (ms32 * 1e-3),
             "roofline": roofline(kt64, st64, 1, fp64_peak, peaks.get("hbm_gbs"), cells_s,
-                                 "fp64"),
+                                 "fp64", k64),
             "flux_rel_err_fp32_vs_fp64": flux_err,
             "flux_err_of": (f"the headline FP32 run after its {steps_done} steps (warm-up + "
                             f"timed), at {n} sampled streams, against the FP64 form's run of "
@@ -766,7 +770,8 @@ def mas_case(args, EpremRun, abi, W, fp32_peak, hbm_peak):
                          sl.h2d_async_bytes - a0},
         "kernel_ms_per_step": {k: v[1] / args.mas_steps for k, v in kt.items() if v[0]},
         "gpu_launches": launches,
-        "roofline": roofline(kt, stats, args.mas_steps, fp32_peak, hbm_peak, w.cells, "fp32"),
+        "roofline": roofline(kt, stats, args.mas_steps, fp32_peak, hbm_peak, w.cells, "fp32",
+                             run.stream_kernel),
     }
     run.close()
     return out

@@ -2,6 +2,7 @@
 // stepped by one CUDA-graph launch (no counterpart in the reference, which
 // runs one simulation per process).
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -15,12 +16,12 @@ using namespace eprem;
 // ---- autotuner ---------------------------------------------------------------
 // Times the FP32 streaming kernels on a scratch copy of the run's first
 // streams (the kernel that takes 90 % of a step) and keeps the fastest: every
-// kind that fits the run (compile-time guards, packed, scalar) in every CTA
+// kind that fits the run (mirrored, compile-time guards, packed, scalar) in every CTA
 // shape of its mu bin (threads per CTA, list nodes per thread, and so the
 // cluster size for the run's stream length).  The copy has its own status
 // block, so the run's statistics are untouched.
 namespace {
-constexpr int kTuneKinds[] = {5, 4, 3};
+constexpr int kTuneKinds[] = {7, 6, 5, 4, 3};
 
 int tune_stream(eprem_gpu_run *r, int *chosen) {
   const eprem_params_t &p = r->params;
@@ -64,7 +65,9 @@ int tune_stream(eprem_gpu_run *r, int *chosen) {
   for (int variant : variants) {
     if (e != cudaSuccess) break;
     StreamPlan pl{};
-    if (plan_stream(EPREM_FP32, r->dims.num_nodes, r->dims.num_mu, r->m0, variant, &pl)) continue;
+    if (plan_stream(EPREM_FP32, r->dims.num_nodes, r->dims.num_mu, r->m0, variant,
+                    r->v.use_bc != 0, &pl))
+      continue;
     if (launch_stream(v, pl, r->m0, r->stream, &dummy)) {  // warm-up
       e = cudaGetLastError();
       break;
@@ -106,10 +109,25 @@ extern "C" int eprem_gpu_autotune(eprem_gpu_run *r, int *chosen_variant) {
   return tune_stream(r, chosen_variant);
 }
 
+extern "C" const char *eprem_gpu_stream_kernel(eprem_gpu_run *r) {
+  if (!r) return "";
+  const StreamPlan &p = r->splan;
+  char buf[96];
+  if (p.reg_coef != 2)
+    snprintf(buf, sizeof(buf), "k_stream<%d> cluster %d", p.mmax, p.cluster);
+  else
+    snprintf(buf, sizeof(buf), "%s<%d,%d,%d> cluster %d",
+             p.mirror ? "k_stream2_mirror" : p.packed ? "k_stream2_pairs" : "k_stream2", p.mmax,
+             p.threads, p.npt, p.cluster);
+  r->skernel = buf;
+  return r->skernel.c_str();
+}
+
 extern "C" int eprem_gpu_set_stream_variant(eprem_gpu_run *r, int variant) {
   if (!r) return fail(EPREM_GPU_ERR_ARG, "null run");
   StreamPlan pl{};
-  if (plan_stream(r->dims.precision, r->dims.num_nodes, r->dims.num_mu, r->m0, variant, &pl))
+  if (plan_stream(r->dims.precision, r->dims.num_nodes, r->dims.num_mu, r->m0, variant,
+                  r->v.use_bc != 0, &pl))
     return fail(EPREM_GPU_ERR_ARG, "streaming variant does not fit this run's sizes");
   r->splan = pl;
   r->params.stream_variant = variant;
@@ -224,7 +242,8 @@ extern "C" int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *e, int *chosen_va
   for (size_t i = 0; i < e->runs.size(); i++) {
     eprem_gpu_run *r = e->runs[i];
     StreamPlan key{};
-    plan_stream(r->dims.precision, r->dims.num_nodes, r->dims.num_mu, r->m0, 0, &key);
+    plan_stream(r->dims.precision, r->dims.num_nodes, r->dims.num_mu, r->m0, 0,
+                r->v.use_bc != 0, &key);
     const std::vector<int> k = {r->dims.precision, key.mmax, key.cluster, key.threads,
                                 r->dims.num_mu, r->m0};
     int variant = -1;
@@ -260,7 +279,8 @@ struct S2Group {
 };
 bool same_plan(const StreamPlan &a, const StreamPlan &b) {
   return a.mmax == b.mmax && a.threads == b.threads && a.npt == b.npt && a.cluster == b.cluster &&
-         a.packed == b.packed && a.filled == b.filled && a.reg_coef == b.reg_coef;
+         a.packed == b.packed && a.filled == b.filled && a.reg_coef == b.reg_coef &&
+         a.mirror == b.mirror;
 }
 }  // namespace
 

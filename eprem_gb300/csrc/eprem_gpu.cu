@@ -148,7 +148,8 @@ extern "C" int eprem_gpu_create(const eprem_dims_t *dims, const eprem_params_t *
   if (r->params.max_subcycles <= 0) r->params.max_subcycles = 1000000;
   const bool fast32 = dims->precision == EPREM_FP32 && params->adiabatic_focus_alg == 1 &&
                       params->adiabatic_change_alg == 1;
-  int prc = plan_stream(dims->precision, N, M, m0, params->stream_variant, &r->splan);
+  const bool bc = params->use_ep_boundary > 0 && params->use_boundary_function > 0;
+  int prc = plan_stream(dims->precision, N, M, m0, params->stream_variant, bc, &r->splan);
   if (!prc) prc = fast32 ? plan_node32(E, M, &r->nplan) : plan_node(dims->precision, E, M, &r->nplan);
   r->nplan.fast32 = fast32 ? 1 : 0;
   if (prc) {

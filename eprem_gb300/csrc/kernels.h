@@ -21,14 +21,19 @@ struct StreamPlan {
   int packed;    // stream2.cu: fp32x2 arithmetic on pairs of mu cells
   int filled;    // stream2.cu: M fills the bin, m0 = M/2 (guards known at compile time)
   int npt;       // stream2.cu: list nodes per thread
+  int mirror;    // stream2.cu: mu < 0 half in mirror order, one coefficient per two cells
+                 // (1 formed on the sub-cycle loop, 2 from shared memory)
 };
-int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan);
+// bc: the run has the seed boundary (the mirrored kinds need it)
+int plan_stream(int precision, int N, int M, int m0, int variant, bool bc, StreamPlan *plan);
 int launch_stream(const RunView &r, const StreamPlan &plan, int m0, cudaStream_t st,
                   uint64_t *launches);
 int launch_seed_check(const RunView &r, cudaStream_t st, uint64_t *launches);
 // stream2.cu -- FP32 streaming, two list nodes per thread (plan.reg_coef == 2)
 // shape: 0 automatic, k >= 1 the k-th CTA shape of M's bin (stream2_shape_count)
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan);
+// mirror: 0, or the mirrored kind (1, 2: StreamPlan::mirror), which needs filled and bc
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, int mirror, bool bc, int shape,
+                 StreamPlan *plan);
 int stream2_shape_count(int M);
 // The packed kinds over the slabs of several runs of one plan: the runs'
 // views (a kernel parameter) and items[i] = (run index, stream, energy, 0)

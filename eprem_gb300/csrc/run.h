@@ -34,6 +34,7 @@ struct eprem_gpu_run {
   eprem::RunView v{};
   eprem::MhdParams mhd{};
   eprem::StreamPlan splan{};
+  std::string skernel;  // eprem_gpu_stream_kernel's text
   eprem::NodePlan nplan{};
   int m0 = 0;
   double norm_radius = 0, neg_beta = 0;

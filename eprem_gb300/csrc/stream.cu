@@ -266,20 +266,26 @@ static int threads_for(int mmax) {
 // variant = kind + 8 * shape.  kind 0 automatic; FP32 form (stream2.cu):
 // 3 several list nodes per thread, 4 the same with packed fp32x2 arithmetic
 // (an odd mu half padded with a zero cell), 5 as 4 with the cell guards
-// resolved at compile time (M fills its bin, m0 = M/2) -- the automatic kind
-// is the first of 5, 4, 3 that fits; shape 0 lets plan_stream2 choose the
-// CTA shape from N, k >= 1 names the k-th shape of the mu bin.  The FP64 form
-// has one shape (k_stream, coefficients in shared memory); variants 1 and 2
-// name it there.
-int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *plan) {
+// resolved at compile time (M fills its bin, m0 = M/2), 6 and 7 as 5 with the
+// mu < 0 half in mirror order, one upwind coefficient per two cells (6 formed
+// on the sub-cycle loop, 7 from shared memory; both need the seed boundary)
+// -- the automatic kind is the first of 7, 5, 4, 3 that fits; shape 0 lets
+// plan_stream2 choose the CTA shape from N, k >= 1 names the k-th shape of
+// the mu bin.  The FP64 form has one shape (k_stream, coefficients in shared
+// memory); variants 1 and 2 name it there.
+int plan_stream(int precision, int N, int M, int m0, int variant, bool bc, StreamPlan *plan) {
   if (precision == EPREM_FP32) {
     const int kind = variant % 8, shape = variant / 8;
-    if (variant < 0 || kind == 1 || kind == 2 || kind > 5) return EPREM_GPU_ERR_ARG;
-    if ((kind == 0 || kind == 5) && plan_stream2(N, M, m0, true, true, shape, plan) == 0)
+    if (variant < 0 || kind == 1 || kind == 2) return EPREM_GPU_ERR_ARG;
+    if (kind == 6) return plan_stream2(N, M, m0, true, true, 1, bc, shape, plan);
+    if ((kind == 0 || kind == 7) && plan_stream2(N, M, m0, true, true, 2, bc, shape, plan) == 0)
       return 0;
-    if ((kind == 0 || kind == 4) && plan_stream2(N, M, m0, true, false, shape, plan) == 0)
+    if (kind == 7) return EPREM_GPU_ERR_ARG;
+    if ((kind == 0 || kind == 5) && plan_stream2(N, M, m0, true, true, 0, bc, shape, plan) == 0)
       return 0;
-    if ((kind == 0 || kind == 3) && plan_stream2(N, M, m0, false, false, shape, plan) == 0)
+    if ((kind == 0 || kind == 4) && plan_stream2(N, M, m0, true, false, 0, bc, shape, plan) == 0)
+      return 0;
+    if ((kind == 0 || kind == 3) && plan_stream2(N, M, m0, false, false, 0, bc, shape, plan) == 0)
       return 0;
     return EPREM_GPU_ERR_ARG;
   }
@@ -290,6 +296,7 @@ int plan_stream(int precision, int N, int M, int m0, int variant, StreamPlan *pl
   if (!mmax) return EPREM_GPU_ERR_ARG;
   plan->mmax = mmax;
   plan->reg_coef = 0;
+  plan->mirror = 0;
   plan->threads = threads_for<double, false>(mmax);
   plan->cluster = (N + plan->threads - 1) / plan->threads;
   if (plan->cluster > 8) return EPREM_GPU_ERR_ARG;  // portable cluster limit

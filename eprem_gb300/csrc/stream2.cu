@@ -15,9 +15,13 @@
 //   * warp-edge lanes publish only the half their neighbour needs (lane 31's
 //     last node for mu >= 0, lane 0's first node for mu < 0).
 // A CTA of T threads holds NPT*T list nodes (shapes per mu bin below; a
-// 1000-node stream fits one CTA of the default shapes).  Two kernels: k_stream2, the scalar shape
-// (any M and split), and k_stream2_pairs, the packed fp32x2 shapes, with f
-// held as float2 pairs (an odd half padded with a zero cell).
+// 1000-node stream fits one CTA of the default shapes).  Three kernels: k_stream2, the scalar
+// shape (any M and split), k_stream2_pairs, the packed fp32x2 shapes, with f
+// held as float2 pairs (an odd half padded with a zero cell), and
+// k_stream2_mirror, the packed shape with the mu < 0 half in mirror order so
+// that one upwind coefficient serves a cell of each half (coefficients in
+// shared memory; on one CTA per slab, warps hand their halo rows to their
+// neighbours through mbarriers instead of a CTA barrier per sub-cycle).
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -731,6 +735,391 @@ __global__ void __launch_bounds__(T, 1)
   stream2_pairs_slab<MMAX, T, NPT, FILLED>(mv.v[it.x], it.y, it.z, mv.m0[it.x]);
 }
 
+// The mirrored shapes (kinds 6 and 7): the packed shape with every cell guard
+// known at compile time (M = MMAX, m0 = M/2), with the mu < 0 half held in
+// mirror order -- slot j of that half is cell H-1-j, whose |mugrid| is that of
+// cell H+j on the uniform mu grid -- so that pair p of either half moves with
+// the same upwind coefficient c = mult |v dtProp mugrid|, written for the
+// mu < 0 half as f + c (f[+1] - f) (the reference's f + mult del (f - f[+1])
+// with del < 0, src/energeticParticles.c:2392-2397).  Per cell and sub-cycle
+// that leaves the difference, the update, the sum and the relaxation on the
+// FMA pipe.  Kind 7 forms the coefficients once per launch into shared memory
+// ([P/2][NPT][T] float4: one 16-byte load serves four cells on the sub-cycle
+// loop); kind 6 forms them on the loop (one packed multiply per node and pair
+// index, shared by the two halves).
+// The two ends of the stream keep their values without a zero multiplier:
+//   * list node 0, mu >= 0 (:2380): with the seed boundary, node 0 holds the
+//     seed at the upwind step, and so does its upwind neighbour -- the empty
+//     slots in front of it, which the boundary sets alike, or the first halo
+//     row, set to the seed once per launch -- so its difference is zero;
+//   * the last list node, mu < 0 (:2391): the slots are shifted so that it is
+//     the last node of its thread, which publishes its mu < 0 half each
+//     sub-cycle with the halo rows and reads it back as its neighbour.
+// So these kinds need the seed boundary and N + NPT - 1 slots.
+template <int MMAX, int T, int NPT, bool CSM>
+constexpr size_t stream2_mirror_smem_bytes() {
+  return stream2_smem_bytes<MMAX, T>() + sizeof(float) * 2 * (MMAX / 2) +
+         (CSM ? sizeof(float4) * (MMAX / 8) * NPT * T : 0);
+}
+
+// Bounded wait on a CTA mbarrier phase: at most kMirrorWaitLimit try_waits,
+// each of which suspends the warp until the phase completes or about a
+// microsecond has passed; false when the limit ran out.
+constexpr int kMirrorWaitLimit = 1 << 20;
+__device__ __forceinline__ bool halo_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  for (int i = 0; i < kMirrorWaitLimit; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(1000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void halo_arrive(uint64_t *bar) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a)
+               : "memory");
+}
+
+// ASYNC (one CTA per slab): instead of a CTA barrier per sub-cycle, each warp
+// waits only for the halo rows of its two neighbour warps -- an mbarrier per
+// (parity, warp) that lane 31 of the warp before and lane 0 of the warp after
+// arrive on once their rows are stored (release / acquire at CTA scope).
+// Warps then drift up to one sub-cycle apart; the two parities of the halo
+// rows cover that: a warp writes a parity's row again only after its
+// neighbour has published the next sub-cycle, i.e. has read the row.
+template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+__device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int s, const int e) {
+  constexpr int W = T / 32;
+  constexpr int H = MMAX / 2;  // cells per direction
+  constexpr int P = H / 2;     // pairs per direction
+  constexpr int M = MMAX;
+  static_assert(H % 4 == 0, "rows move as float4");
+  constexpr unsigned FULL = 0xffffffffu;
+  // [p][hi/lo][W+1][H] halo rows, then [p][H] the last node's own row, then
+  // (kind 7) the coefficients [P/2][NPT][T]
+  extern __shared__ __align__(16) float halo[];
+  auto hi = [&](int p, int w) { return halo + ((p * 2 + 0) * (W + 1) + w) * H; };
+  auto lo = [&](int p, int w) { return halo + ((p * 2 + 1) * (W + 1) + w) * H; };
+  float *self = halo + 2 * 2 * (W + 1) * H;
+  float4 *csm = reinterpret_cast<float4 *>(self + 2 * H);
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int crank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int N = r.N;
+  const int L = r.list_size[s];
+  if (L < 3) return;
+
+  const EnergyConsts ec = r.ec[e];
+  const double dtMin = 0.4 * r.ds_min[s] * ec.vgrid_i;
+  const double nst = floor(r.dt / dtMin + 1.0);
+  if (!(nst <= (double)r.max_subcycles)) {
+    if (crank == 0 && tid == 0) set_error(r, EPREM_GPU_ERR_SUBCYCLES, 1, s, -1, e, -1);
+    return;
+  }
+  const int nsteps = (int)nst;
+  const double dtProp = r.dt / (1.0 * nsteps);
+  if (crank == 0 && tid == 0) {
+    atomicMax(&r.status->max_stream, nsteps);
+    atomicAdd(&r.status->stream_cs, (unsigned long long)nsteps * L * M);
+  }
+  for (int j = tid; j < 2 * 2 * (W + 1) * H + 2 * H; j += T) halo[j] = 0.f;
+  __shared__ uint64_t s_bar[2][W];  // ASYNC: [parity][warp], arrivals of the neighbour warps
+  if (ASYNC && tid < 2 * W) {
+    const int w = tid % W, cnt = (w > 0) + (w < W - 1);
+    if (cnt)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(&s_bar[tid / W][w])),
+                   "r"(cnt)
+                   : "memory");
+  }  // made visible by the barriers before the sub-cycle loop
+
+  // list node of this thread's first slot: the slots start sh < NPT nodes
+  // before list node 0, so that node L-1 is the last node of its thread
+  const int sh = (NPT - L % NPT) % NPT;
+  const int i0 = NPT * (crank * T + tid) - sh;
+  const bool is_last = i0 + NPT - 1 == L - 1;
+  const size_t sN = (size_t)s * N;
+  // Lf pair p: cells H-1-2p, H-2-2p (mirror order); Rf pair p: cells H+2p, H+2p+1
+  float2 Lf[NPT][P], Rf[NPT][P];
+  float2 m2[NPT];
+  float phi[NPT], omlo[NPT], dith[NPT];
+  __shared__ float s_bcv[3];
+  __shared__ int s_red[W + 1];
+  const double vdt = ec.vgrid * dtProp;
+  const float4 *cf = r.scoef + ((size_t)s * r.E + e) * N;
+  int xr[NPT];
+  float sw[NPT];
+  int lg = kNoExp;
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    m2[q] = make_float2(0.f, 0.f);
+    phi[q] = omlo[q] = 0.f;
+    dith[q] = 0.5f;
+    xr[q] = 0;
+    sw[q] = 0.f;
+#pragma unroll
+    for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(0.f, 0.f);
+    const int il = i0 + q;
+    if (il >= 0 && il < L) {
+      const int k = r.list[sN + il];
+      const float4 c = cf[il];
+      const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(r.f) +
+                                                          ((sN + k) * r.E + e) * M);
+#pragma unroll
+      for (int t = 0; t < P / 2; ++t) {
+        const float4 a = fp[t], b = fp[H / 4 + t];
+        Lf[q][P - 1 - 2 * t] = make_float2(a.y, a.x);
+        Lf[q][P - 2 - 2 * t] = make_float2(a.w, a.z);
+        Rf[q][2 * t] = make_float2(b.x, b.y);
+        Rf[q][2 * t + 1] = make_float2(b.z, b.w);
+      }
+      float mx = 0.f;
+#pragma unroll
+      for (int t = 0; t < P; ++t)
+        mx = fmaxf(mx, fmaxf(fmaxf(Lf[q][t].x, Lf[q][t].y), fmaxf(Rf[q][t].x, Rf[q][t].y)));
+      xr[q] = r.fexp[(sN + k) * r.E + e];
+      sw[q] = c.w;
+      const int lr = ilogb_f(mx);
+      if (lr != kNoExp) lg = max(lg, lr - xr[q]);
+      const int ls = ilogb_f(c.w);
+      if ((r.check_seed || il < 3) && ls != kNoExp) lg = max(lg, ls - ec.seed_k);
+      m2[q] = make_float2(c.x, c.x);
+      phi[q] = c.y;
+      omlo[q] = c.z;
+    }
+  }
+  const int K = slab_exp<T>(lg, s_red, cluster, C);
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il >= 0 && il < L) {
+      const Pow2Pair pf = pow2_pair(K - xr[q]);
+      const float seedf = scale2(sw[q], pow2_pair(K - ec.seed_k));
+#pragma unroll
+      for (int t = 0; t < P; ++t) {
+        Lf[q][t] = make_float2(scale2(Lf[q][t].x, pf), scale2(Lf[q][t].y, pf));
+        Rf[q][t] = make_float2(scale2(Rf[q][t].x, pf), scale2(Rf[q][t].y, pf));
+      }
+      if (r.check_seed) {
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+          Lf[q][t].x = Lf[q][t].x < seedf ? seedf : Lf[q][t].x;
+          Lf[q][t].y = Lf[q][t].y < seedf ? seedf : Lf[q][t].y;
+          Rf[q][t].x = Rf[q][t].x < seedf ? seedf : Rf[q][t].x;
+          Rf[q][t].y = Rf[q][t].y < seedf ? seedf : Rf[q][t].y;
+        }
+      }
+      if (il < 3) s_bcv[il] = seedf;
+    }
+  }
+  // |del| of pair p of either half: v dtProp mugrid of cells H+2p, H+2p+1
+  const float ddel = (float)(vdt * r.dmu);
+  const float d0 = (float)(vdt * r.mugrid[H]);
+  if constexpr (CSM) {  // this thread's own coefficients: no barrier needed
+#pragma unroll
+    for (int t = 0; t < P / 2; ++t) {
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const float m = m2[q].x;
+        csm[(t * NPT + q) * T + tid] =
+            make_float4(m * (d0 + (float)(4 * t) * ddel), m * (d0 + (float)(4 * t + 1) * ddel),
+                        m * (d0 + (float)(4 * t + 2) * ddel), m * (d0 + (float)(4 * t + 3) * ddel));
+      }
+    }
+  }
+  const float inv_m = (float)(1.0 / M);
+  float *next_hi0 = (C > 1 && crank < C - 1) ? cluster.map_shared_rank(halo, crank + 1) : nullptr;
+  float *prev_loW = (C > 1 && crank > 0) ? cluster.map_shared_rank(halo, crank - 1) : nullptr;
+  if (C > 1)
+    cluster.sync();
+  else
+    __syncthreads();
+  if (crank == 0 && tid == 0) {  // list node 0's upwind neighbour for mu >= 0: the seed
+    const float b = s_bcv[0];
+    for (int j = 0; j < H; ++j) hi(0, 0)[j] = hi(1, 0)[j] = b;
+  }
+
+  const float2 neg1 = make_float2(-1.f, -1.f);
+  bool timed_out = false;
+  for (int step = 0; step < nsteps; ++step) {
+    const int ph = step & 1;
+    if (crank == 0 && warp == 0) {  // seed boundary: list nodes 0..2 and the slots in front
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const int il = i0 + q;
+        if (il < 3) {
+          const float b = s_bcv[il < 0 ? 0 : il];
+#pragma unroll
+          for (int p = 0; p < P; ++p) Lf[q][p] = Rf[q][p] = make_float2(b, b);
+        }
+      }
+    }
+    if (lane == 31) {  // last node's outward half for the next warp's first node
+      float4 *dst = reinterpret_cast<float4 *>(hi(ph, warp + 1));
+      float4 *rdst = (warp == W - 1 && next_hi0)
+                         ? reinterpret_cast<float4 *>(next_hi0 + ((ph * 2 + 0) * (W + 1)) * H)
+                         : nullptr;
+#pragma unroll
+      for (int t = 0; t < P / 2; ++t) {
+        const float4 v = make_float4(Rf[NPT - 1][2 * t].x, Rf[NPT - 1][2 * t].y,
+                                     Rf[NPT - 1][2 * t + 1].x, Rf[NPT - 1][2 * t + 1].y);
+        dst[t] = v;
+        if (rdst) rdst[t] = v;
+      }
+    }
+    if (lane == 0) {  // first node's inward half (mirror order) for the previous warp
+      float4 *dst = reinterpret_cast<float4 *>(lo(ph, warp));
+      float4 *rdst = (warp == 0 && prev_loW)
+                         ? reinterpret_cast<float4 *>(prev_loW + ((ph * 2 + 1) * (W + 1) + W) * H)
+                         : nullptr;
+#pragma unroll
+      for (int t = 0; t < P / 2; ++t) {
+        const float4 v = make_float4(Lf[0][2 * t].x, Lf[0][2 * t].y, Lf[0][2 * t + 1].x,
+                                     Lf[0][2 * t + 1].y);
+        dst[t] = v;
+        if (rdst) rdst[t] = v;
+      }
+    }
+    if (is_last) {  // the last list node is its own outer neighbour
+      float4 *dst = reinterpret_cast<float4 *>(self + ph * H);
+#pragma unroll
+      for (int t = 0; t < P / 2; ++t)
+        dst[t] = make_float4(Lf[NPT - 1][2 * t].x, Lf[NPT - 1][2 * t].y,
+                             Lf[NPT - 1][2 * t + 1].x, Lf[NPT - 1][2 * t + 1].y);
+    }
+    if constexpr (ASYNC) {
+      if (lane == 31 && warp + 1 < W) halo_arrive(&s_bar[ph][warp + 1]);
+      if (lane == 0 && warp > 0) halo_arrive(&s_bar[ph][warp - 1]);
+      if (W > 1 && !timed_out && !halo_wait(&s_bar[ph][warp], (uint32_t)(step >> 1) & 1u)) {
+        timed_out = true;  // reported once; later waits are skipped
+        if (lane == 0) set_error(r, EPREM_GPU_ERR_CUDA, 1, s, -1, e, -1);
+      }
+    } else if (C > 1) {
+      cluster.sync();
+    } else {
+      __syncthreads();
+    }
+    const float2 *my_hi = reinterpret_cast<const float2 *>(hi(ph, warp));
+    const float2 *lo_src =
+        reinterpret_cast<const float2 *>(is_last ? self + ph * H : lo(ph, warp + 1));
+    const bool take_lo = is_last || lane == 31;
+    float2 acc[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) acc[q] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      float2 c[NPT];
+      if constexpr (CSM) {
+#pragma unroll
+        for (int q = 0; q < NPT; ++q) {
+          const float2 *c2 = reinterpret_cast<const float2 *>(csm + ((p >> 1) * NPT + q) * T + tid);
+          c[q] = c2[p & 1];
+        }
+      } else {
+        float dd0 = d0 + (float)(2 * p) * ddel, dd1 = d0 + (float)(2 * p + 1) * ddel;
+        // opaque to loop-invariant code motion (see stream2_pairs_slab)
+        asm volatile("" : "+f"(dd0), "+f"(dd1));
+        const float2 del2 = make_float2(dd0, dd1);
+#pragma unroll
+        for (int q = 0; q < NPT; ++q) c[q] = __fmul2_rn(m2[q], del2);
+      }
+      float2 nbL, nbR;
+      nbL.x = __shfl_down_sync(FULL, Lf[0][p].x, 1);
+      nbL.y = __shfl_down_sync(FULL, Lf[0][p].y, 1);
+      if (take_lo) nbL = lo_src[p];
+      nbR.x = __shfl_up_sync(FULL, Rf[NPT - 1][p].x, 1);
+      nbR.y = __shfl_up_sync(FULL, Rf[NPT - 1][p].y, 1);
+      if (lane == 0) nbR = my_hi[p];
+      // mu < 0: upwind from the outer neighbour (list node + 1), old values
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const float2 cur = Lf[q][p];
+        const float2 right = (q + 1 < NPT) ? Lf[q + 1 < NPT ? q + 1 : q][p] : nbL;
+        const float2 nw = __ffma2_rn(c[q], __ffma2_rn(cur, neg1, right), cur);
+        Lf[q][p] = nw;
+        acc[q] = __fadd2_rn(acc[q], nw);
+      }
+      // mu >= 0: upwind from the inner neighbour (list node - 1), old values
+#pragma unroll
+      for (int q = NPT - 1; q >= 0; --q) {
+        const float2 cur = Rf[q][p];
+        const float2 left = (q > 0) ? Rf[q > 0 ? q - 1 : 0][p] : nbR;
+        const float2 nw = __ffma2_rn(c[q], __ffma2_rn(cur, neg1, left), cur);
+        Rf[q][p] = nw;
+        acc[q] = __fadd2_rn(acc[q], nw);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const float om = relax_weight(omlo[q], phi[q], dith[q]), em = 1.f - om;
+      const float iso = (inv_m * (acc[q].x + acc[q].y)) * om;
+      const float2 iso2 = make_float2(iso, iso), em2 = make_float2(em, em);
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        Lf[q][p] = __ffma2_rn(Lf[q][p], em2, iso2);
+        Rf[q][p] = __ffma2_rn(Rf[q][p], em2, iso2);
+      }
+    }
+  }
+
+#pragma unroll
+  for (int q = 0; q < NPT; ++q) {
+    const int il = i0 + q;
+    if (il >= 0 && il < L) {
+      const int k = r.list[sN + il];
+      int code = 0;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        float2 a = Lf[q][p], b = Rf[q][p];
+        if (bad_value(a.x, &code)) set_error(r, code, 1, s, k, e, H - 1 - 2 * p);
+        if (bad_value(a.y, &code)) set_error(r, code, 1, s, k, e, H - 2 - 2 * p);
+        if (bad_value(b.x, &code)) set_error(r, code, 1, s, k, e, H + 2 * p);
+        if (bad_value(b.y, &code)) set_error(r, code, 1, s, k, e, H + 2 * p + 1);
+        a.x = a.x < FLT_MIN ? FLT_MIN : a.x; a.y = a.y < FLT_MIN ? FLT_MIN : a.y;
+        b.x = b.x < FLT_MIN ? FLT_MIN : b.x; b.y = b.y < FLT_MIN ? FLT_MIN : b.y;
+        Lf[q][p] = a;
+        Rf[q][p] = b;
+      }
+      // node k and the thinned nodes that reference it (previous list node + 1 .. k)
+      const int kfirst = (il == 0) ? 0 : r.list[sN + il - 1] + 1;
+      for (int kk = kfirst; kk <= k; ++kk) {
+        r.fexp[(sN + kk) * r.E + e] = (short)K;
+        float4 *op = reinterpret_cast<float4 *>(reinterpret_cast<float *>(r.f) +
+                                                ((sN + kk) * r.E + e) * M);
+#pragma unroll
+        for (int t = 0; t < P / 2; ++t) {
+          op[t] = make_float4(Lf[q][P - 1 - 2 * t].y, Lf[q][P - 1 - 2 * t].x,
+                              Lf[q][P - 2 - 2 * t].y, Lf[q][P - 2 - 2 * t].x);
+          op[H / 4 + t] = make_float4(Rf[q][2 * t].x, Rf[q][2 * t].y, Rf[q][2 * t + 1].x,
+                                      Rf[q][2 * t + 1].y);
+        }
+      }
+    }
+  }
+  if (C > 1) cluster.sync();
+}
+
+template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+__global__ void __launch_bounds__(T, 1) k_stream2_mirror(RunView r, int) {
+  stream2_mirror_slab<MMAX, T, NPT, CSM, ASYNC>(r, blockIdx.y, r.E - 1 - (int)blockIdx.z);
+}
+
+template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+__global__ void __launch_bounds__(T, 1)
+    k_stream2_mirror_multi(const __grid_constant__ MultiRunViews mv, const int4 *items) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int4 it = items[blockIdx.x / cluster.num_blocks()];
+  stream2_mirror_slab<MMAX, T, NPT, CSM, ASYNC>(mv.v[it.x], it.y, it.z);
+}
+
 // Per (stream, energy, list node): mult = ds_i min(tau / dtProp, 1), the
 // relaxation factor exp(-dtProp / tau) and 1 - it, and the seed times
 // 2^seed_k (the energy's own power of two, so that seeds far below the float
@@ -828,23 +1217,39 @@ constexpr S2Shape kS2Shapes[] = {
 };
 }  // namespace
 
+// The shapes the mirrored kinds are built for (a subset of the shapes above).
+// Wider CTAs do not pay: the register file is split between the four warp
+// schedulers, so 9 to 12 warps cap a thread at 168 registers, and 3 or 4
+// list nodes of 40 cells then spill (288x4, 352x3, 384x3 measured with ptxas).
+#define EPREM_S2M_SHAPES(X) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3)
+
 // shape: 0 automatic, k >= 1 the k-th shape of the mu bin.  Automatic: the
 // bin's default when one CTA holds the stream, else the shape whose cluster
-// wastes the fewest list-node slots (ties to the earlier shape).
-int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, StreamPlan *plan) {
+// wastes the fewest list-node slots (ties to the earlier shape).  The
+// mirrored kinds need N + NPT - 1 slots (list node 0 may start up to NPT - 1
+// slots in) and take only the shapes they are built for.
+int plan_stream2(int N, int M, int m0, bool packed, bool filled, int mirror, bool bc, int shape,
+                 StreamPlan *plan) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
   // packed: odd halves take one padding cell (mmax/2 is even, so it fits)
   if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
+  if (mirror && !(packed && filled && bc)) return EPREM_GPU_ERR_ARG;
   const S2Shape *pick = nullptr;
   int k = 0;
   double best = 0.0;
   for (const S2Shape &sh : kS2Shapes) {
     if (sh.mmax != mmax) continue;
     ++k;
-    const int per = sh.T * sh.npt, cl = (N + per - 1) / per;
+    bool built = !mirror;
+#define EPREM_S2M_HAS(MM, TT, NN) built |= sh.mmax == MM && sh.T == TT && sh.npt == NN;
+    EPREM_S2M_SHAPES(EPREM_S2M_HAS)
+#undef EPREM_S2M_HAS
+    if (!built) continue;
+    const int per = sh.T * sh.npt, need = mirror ? N + sh.npt - 1 : N;
+    const int cl = (need + per - 1) / per;
     if (cl > 8) continue;
     if (shape) {
       if (k == shape) pick = &sh;
@@ -861,7 +1266,9 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, int shape, Stre
   plan->reg_coef = 2;  // marks the several-nodes-per-thread kernels
   plan->packed = packed ? 1 : 0;
   plan->filled = filled ? 1 : 0;
-  plan->cluster = (N + pick->T * pick->npt - 1) / (pick->T * pick->npt);
+  plan->mirror = mirror;
+  const int per = pick->T * pick->npt;
+  plan->cluster = ((mirror ? N + pick->npt - 1 : N) + per - 1) / per;
   return 0;
 }
 
@@ -874,6 +1281,28 @@ int stream2_shape_count(int M) {
   return k;
 }
 
+static cudaError_t launch_cluster(const void *kern, dim3 grid, int T, int cluster, size_t dyn,
+                                  cudaStream_t st, void **args) {
+  if (dyn > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(T, 1, 1);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, kern, args);
+}
+
 template <int MMAX, int T, int NPT>
 static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int m0,
                                     cudaStream_t st) {
@@ -881,19 +1310,51 @@ static cudaError_t launch_stream2_t(const RunView &r, const StreamPlan &pl, int 
   void (*kern)(RunView, int) = !pl.packed  ? k_stream2<MMAX, T, NPT>
                                : pl.filled ? k_stream2_pairs<MMAX, T, NPT, true>
                                            : k_stream2_pairs<MMAX, T, NPT, false>;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(pl.cluster, r.S, r.E);
-  cfg.blockDim = dim3(T, 1, 1);
-  cfg.dynamicSmemBytes = dyn;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = pl.cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, r, m0);
+  RunView rv = r;
+  void *args[] = {&rv, &m0};
+  return launch_cluster((const void *)kern, dim3(pl.cluster, r.S, r.E), T, pl.cluster, dyn, st,
+                        args);
+}
+
+// The mirrored kernel of a plan: kind 7 with its coefficients in shared
+// memory and, on one CTA per slab, the neighbour-warp halo hand-over; kind 6
+// with the coefficients formed on the loop and a barrier per sub-cycle.
+template <int MMAX, int T, int NPT, typename Args>
+static cudaError_t launch_mirror_kind(const StreamPlan &pl, dim3 grid, Args args, bool multi,
+                                      cudaStream_t st) {
+  const void *kern;
+  size_t dyn;
+  if (pl.mirror == 2 && pl.cluster == 1) {
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, true>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, true>;
+    dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, true>();
+  } else if (pl.mirror == 2) {
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, false>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, false>;
+    dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, true>();
+  } else {
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, false, false>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, false, false>;
+    dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, false>();
+  }
+  return launch_cluster(kern, grid, T, pl.cluster, dyn, st, args);
+}
+
+template <int MMAX, int T, int NPT>
+static cudaError_t launch_stream2_mirror_t(const RunView &r, const StreamPlan &pl,
+                                           cudaStream_t st) {
+  RunView rv = r;
+  int unused = 0;
+  void *args[] = {&rv, &unused};
+  return launch_mirror_kind<MMAX, T, NPT>(pl, dim3(pl.cluster, r.S, r.E), args, false, st);
+}
+
+template <int MMAX, int T, int NPT>
+static cudaError_t launch_stream2_mirror_multi_t(const StreamPlan &pl, const MultiRunViews &mv,
+                                                 const int4 *items, int n_items,
+                                                 cudaStream_t st) {
+  void *args[] = {const_cast<MultiRunViews *>(&mv), &items};
+  return launch_mirror_kind<MMAX, T, NPT>(pl, dim3(pl.cluster * n_items, 1, 1), args, true, st);
 }
 
 template <int MMAX, int T, int NPT>
@@ -903,31 +1364,30 @@ static cudaError_t launch_stream2_multi_t(const StreamPlan &pl, const MultiRunVi
   void (*kern)(const MultiRunViews, const int4 *) =
       pl.filled ? k_stream2_pairs_multi<MMAX, T, NPT, true>
                 : k_stream2_pairs_multi<MMAX, T, NPT, false>;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(pl.cluster * n_items, 1, 1);
-  cfg.blockDim = dim3(T, 1, 1);
-  cfg.dynamicSmemBytes = dyn;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = pl.cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, mv, items);
+  void *args[] = {const_cast<MultiRunViews *>(&mv), &items};
+  return launch_cluster((const void *)kern, dim3(pl.cluster * n_items, 1, 1), T, pl.cluster, dyn,
+                        st, args);
 }
 
 int launch_stream2_multi(const StreamPlan &pl, const MultiRunViews &mv, const int4 *items,
                          int n_items, cudaStream_t st, uint64_t *launches) {
   if (!pl.packed || n_items <= 0) return EPREM_GPU_ERR_ARG;
   cudaError_t err = cudaErrorInvalidValue;
+  if (pl.mirror) {
+#define EPREM_S2M_MCASE(MM, TT, NN)                                                \
+  if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)                           \
+    err = launch_stream2_mirror_multi_t<MM, TT, NN>(pl, mv, items, n_items, st); \
+  else
+    EPREM_S2M_SHAPES(EPREM_S2M_MCASE) {}
+#undef EPREM_S2M_MCASE
+  } else {
 #define EPREM_S2_MCASE(MM, TT, NN)                                          \
   if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)                    \
     err = launch_stream2_multi_t<MM, TT, NN>(pl, mv, items, n_items, st); \
   else
-  EPREM_S2_SHAPES(EPREM_S2_MCASE) {}
+    EPREM_S2_SHAPES(EPREM_S2_MCASE) {}
 #undef EPREM_S2_MCASE
+  }
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
@@ -935,12 +1395,22 @@ int launch_stream2_multi(const StreamPlan &pl, const MultiRunViews &mv, const in
 int launch_stream2(const RunView &r, const StreamPlan &pl, int m0, cudaStream_t st,
                    uint64_t *launches) {
   cudaError_t err = cudaErrorInvalidValue;
+  if (pl.mirror) {
+    if (!r.use_bc) return EPREM_GPU_ERR_ARG;  // the mirrored kinds need the seed boundary
+#define EPREM_S2M_CASE(MM, TT, NN)                                \
+  if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)          \
+    err = launch_stream2_mirror_t<MM, TT, NN>(r, pl, st);         \
+  else
+    EPREM_S2M_SHAPES(EPREM_S2M_CASE) {}
+#undef EPREM_S2M_CASE
+  } else {
 #define EPREM_S2_CASE(MM, TT, NN)                                   \
   if (pl.mmax == MM && pl.threads == TT && pl.npt == NN)            \
     err = launch_stream2_t<MM, TT, NN>(r, pl, m0, st);             \
   else
-  EPREM_S2_SHAPES(EPREM_S2_CASE) {}
+    EPREM_S2_SHAPES(EPREM_S2_CASE) {}
 #undef EPREM_S2_CASE
+  }
   *launches += 1;
   return err == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }

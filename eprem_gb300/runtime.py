@@ -70,6 +70,7 @@ EXPORTS = [
     ("eprem_gpu_init_seed_population", C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
     ("eprem_gpu_autotune", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("eprem_gpu_set_stream_variant", C.c_int, [C.c_void_p, C.c_int]),
+    ("eprem_gpu_stream_kernel", C.c_char_p, [C.c_void_p]),
     ("eprem_gpu_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int,
                                             C.POINTER(C.c_void_p)]),
     ("eprem_gpu_ensemble_destroy", C.c_int, [C.c_void_p]),
@@ -367,6 +368,11 @@ class EpremRun:
         v = C.c_int()
         self._check(self.lib.eprem_gpu_autotune(self.handle, C.byref(v)))
         return v.value
+
+    @property
+    def stream_kernel(self) -> str:
+        """The streaming kernel this run launches, with its shape."""
+        return self.lib.eprem_gpu_stream_kernel(self.handle).decode()
 
     def set_stream_variant(self, variant: int):
         self._check(self.lib.eprem_gpu_set_stream_variant(self.handle, int(variant)))

@@ -127,11 +127,17 @@ typedef struct {
   int32_t stream_variant;           /* streaming-kernel shape in the FP32 form
                                        (tuning; results agree to rounding):
                                        kind + 8 * shape.  kind 0 automatic
-                                       (the first of 5, 4, 3 that fits);
+                                       (the first of 7, 5, 4, 3 that fits);
                                        3 several nodes per thread; 4 as 3
                                        with packed fp32x2 arithmetic; 5 as 4
                                        with compile-time cell guards (M = 8,
-                                       16, ..., 64 and m0 = M/2).  shape 0
+                                       16, ..., 64 and m0 = M/2); 6 and 7 as
+                                       5 with the mu < 0 half in mirror
+                                       order, one upwind coefficient per two
+                                       cells (M = 40 and the seed boundary
+                                       on; 7 with the coefficients in shared
+                                       memory and, on one CTA per stream,
+                                       no CTA barrier per sub-cycle).  shape 0
                                        automatic, k >= 1 the k-th CTA shape
                                        (threads, nodes per thread, cluster)
                                        of the run's mu bin.  A shape whose
@@ -494,7 +500,7 @@ int eprem_gpu_alu_peak(int precision, double *tflops);
 int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double perturbation);
 
 /* Time the streaming-kernel kinds and CTA shapes that fit this run (FP32
- * form: every kind 3, 4, 5 with every shape of its mu bin, encoded as
+ * form: every kind 3 to 7 with every shape of its mu bin, encoded as
  * eprem_params_t.stream_variant) on a scratch copy of its first 96 streams
  * and keep the fastest; *chosen_variant receives it.  The run's f
  * and statistics are not touched.  The FP64 form has one shape.  Allocates
@@ -502,6 +508,11 @@ int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double per
 int eprem_gpu_autotune(eprem_gpu_run *run, int *chosen_variant);
 /* Force a streaming-kernel shape (EPREM_GPU_ERR_ARG if it does not fit). */
 int eprem_gpu_set_stream_variant(eprem_gpu_run *run, int variant);
+/* The streaming kernel this run launches, with its shape, e.g.
+ * "k_stream2_mirror<40,256,4> cluster 1" (a string owned by the run, valid
+ * until its next eprem_gpu_set_stream_variant / autotune / destroy).  No
+ * counterpart in the reference (one CPU loop there). */
+const char *eprem_gpu_stream_kernel(eprem_gpu_run *run);
 
 /* A set of independent runs (different sizes and parameters allowed, all on
  * the current device, analytic background) stepped together.  The first

@@ -139,7 +139,7 @@ def test_autotune_keeps_a_correct_shape(oracle_lib):
     run.upload_f(f)
     run.upload_nodes(nodes)
     v = run.autotune()
-    assert v % 8 in (3, 4, 5) and 1 <= v // 8  # a kind and a CTA shape
+    assert v % 8 in (3, 4, 5, 6, 7) and 1 <= v // 8  # a kind and a CTA shape
     # the scratch copy leaves the state alone
     np.testing.assert_array_equal(run.download_f(), f.astype(np.float32).astype(np.float64))
     run.update_energetic_particles(0.0)

@@ -84,6 +84,53 @@ def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
         assert err <= 1e-4, f"variant {v} vs variant 3: {err:.3e}"
 
 
+@pytest.mark.parametrize("nodes,thin,seed_check", [(48, 0, 1), (401, 0, 1), (402, 5, 0),
+                                                    (403, 0, 0), (1100, 0, 1), (1500, 7, 1)])
+def test_fp32_mirrored_kinds_agree(oracle_lib, nodes, thin, seed_check):
+    """The mirrored streaming kinds (the mu < 0 half in mirror order, one
+    upwind coefficient per two cells; 7 with the coefficients in shared memory
+    and, on one CTA, the neighbour-warp halo hand-over) against the packed
+    kind and the FP64 oracle.  The list lengths cover every position of the
+    last list node modulo the nodes per thread (the slots start up to three
+    nodes before list node 0), thinned streams, clusters of two and three
+    CTAs, the seed check on and off; both stream ends must keep the values
+    the reference keeps."""
+    w = W.custom(1, 1, nodes, 3, 40, num_ep_steps=2, use_adiabatic_focus=0,
+                 use_adiabatic_change=0, check_seed_population=seed_check)
+    w.cluster_inner = thin
+    d, g, f, nodes_arr = primed_state(w, oracle_lib)
+    f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes_arr)
+    outs = {}
+    for variant in (5, 6, 7):
+        w.params.stream_variant = variant
+        run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+        run.upload_f(f)
+        run.upload_nodes(nodes_arr)
+        run.update_energetic_particles(0.0)
+        outs[variant] = run.download_f()
+        run.close()
+    w.params.stream_variant = 0
+    for v, o in outs.items():
+        err = np.max(np.abs(o - f_ref) / f_ref)
+        assert err <= 1e-3, f"variant {v} vs FP64 oracle: {err:.3e}"
+    for v in (6, 7):
+        err = np.max(np.abs(outs[v] - outs[5]) / outs[5])
+        assert err <= 1e-4, f"variant {v} vs variant 5: {err:.3e}"
+
+
+def test_fp32_mirrored_kinds_need_the_seed_boundary():
+    """Without the seed boundary list node 0 has no fixed upwind value, so the
+    mirrored kinds are refused and the automatic choice is the packed kind."""
+    w = W.custom(1, 1, 100, 3, 40, use_ep_boundary=0)
+    g = W.build_grids(w)
+    for variant in (6, 7):
+        w.params.stream_variant = variant
+        with pytest.raises(RuntimeError):
+            EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
+    w.params.stream_variant = 0
+    EpremRun(w.dims(abi.EPREM_FP32), w.params, g).close()
+
+
 def test_fp32_variants_of_the_fp64_kernel_refused():
     """Variants 1 and 2 name the FP64 streaming kernel's shape: an FP32 run
     refuses them instead of running another kernel."""
