@@ -451,8 +451,10 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   }
 }
 
+// Row lengths the focusing kernel is built for (20: the CPU-runnable case's
+// mu count, with compile-time cell guards).
 static int bucket(int n) {
-  for (int b : {8, 16, 24, 32, 40, 48, 56, 64})
+  for (int b : {8, 16, 20, 24, 32, 40, 48, 56, 64})
     if (n <= b) return b;
   return 0;
 }
@@ -501,6 +503,7 @@ static void launch_change(const RunView &r, cudaStream_t st) {
   switch (p) {                         \
     case 8: F<8>(__VA_ARGS__); break;   \
     case 16: F<16>(__VA_ARGS__); break; \
+    case 20: F<20>(__VA_ARGS__); break; \
     case 24: F<24>(__VA_ARGS__); break; \
     case 32: F<32>(__VA_ARGS__); break; \
     case 40: F<40>(__VA_ARGS__); break; \

@@ -759,12 +759,35 @@ __global__ void __launch_bounds__(T, 1)
 template <int MMAX, int T, int NPT, bool CSM>
 constexpr size_t stream2_mirror_smem_bytes() {
   return stream2_smem_bytes<MMAX, T>() + sizeof(float) * 2 * (MMAX / 2) +
-         (CSM ? sizeof(float4) * (MMAX / 8) * NPT * T : 0);
+         (CSM ? sizeof(float2) * (MMAX / 4) * NPT * T : 0);
+}
+
+// A half row of P pairs to shared memory (and to a second, possibly remote,
+// copy): as float4 when V4, else as float2.
+template <int P, bool V4>
+__device__ __forceinline__ void put_half(const float2 (&h)[P], float *dst, float *dst2) {
+  if constexpr (V4) {
+#pragma unroll
+    for (int t = 0; t < P / 2; ++t) {
+      const float4 v = make_float4(h[2 * t].x, h[2 * t].y, h[2 * t + 1].x, h[2 * t + 1].y);
+      reinterpret_cast<float4 *>(dst)[t] = v;
+      if (dst2) reinterpret_cast<float4 *>(dst2)[t] = v;
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+      reinterpret_cast<float2 *>(dst)[t] = h[t];
+      if (dst2) reinterpret_cast<float2 *>(dst2)[t] = h[t];
+    }
+  }
 }
 
 // Bounded wait on a CTA mbarrier phase: at most kMirrorWaitLimit try_waits,
 // each of which suspends the warp until the phase completes or about a
-// microsecond has passed; false when the limit ran out.
+// microsecond has passed; false when the limit ran out.  (Publishing the
+// warp-edge rows right after relaxing the edge nodes, before the others, and
+// a few test_wait polls before suspending measured slower: 8.00 against
+// 7.75 ms per 96-stream launch, the reordering spilling registers.)
 constexpr int kMirrorWaitLimit = 1 << 20;
 __device__ __forceinline__ bool halo_wait(uint64_t *bar, uint32_t parity) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
@@ -785,21 +808,26 @@ __device__ __forceinline__ void halo_arrive(uint64_t *bar) {
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a)
                : "memory");
 }
-
-// ASYNC (one CTA per slab): instead of a CTA barrier per sub-cycle, each warp
-// waits only for the halo rows of its two neighbour warps -- an mbarrier per
-// (parity, warp) that lane 31 of the warp before and lane 0 of the warp after
-// arrive on once their rows are stored (release / acquire at CTA scope).
+// ASYNC (1, one CTA per slab; 0: a CTA or cluster barrier per sub-cycle):
+// instead of a CTA barrier per sub-cycle, each warp waits only for the halo
+// rows of its two neighbour warps -- an mbarrier per (parity, warp) that lane
+// 31 of the warp before and lane 0 of the warp after arrive on once their
+// rows are stored (release / acquire at CTA scope).  Across the CTAs of a
+// cluster the same hand-over (remote arrivals at cluster scope) measured no
+// faster than the cluster barrier: 15.02 against 14.88 ms per 96-stream
+// launch at N = 1500, whose 128-thread CTAs share an SM two by two, so one
+// CTA's barrier wait overlaps the other's work.
 // Warps then drift up to one sub-cycle apart; the two parities of the halo
 // rows cover that: a warp writes a parity's row again only after its
 // neighbour has published the next sub-cycle, i.e. has read the row.
-template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+template <int MMAX, int T, int NPT, bool CSM, int ASYNC>
 __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int s, const int e) {
   constexpr int W = T / 32;
   constexpr int H = MMAX / 2;  // cells per direction
   constexpr int P = H / 2;     // pairs per direction
   constexpr int M = MMAX;
-  static_assert(H % 4 == 0, "rows move as float4");
+  static_assert(H % 2 == 0, "rows move as float2 pairs");
+  constexpr bool V4 = H % 4 == 0;  // rows, halo rows and coefficients as float4
   constexpr unsigned FULL = 0xffffffffu;
   // [p][hi/lo][W+1][H] halo rows, then [p][H] the last node's own row, then
   // (kind 7) the coefficients [P/2][NPT][T]
@@ -807,7 +835,7 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
   auto hi = [&](int p, int w) { return halo + ((p * 2 + 0) * (W + 1) + w) * H; };
   auto lo = [&](int p, int w) { return halo + ((p * 2 + 1) * (W + 1) + w) * H; };
   float *self = halo + 2 * 2 * (W + 1) * H;
-  float4 *csm = reinterpret_cast<float4 *>(self + 2 * H);
+  float *csm = self + 2 * H;  // V4: float4 [P/2][NPT][T], else float2 [P][NPT][T]
 
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
@@ -832,7 +860,7 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
   }
   for (int j = tid; j < 2 * 2 * (W + 1) * H + 2 * H; j += T) halo[j] = 0.f;
   __shared__ uint64_t s_bar[2][W];  // ASYNC: [parity][warp], arrivals of the neighbour warps
-  if (ASYNC && tid < 2 * W) {
+  if (ASYNC && tid < 2 * W) {  // writers: the warps before and after
     const int w = tid % W, cnt = (w > 0) + (w < W - 1);
     if (cnt)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(
@@ -871,15 +899,25 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
     if (il >= 0 && il < L) {
       const int k = r.list[sN + il];
       const float4 c = cf[il];
-      const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(r.f) +
-                                                          ((sN + k) * r.E + e) * M);
+      const float *row = reinterpret_cast<const float *>(r.f) + ((sN + k) * r.E + e) * M;
+      if constexpr (V4) {
+        const float4 *fp = reinterpret_cast<const float4 *>(row);
 #pragma unroll
-      for (int t = 0; t < P / 2; ++t) {
-        const float4 a = fp[t], b = fp[H / 4 + t];
-        Lf[q][P - 1 - 2 * t] = make_float2(a.y, a.x);
-        Lf[q][P - 2 - 2 * t] = make_float2(a.w, a.z);
-        Rf[q][2 * t] = make_float2(b.x, b.y);
-        Rf[q][2 * t + 1] = make_float2(b.z, b.w);
+        for (int t = 0; t < P / 2; ++t) {
+          const float4 a = fp[t], b = fp[H / 4 + t];
+          Lf[q][P - 1 - 2 * t] = make_float2(a.y, a.x);
+          Lf[q][P - 2 - 2 * t] = make_float2(a.w, a.z);
+          Rf[q][2 * t] = make_float2(b.x, b.y);
+          Rf[q][2 * t + 1] = make_float2(b.z, b.w);
+        }
+      } else {
+        const float2 *fp = reinterpret_cast<const float2 *>(row);
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+          const float2 a = fp[t];
+          Lf[q][P - 1 - t] = make_float2(a.y, a.x);
+          Rf[q][t] = fp[H / 2 + t];
+        }
       }
       float mx = 0.f;
 #pragma unroll
@@ -925,13 +963,17 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
   const float d0 = (float)(vdt * r.mugrid[H]);
   if constexpr (CSM) {  // this thread's own coefficients: no barrier needed
 #pragma unroll
-    for (int t = 0; t < P / 2; ++t) {
+    for (int p = 0; p < P; ++p) {
 #pragma unroll
       for (int q = 0; q < NPT; ++q) {
         const float m = m2[q].x;
-        csm[(t * NPT + q) * T + tid] =
-            make_float4(m * (d0 + (float)(4 * t) * ddel), m * (d0 + (float)(4 * t + 1) * ddel),
-                        m * (d0 + (float)(4 * t + 2) * ddel), m * (d0 + (float)(4 * t + 3) * ddel));
+        const float2 c = make_float2(m * (d0 + (float)(2 * p) * ddel),
+                                     m * (d0 + (float)(2 * p + 1) * ddel));
+        if constexpr (V4)
+          reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(csm) +
+                                     ((p >> 1) * NPT + q) * T + tid)[p & 1] = c;
+        else
+          reinterpret_cast<float2 *>(csm)[(p * NPT + q) * T + tid] = c;
       }
     }
   }
@@ -949,6 +991,25 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
 
   const float2 neg1 = make_float2(-1.f, -1.f);
   bool timed_out = false;
+  // the warp-edge rows of sub-cycle parity p: lane 31's outward half for the
+  // next warp's first node, lane 0's inward half (mirror order) for the
+  // previous warp's last node; with ASYNC, each followed by the arrival its
+  // reader waits on (the seed boundary is set before: list nodes 0..2 sit in
+  // threads 0 and 1)
+  auto publish_edges = [&](int p) {
+    if (lane == 31) {
+      put_half<P, V4>(Rf[NPT - 1], hi(p, warp + 1),
+                      (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H
+                                                  : nullptr);
+      if (ASYNC && warp + 1 < W) halo_arrive(&s_bar[p][warp + 1]);
+    }
+    if (lane == 0) {
+      put_half<P, V4>(Lf[0], lo(p, warp),
+                      (warp == 0 && prev_loW) ? prev_loW + ((p * 2 + 1) * (W + 1) + W) * H
+                                              : nullptr);
+      if (ASYNC && warp > 0) halo_arrive(&s_bar[p][warp - 1]);
+    }
+  };
   for (int step = 0; step < nsteps; ++step) {
     const int ph = step & 1;
     if (crank == 0 && warp == 0) {  // seed boundary: list nodes 0..2 and the slots in front
@@ -962,42 +1023,10 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
         }
       }
     }
-    if (lane == 31) {  // last node's outward half for the next warp's first node
-      float4 *dst = reinterpret_cast<float4 *>(hi(ph, warp + 1));
-      float4 *rdst = (warp == W - 1 && next_hi0)
-                         ? reinterpret_cast<float4 *>(next_hi0 + ((ph * 2 + 0) * (W + 1)) * H)
-                         : nullptr;
-#pragma unroll
-      for (int t = 0; t < P / 2; ++t) {
-        const float4 v = make_float4(Rf[NPT - 1][2 * t].x, Rf[NPT - 1][2 * t].y,
-                                     Rf[NPT - 1][2 * t + 1].x, Rf[NPT - 1][2 * t + 1].y);
-        dst[t] = v;
-        if (rdst) rdst[t] = v;
-      }
-    }
-    if (lane == 0) {  // first node's inward half (mirror order) for the previous warp
-      float4 *dst = reinterpret_cast<float4 *>(lo(ph, warp));
-      float4 *rdst = (warp == 0 && prev_loW)
-                         ? reinterpret_cast<float4 *>(prev_loW + ((ph * 2 + 1) * (W + 1) + W) * H)
-                         : nullptr;
-#pragma unroll
-      for (int t = 0; t < P / 2; ++t) {
-        const float4 v = make_float4(Lf[0][2 * t].x, Lf[0][2 * t].y, Lf[0][2 * t + 1].x,
-                                     Lf[0][2 * t + 1].y);
-        dst[t] = v;
-        if (rdst) rdst[t] = v;
-      }
-    }
-    if (is_last) {  // the last list node is its own outer neighbour
-      float4 *dst = reinterpret_cast<float4 *>(self + ph * H);
-#pragma unroll
-      for (int t = 0; t < P / 2; ++t)
-        dst[t] = make_float4(Lf[NPT - 1][2 * t].x, Lf[NPT - 1][2 * t].y,
-                             Lf[NPT - 1][2 * t + 1].x, Lf[NPT - 1][2 * t + 1].y);
-    }
+    publish_edges(ph);
+    if (is_last)  // the last list node is its own outer neighbour
+      put_half<P, V4>(Lf[NPT - 1], self + ph * H, nullptr);
     if constexpr (ASYNC) {
-      if (lane == 31 && warp + 1 < W) halo_arrive(&s_bar[ph][warp + 1]);
-      if (lane == 0 && warp > 0) halo_arrive(&s_bar[ph][warp - 1]);
       if (W > 1 && !timed_out && !halo_wait(&s_bar[ph][warp], (uint32_t)(step >> 1) & 1u)) {
         timed_out = true;  // reported once; later waits are skipped
         if (lane == 0) set_error(r, EPREM_GPU_ERR_CUDA, 1, s, -1, e, -1);
@@ -1020,8 +1049,11 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
       if constexpr (CSM) {
 #pragma unroll
         for (int q = 0; q < NPT; ++q) {
-          const float2 *c2 = reinterpret_cast<const float2 *>(csm + ((p >> 1) * NPT + q) * T + tid);
-          c[q] = c2[p & 1];
+          if constexpr (V4)
+            c[q] = reinterpret_cast<const float2 *>(reinterpret_cast<const float4 *>(csm) +
+                                                    ((p >> 1) * NPT + q) * T + tid)[p & 1];
+          else
+            c[q] = reinterpret_cast<const float2 *>(csm)[(p * NPT + q) * T + tid];
         }
       } else {
         float dd0 = d0 + (float)(2 * p) * ddel, dd1 = d0 + (float)(2 * p + 1) * ddel;
@@ -1092,14 +1124,23 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
       const int kfirst = (il == 0) ? 0 : r.list[sN + il - 1] + 1;
       for (int kk = kfirst; kk <= k; ++kk) {
         r.fexp[(sN + kk) * r.E + e] = (short)K;
-        float4 *op = reinterpret_cast<float4 *>(reinterpret_cast<float *>(r.f) +
-                                                ((sN + kk) * r.E + e) * M);
+        float *row = reinterpret_cast<float *>(r.f) + ((sN + kk) * r.E + e) * M;
+        if constexpr (V4) {
+          float4 *op = reinterpret_cast<float4 *>(row);
 #pragma unroll
-        for (int t = 0; t < P / 2; ++t) {
-          op[t] = make_float4(Lf[q][P - 1 - 2 * t].y, Lf[q][P - 1 - 2 * t].x,
-                              Lf[q][P - 2 - 2 * t].y, Lf[q][P - 2 - 2 * t].x);
-          op[H / 4 + t] = make_float4(Rf[q][2 * t].x, Rf[q][2 * t].y, Rf[q][2 * t + 1].x,
-                                      Rf[q][2 * t + 1].y);
+          for (int t = 0; t < P / 2; ++t) {
+            op[t] = make_float4(Lf[q][P - 1 - 2 * t].y, Lf[q][P - 1 - 2 * t].x,
+                                Lf[q][P - 2 - 2 * t].y, Lf[q][P - 2 - 2 * t].x);
+            op[H / 4 + t] = make_float4(Rf[q][2 * t].x, Rf[q][2 * t].y, Rf[q][2 * t + 1].x,
+                                        Rf[q][2 * t + 1].y);
+          }
+        } else {
+          float2 *op = reinterpret_cast<float2 *>(row);
+#pragma unroll
+          for (int t = 0; t < P; ++t) {
+            op[t] = make_float2(Lf[q][P - 1 - t].y, Lf[q][P - 1 - t].x);
+            op[H / 2 + t] = Rf[q][t];
+          }
         }
       }
     }
@@ -1107,12 +1148,12 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
   if (C > 1) cluster.sync();
 }
 
-template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+template <int MMAX, int T, int NPT, bool CSM, int ASYNC>
 __global__ void __launch_bounds__(T, 1) k_stream2_mirror(RunView r, int) {
   stream2_mirror_slab<MMAX, T, NPT, CSM, ASYNC>(r, blockIdx.y, r.E - 1 - (int)blockIdx.z);
 }
 
-template <int MMAX, int T, int NPT, bool CSM, bool ASYNC>
+template <int MMAX, int T, int NPT, bool CSM, int ASYNC>
 __global__ void __launch_bounds__(T, 1)
     k_stream2_mirror_multi(const __grid_constant__ MultiRunViews mv, const int4 *items) {
   cg::cluster_group cluster = cg::this_cluster();
@@ -1210,18 +1251,22 @@ namespace {
 struct S2Shape {
   int mmax, T, npt;
 };
+// The mirrored kinds' own bin: M = 20 exactly (the CPU-runnable case's size,
+// which the packed kinds run in the 24 bin with run-time guards), with shapes
+// for short streams: 64 x 7 holds a 400-node stream in two warps.
+#define EPREM_S2M20_SHAPES(X) X(20, 64, 7) X(20, 128, 8) X(20, 256, 4)
 constexpr S2Shape kS2Shapes[] = {
 #define EPREM_S2_ROW(MM, TT, NN) {MM, TT, NN},
-    EPREM_S2_SHAPES(EPREM_S2_ROW)
+    EPREM_S2_SHAPES(EPREM_S2_ROW) EPREM_S2M20_SHAPES(EPREM_S2_ROW)
 #undef EPREM_S2_ROW
 };
 }  // namespace
 
-// The shapes the mirrored kinds are built for (a subset of the shapes above).
-// Wider CTAs do not pay: the register file is split between the four warp
-// schedulers, so 9 to 12 warps cap a thread at 168 registers, and 3 or 4
+// The shapes the mirrored kinds are built for: three of the 40 bin and the 20
+// bin.  Wider CTAs do not pay: the register file is split between the four
+// warp schedulers, so 9 to 12 warps cap a thread at 168 registers, and 3 or 4
 // list nodes of 40 cells then spill (288x4, 352x3, 384x3 measured with ptxas).
-#define EPREM_S2M_SHAPES(X) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3)
+#define EPREM_S2M_SHAPES(X) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3) EPREM_S2M20_SHAPES(X)
 
 // shape: 0 automatic, k >= 1 the k-th shape of the mu bin.  Automatic: the
 // bin's default when one CTA holds the stream, else the shape whose cluster
@@ -1231,12 +1276,16 @@ constexpr S2Shape kS2Shapes[] = {
 int plan_stream2(int N, int M, int m0, bool packed, bool filled, int mirror, bool bc, int shape,
                  StreamPlan *plan) {
   int mmax = 0;
+  if (mirror) {  // their own bins: M exactly, halves of equal length
+    if (!(packed && filled && bc) || !(M == 20 || M == 40) || 2 * m0 != M)
+      return EPREM_GPU_ERR_ARG;
+    mmax = M;
+  }
   for (int b : {8, 16, 24, 32, 40, 48, 64})
-    if (M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
+    if (!mmax && M <= b && m0 <= b / 2 && M - m0 <= b / 2) { mmax = b; break; }
   if (!mmax) return EPREM_GPU_ERR_ARG;
   // packed: odd halves take one padding cell (mmax/2 is even, so it fits)
   if (filled && !(M == mmax && 2 * m0 == mmax)) return EPREM_GPU_ERR_ARG;
-  if (mirror && !(packed && filled && bc)) return EPREM_GPU_ERR_ARG;
   const S2Shape *pick = nullptr;
   int k = 0;
   double best = 0.0;
@@ -1272,13 +1321,18 @@ int plan_stream2(int N, int M, int m0, bool packed, bool filled, int mirror, boo
   return 0;
 }
 
+// Shapes of M's bin: the larger count of the packed kinds' bin and, for M = 20,
+// the mirrored kinds' own bin.
 int stream2_shape_count(int M) {
   int mmax = 0;
   for (int b : {8, 16, 24, 32, 40, 48, 64})
     if (M <= b) { mmax = b; break; }
-  int k = 0;
-  for (const S2Shape &sh : kS2Shapes) k += sh.mmax == mmax;
-  return k;
+  int k = 0, k20 = 0;
+  for (const S2Shape &sh : kS2Shapes) {
+    k += sh.mmax == mmax;
+    k20 += M == 20 && sh.mmax == 20;
+  }
+  return k > k20 ? k : k20;
 }
 
 static cudaError_t launch_cluster(const void *kern, dim3 grid, int T, int cluster, size_t dyn,
@@ -1325,16 +1379,16 @@ static cudaError_t launch_mirror_kind(const StreamPlan &pl, dim3 grid, Args args
   const void *kern;
   size_t dyn;
   if (pl.mirror == 2 && pl.cluster == 1) {
-    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, true>
-                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, true>;
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, 1>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, 1>;
     dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, true>();
   } else if (pl.mirror == 2) {
-    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, false>
-                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, false>;
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, true, 0>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, true, 0>;
     dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, true>();
   } else {
-    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, false, false>
-                 : (const void *)k_stream2_mirror<MMAX, T, NPT, false, false>;
+    kern = multi ? (const void *)k_stream2_mirror_multi<MMAX, T, NPT, false, 0>
+                 : (const void *)k_stream2_mirror<MMAX, T, NPT, false, 0>;
     dyn = stream2_mirror_smem_bytes<MMAX, T, NPT, false>();
   }
   return launch_cluster(kern, grid, T, pl.cluster, dyn, st, args);

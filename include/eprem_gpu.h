@@ -134,8 +134,8 @@ typedef struct {
                                        16, ..., 64 and m0 = M/2); 6 and 7 as
                                        5 with the mu < 0 half in mirror
                                        order, one upwind coefficient per two
-                                       cells (M = 40 and the seed boundary
-                                       on; 7 with the coefficients in shared
+                                       cells (M = 20 or 40 and the seed
+                                       boundary on; 7 with the coefficients in shared
                                        memory and, on one CTA per stream,
                                        no CTA barrier per sub-cycle).  shape 0
                                        automatic, k >= 1 the k-th CTA shape

@@ -84,24 +84,27 @@ def test_fp32_streaming_shapes_agree(oracle_lib, nodes):
         assert err <= 1e-4, f"variant {v} vs variant 3: {err:.3e}"
 
 
-@pytest.mark.parametrize("nodes,thin,seed_check", [(48, 0, 1), (401, 0, 1), (402, 5, 0),
-                                                    (403, 0, 0), (1100, 0, 1), (1500, 7, 1)])
-def test_fp32_mirrored_kinds_agree(oracle_lib, nodes, thin, seed_check):
+@pytest.mark.parametrize("nodes,thin,seed_check,mu", [
+    (48, 0, 1, 40), (401, 0, 1, 40), (402, 5, 0, 40), (403, 0, 0, 40), (1100, 0, 1, 40),
+    (1500, 7, 1, 40), (400, 0, 1, 20), (447, 3, 0, 20), (1000, 0, 1, 20), (2000, 0, 1, 20)])
+def test_fp32_mirrored_kinds_agree(oracle_lib, nodes, thin, seed_check, mu):
     """The mirrored streaming kinds (the mu < 0 half in mirror order, one
     upwind coefficient per two cells; 7 with the coefficients in shared memory
     and, on one CTA, the neighbour-warp halo hand-over) against the packed
     kind and the FP64 oracle.  The list lengths cover every position of the
     last list node modulo the nodes per thread (the slots start up to three
     nodes before list node 0), thinned streams, clusters of two and three
-    CTAs, the seed check on and off; both stream ends must keep the values
-    the reference keeps."""
-    w = W.custom(1, 1, nodes, 3, 40, num_ep_steps=2, use_adiabatic_focus=0,
+    CTAs, the seed check on and off, and both mu bins the mirrored kinds are
+    built for (40; 20 with two-warp CTAs for short streams and float2 rows);
+    both stream ends must keep the values the reference keeps."""
+    w = W.custom(1, 1, nodes, 3, mu, num_ep_steps=2, use_adiabatic_focus=0,
                  use_adiabatic_change=0, check_seed_population=seed_check)
     w.cluster_inner = thin
     d, g, f, nodes_arr = primed_state(w, oracle_lib)
     f_ref, _, _ = oracle_update(oracle_lib, w, g, f, nodes_arr)
     outs = {}
-    for variant in (5, 6, 7):
+    base = 5 if mu == 40 else 4  # the packed kind of the run's mu bin
+    for variant in (base, 6, 7):
         w.params.stream_variant = variant
         run = EpremRun(w.dims(abi.EPREM_FP32), w.params, g)
         run.upload_f(f)
@@ -114,8 +117,8 @@ def test_fp32_mirrored_kinds_agree(oracle_lib, nodes, thin, seed_check):
         err = np.max(np.abs(o - f_ref) / f_ref)
         assert err <= 1e-3, f"variant {v} vs FP64 oracle: {err:.3e}"
     for v in (6, 7):
-        err = np.max(np.abs(outs[v] - outs[5]) / outs[5])
-        assert err <= 1e-4, f"variant {v} vs variant 5: {err:.3e}"
+        err = np.max(np.abs(outs[v] - outs[base]) / outs[base])
+        assert err <= 1e-4, f"variant {v} vs variant {base}: {err:.3e}"
 
 
 def test_fp32_mirrored_kinds_need_the_seed_boundary():
