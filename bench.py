@@ -43,11 +43,11 @@ UNIT = "cell-updates/s"
 FLOPS_PER_CELL_SUBCYCLE = {"stream": 8.0, "focus": 11.0, "change": 11.0}
 BYTES_PER_CELL_UPDATE = {"fp64": 32.0, "fp32": 16.0}
 # DRAM bytes (read + write) per cell per launch of the dominant kernel, from
-# one ncu capture of the 96-stream subset (profiles/k_stream2_pairs_fp32_96streams.txt,
+# one ncu capture of the 96-stream subset (profiles/k_stream2_mirror_fp32_96streams.txt,
 # profiles/k_stream_fp64_96streams.txt, profiles/k_focus32_k_change32_fp32_96streams.txt):
 # traffic per launch / 96*1000*50*40 cells; traffic grows with the number of
 # (stream, energy) slabs, so it scales to a full launch by the cells processed.
-NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1600.7276e6 / 192e6,
+NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1600.0832e6 / 192e6,
                            ("stream", "fp64"): 3054.831e6 / 192e6,
                            ("node", "fp32"): 1488.048e6 / 192e6}
 
