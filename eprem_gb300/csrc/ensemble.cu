@@ -269,7 +269,9 @@ extern "C" int eprem_gpu_ensemble_autotune(eprem_gpu_ensemble *e, int *chosen_va
 // share a packed streaming kernel (mu bin, CTA shape, cluster size, guards),
 // the group's (run, stream, energy) slabs ordered by their estimated work,
 // longest first, so the slabs of small runs fill the tails of large ones --
-// and each run's node phase; all on the ensemble's stream.  Each slab and
+// and the node phases -- one focusing and one change launch per group of
+// runs of one mu count over all their row and node blocks, the other runs'
+// own launches; all on the ensemble's stream.  Each slab and
 // row is computed by the same code as in a run's own update: the results are
 // the runs' own, bit for bit.  Needs the same numEpSteps in every run.
 namespace {
@@ -352,6 +354,45 @@ static int ensemble_capture_lockstep(eprem_gpu_ensemble *e) {
     CK(cudaMemcpy(d, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
     n_items[gi] = (int)flat.size();
   }
+  // node phases: runs of one mu count in the plain form, focusing and change
+  // both on, in two launches per sub-step over all their (run, block) items
+  struct NodeGroup {
+    int M;
+    std::vector<int> runs;
+    NodeRunViews views;
+  };
+  std::vector<NodeGroup> ngroups;
+  std::vector<char> node_grouped(n, 0);
+  for (int i = 0; i < n; i++) {
+    eprem_gpu_run *r = e->runs[i];
+    if (r->node_mode != EPREM_NODE_PHASE_REFERENCE || !r->nplan.fast32 || !r->v.use_focus ||
+        !r->v.use_change || r->shell_on || r->drift_on)
+      continue;
+    NodeGroup *grp = nullptr;
+    for (auto &ng : ngroups)
+      if (ng.M == r->dims.num_mu && (int)ng.runs.size() < kMultiRuns) grp = &ng;
+    if (!grp) {
+      ngroups.push_back(NodeGroup{});
+      grp = &ngroups.back();
+      grp->M = r->dims.num_mu;
+    }
+    grp->runs.push_back(i);
+  }
+  for (auto &ng : ngroups) {
+    ng.views.n = 0;
+    if (ng.runs.size() < 2) continue;  // a lone run keeps its own launches
+    ng.views.n = (int)ng.runs.size();
+    ng.views.foff[0] = ng.views.coff[0] = 0;
+    for (int j = 0; j < ng.views.n; j++) {
+      eprem_gpu_run *r = e->runs[ng.runs[j]];
+      ng.views.v[j] = r->v;
+      int nf = 0, nc = 0;
+      node32_blocks(r->v, &nf, &nc);
+      ng.views.foff[j + 1] = ng.views.foff[j] + nf;
+      ng.views.coff[j + 1] = ng.views.coff[j] + nc;
+      node_grouped[ng.runs[j]] = 1;
+    }
+  }
   std::vector<bool> saved(n);
   std::vector<cudaStream_t> own(n);
   for (int i = 0; i < n; i++) {
@@ -382,8 +423,13 @@ static int ensemble_capture_lockstep(eprem_gpu_ensemble *e) {
         err = cudaGetLastError();
     for (int i : solo)
       if (!rc && err == cudaSuccess) rc = ep_stream_phase(e->runs[i], e->runs[i]->v);
+    for (auto &ng : ngroups)
+      if (ng.views.n && !rc && err == cudaSuccess &&
+          launch_node32_multi(e->runs[ng.runs[0]]->nplan, ng.views, e->origin,
+                              &e->runs[ng.runs[0]]->launches))
+        err = cudaGetLastError();
     for (int i = 0; i < n && !rc && err == cudaSuccess; i++)
-      rc = ep_node_phase(e->runs[i], e->runs[i]->v);
+      if (!node_grouped[i]) rc = ep_node_phase(e->runs[i], e->runs[i]->v);
   }
   for (int i = 0; i < n && !rc && err == cudaSuccess; i++) {
     eprem_gpu_run *r = e->runs[i];

@@ -67,6 +67,18 @@ int plan_node32(int E, int M, NodePlan *plan);
 int launch_node32(const RunView &r, const NodePlan &plan, cudaStream_t st, uint64_t *launches);
 // once per updateEnergeticParticles call, before the first launch_node32
 int launch_node32_setup(const RunView &r, cudaStream_t st, uint64_t *launches);
+// The node phase (focusing then change, both on) of several runs of one mu
+// count and one plan in two launches; a run's own launches are the same
+// kernels over one view.  foff / coff: each run's first focusing / change
+// CTA (prefix sums of node32_blocks), n runs.
+struct NodeRunViews {
+  RunView v[kMultiRuns];
+  int foff[kMultiRuns + 1], coff[kMultiRuns + 1];
+  int n;
+};
+void node32_blocks(const RunView &r, int *focus_blocks, int *change_blocks);
+int launch_node32_multi(const NodePlan &pl, const NodeRunViews &nv, cudaStream_t st,
+                        uint64_t *launches);
 
 // mhd.cu -- updateMhd (analytic), moveNodes, omnidirectional flux, f conversion
 struct MhdParams {

@@ -188,14 +188,16 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_node32_setup(RunView r) {
 // reads are free of bank conflicts) instead of one strided row per thread.
 // FULL: M fills the register row (M = P), so every cell guard and the row /
 // column split of the staging loops are known at compile time.
+// One CTA's block blk of kFocusThreads rows of run r: the body of k_focus32
+// and k_focus32_multi.
 template <int P, bool FULL>
-__global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
+__device__ __forceinline__ void focus_block(const RunView &r, size_t blk) {
   extern __shared__ float tile[];  // [kFocusThreads][pitch]
   const int E = r.E, N = r.N;
   const int M = FULL ? P : r.M;
   const int pitch = M | 1;
   const size_t rows = (size_t)r.S * N * E;
-  const size_t it0 = (size_t)blockIdx.x * kFocusThreads;
+  const size_t it0 = blk * kFocusThreads;
   const int nrows = (int)((rows - it0) < (size_t)kFocusThreads ? (rows - it0) : kFocusThreads);
   const int tid = threadIdx.x;
   float *base = reinterpret_cast<float *>(r.f) + it0 * M;
@@ -291,6 +293,22 @@ __global__ void __launch_bounds__(kFocusThreads) k_focus32(RunView r) {
   }
 }
 
+// The run of CTA b among the runs of nv, whose first CTAs are off[0..n-1].
+__device__ __forceinline__ int run_of_block(const int *off, int n, unsigned b) {
+  int j = 0;
+  while (j + 1 < n && (unsigned)off[j + 1] <= b) ++j;
+  return j;
+}
+
+// Focusing over the rows of the runs of nv (one run, or the runs of one mu
+// count of a lock-step ensemble): one launch, the same kernel either way, so
+// a run's rows come out the same bit for bit.
+template <int P, bool FULL>
+__global__ void __launch_bounds__(kFocusThreads) k_focus32(const __grid_constant__ NodeRunViews nv) {
+  const int j = run_of_block(nv.foff, nv.n, blockIdx.x);
+  focus_block<P, FULL>(nv.v[j], blockIdx.x - (unsigned)nv.foff[j]);
+}
+
 // ---- adiabatic change: one (node, mu) column per thread --------------------
 // A CTA holds whole nodes (npc = max(1, 128 / M) of them on npc * M threads)
 // so that, after the sub-cycles, it can renormalise every row it writes.
@@ -336,7 +354,9 @@ __device__ __forceinline__ float exp_rel(float l, float scale) {
   return __expf(near ? l : l + 64.f * kLn2) * (near ? scale : scale * 0x1p-64f);
 }
 
-__global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc) {
+// One CTA's block blk of npc nodes of run r: the body of k_change32 and
+// k_change32_multi.
+__device__ __forceinline__ void change_block(const RunView &r, int npc, size_t blk) {
   extern __shared__ float sm[];
   constexpr float kLn2 = 0.6931471805599453f;
   const int E = r.E, M = r.M;
@@ -344,7 +364,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   const int tid = threadIdx.x;
   const int j = tid / M, m = tid - (tid / M) * M;
   const size_t SN = (size_t)r.S * r.N;
-  const size_t g = (size_t)blockIdx.x * npc + j;
+  const size_t g = blk * npc + j;
   float *lnf = sm;                                             // [E][T]
   int *xs = reinterpret_cast<int *>(sm + (size_t)E * T);     // [npc][E] row exponents
   int *sh = xs + npc * E;                                      // [npc][E] renormalising shifts
@@ -355,7 +375,7 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   // the rows' exponents less kRowTop: ln f = lnf - xs ln 2 with lnf the ln of
   // a stored value relative to 2^kRowTop (see ln_rel)
   for (int i = tid; i < npc * E; i += blockDim.x) {
-    const size_t gg = (size_t)blockIdx.x * npc + i / E;
+    const size_t gg = blk * npc + i / E;
     xs[i] = (gg < SN ? r.fexp[gg * E + i % E] : 0) - kRowTop;
   }
   for (int e = tid; e < E; e += blockDim.x)
@@ -451,6 +471,13 @@ __global__ void __launch_bounds__(kChangeThreads) k_change32(RunView r, int npc)
   }
 }
 
+// The change over the nodes of the runs of nv, as k_focus32 over their rows.
+__global__ void __launch_bounds__(kChangeThreads)
+    k_change32(const __grid_constant__ NodeRunViews nv, int npc) {
+  const int j = run_of_block(nv.coff, nv.n, blockIdx.x);
+  change_block(nv.v[j], npc, blockIdx.x - (unsigned)nv.coff[j]);
+}
+
 // Row lengths the focusing kernel is built for (20: the CPU-runnable case's
 // mu count, with compile-time cell guards).
 static int bucket(int n) {
@@ -477,26 +504,41 @@ int launch_node32_setup(const RunView &r, cudaStream_t st, uint64_t *launches) {
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
 }
 
-template <int P>
-static void launch_focus_t(const RunView &r, cudaStream_t st) {
-  const size_t rows = (size_t)r.S * r.N * r.E;
-  const size_t smem = (size_t)kFocusThreads * (r.M | 1) * sizeof(float);
-  const unsigned blocks = (unsigned)((rows + kFocusThreads - 1) / kFocusThreads);
-  if (r.M == P)
-    k_focus32<P, true><<<blocks, kFocusThreads, smem, st>>>(r);
-  else
-    k_focus32<P, false><<<blocks, kFocusThreads, smem, st>>>(r);
+static int change_npc(int M) { return M >= kChangeThreads ? 1 : kChangeThreads / M; }
+static size_t change_smem(int E, int M) {
+  const int npc = change_npc(M);
+  return (size_t)E * npc * M * sizeof(float) + 5 * (size_t)npc * E * sizeof(int) +
+         (size_t)E * sizeof(float);
 }
 
-static void launch_change(const RunView &r, cudaStream_t st) {
-  const int npc = r.M >= kChangeThreads ? 1 : kChangeThreads / r.M;
-  const size_t SN = (size_t)r.S * r.N;
-  const size_t smem =
-      (size_t)r.E * npc * r.M * sizeof(float) + 5 * (size_t)npc * r.E * sizeof(int) +
-      (size_t)r.E * sizeof(float);
+void node32_blocks(const RunView &r, int *focus_blocks, int *change_blocks) {
+  const size_t rows = (size_t)r.S * r.N * r.E, SN = (size_t)r.S * r.N;
+  const int npc = change_npc(r.M);
+  *focus_blocks = (int)((rows + kFocusThreads - 1) / kFocusThreads);
+  *change_blocks = (int)((SN + npc - 1) / npc);
+}
+
+// nv's runs share M (and so P and npc)
+template <int P>
+static void launch_focus_t(const NodeRunViews &nv, cudaStream_t st) {
+  const int M = nv.v[0].M;
+  const size_t smem = (size_t)kFocusThreads * (M | 1) * sizeof(float);
+  if (M == P)
+    k_focus32<P, true><<<nv.foff[nv.n], kFocusThreads, smem, st>>>(nv);
+  else
+    k_focus32<P, false><<<nv.foff[nv.n], kFocusThreads, smem, st>>>(nv);
+}
+
+static void launch_change(const NodeRunViews &nv, cudaStream_t st) {
+  const int M = nv.v[0].M, npc = change_npc(M);
+  size_t smem = 0;
+  for (int i = 0; i < nv.n; i++) {
+    const size_t b = change_smem(nv.v[i].E, M);
+    smem = b > smem ? b : smem;
+  }
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_change32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_change32<<<(unsigned)((SN + npc - 1) / npc), kChangeThreads, smem, st>>>(r, npc);
+  k_change32<<<nv.coff[nv.n], kChangeThreads, smem, st>>>(nv, npc);
 }
 
 #define EPREM_P_SWITCH(p, F, ...)      \
@@ -512,13 +554,27 @@ static void launch_change(const RunView &r, cudaStream_t st) {
     default: F<64>(__VA_ARGS__); break; \
   }
 
+int launch_node32_multi(const NodePlan &pl, const NodeRunViews &nv, cudaStream_t st,
+                        uint64_t *launches) {
+  if (nv.n <= 0 || nv.n > kMultiRuns) return EPREM_GPU_ERR_ARG;
+  EPREM_P_SWITCH(pl.pmax, launch_focus_t, nv, st);
+  launch_change(nv, st);
+  *launches += 2;
+  return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
+}
+
 int launch_node32(const RunView &r, const NodePlan &pl, cudaStream_t st, uint64_t *launches) {
+  NodeRunViews nv;
+  nv.v[0] = r;
+  nv.n = 1;
+  nv.foff[0] = nv.coff[0] = 0;
+  node32_blocks(r, &nv.foff[1], &nv.coff[1]);
   if (r.use_focus) {
-    EPREM_P_SWITCH(pl.pmax, launch_focus_t, r, st);
+    EPREM_P_SWITCH(pl.pmax, launch_focus_t, nv, st);
     *launches += 1;
   }
   if (r.use_change) {
-    launch_change(r, st);
+    launch_change(nv, st);
     *launches += 1;
   }
   return cudaGetLastError() == cudaSuccess ? 0 : EPREM_GPU_ERR_CUDA;
