@@ -1263,7 +1263,9 @@ constexpr S2Shape kS2Shapes[] = {
 }  // namespace
 
 // The shapes the mirrored kinds are built for: three of the 40 bin and the 20
-// bin.  Wider CTAs do not pay: the register file is split between the four
+// bin.  At N = 1500 the 128 x 4 shape in clusters of 3 (two CTAs of
+// different slabs share an SM) took 14.8 ms per 96-stream launch, 256 x 3 in
+// clusters of 2 19.4 ms.  Wider CTAs do not pay: the register file is split between the four
 // warp schedulers, so 9 to 12 warps cap a thread at 168 registers, and 3 or 4
 // list nodes of 40 cells then spill (288x4, 352x3, 384x3 measured with ptxas).
 #define EPREM_S2M_SHAPES(X) X(40, 256, 4) X(40, 128, 4) X(40, 256, 3) EPREM_S2M20_SHAPES(X)
