@@ -744,9 +744,10 @@ __global__ void __launch_bounds__(T, 1)
 // with del < 0, src/energeticParticles.c:2392-2397).  Per cell and sub-cycle
 // that leaves the difference, the update, the sum and the relaxation on the
 // FMA pipe.  Kind 7 forms the coefficients once per launch into shared memory
-// ([P/2][NPT][T] float4: one 16-byte load serves four cells on the sub-cycle
-// loop); kind 6 forms them on the loop (one packed multiply per node and pair
-// index, shared by the two halves).
+// (float4 [P/2][NPT][T], or float2 [P][NPT][T] when M/2 is not a multiple of
+// 4; on the sub-cycle loop one 8-byte load per node and pair index serves a
+// pair of cells of each half); kind 6 forms them on the loop (one packed
+// multiply per node and pair index, shared by the two halves).
 // The two ends of the stream keep their values without a zero multiplier:
 //   * list node 0, mu >= 0 (:2380): with the seed boundary, node 0 holds the
 //     seed at the upwind step, and so does its upwind neighbour -- the empty
@@ -812,14 +813,14 @@ __device__ __forceinline__ void halo_arrive(uint64_t *bar) {
 // instead of a CTA barrier per sub-cycle, each warp waits only for the halo
 // rows of its two neighbour warps -- an mbarrier per (parity, warp) that lane
 // 31 of the warp before and lane 0 of the warp after arrive on once their
-// rows are stored (release / acquire at CTA scope).  Across the CTAs of a
-// cluster the same hand-over (remote arrivals at cluster scope) measured no
-// faster than the cluster barrier: 15.02 against 14.88 ms per 96-stream
-// launch at N = 1500, whose 128-thread CTAs share an SM two by two, so one
-// CTA's barrier wait overlaps the other's work.
-// Warps then drift up to one sub-cycle apart; the two parities of the halo
-// rows cover that: a warp writes a parity's row again only after its
-// neighbour has published the next sub-cycle, i.e. has read the row.
+// rows are stored (release / acquire at CTA scope).  Warps then drift up to
+// one sub-cycle apart; the two parities of the halo rows cover that: a warp
+// writes a parity's row again only after its neighbour has published the
+// next sub-cycle, i.e. has read the row.  Across the CTAs of a cluster the
+// same hand-over (remote arrivals at cluster scope) measured no faster than
+// the cluster barrier: 15.02 against 14.88 ms per 96-stream launch at
+// N = 1500, whose 128-thread CTAs share an SM two by two, so one CTA's
+// barrier wait overlaps the other's work.
 template <int MMAX, int T, int NPT, bool CSM, int ASYNC>
 __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int s, const int e) {
   constexpr int W = T / 32;
