@@ -804,6 +804,39 @@ __device__ __forceinline__ bool halo_wait(uint64_t *bar, uint32_t parity) {
   }
   return false;
 }
+// put_half and halo_arrive by the lanes where p holds, as predicated
+// instructions of the whole warp rather than a divergent branch.
+template <int P, bool V4>
+__device__ __forceinline__ void put_half_if(bool p, const float2 (&h)[P], float *dst) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(dst);
+  const uint32_t pr = p ? 1u : 0u;
+  if constexpr (V4) {
+#pragma unroll
+    for (int t = 0; t < P / 2; ++t)
+      asm volatile(
+          "{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n"
+          " @q st.shared.v4.f32 [%1], {%2, %3, %4, %5};\n}\n" ::"r"(pr),
+          "r"(a + 16u * t), "f"(h[2 * t].x), "f"(h[2 * t].y), "f"(h[2 * t + 1].x),
+          "f"(h[2 * t + 1].y)
+          : "memory");
+  } else {
+#pragma unroll
+    for (int t = 0; t < P; ++t)
+      asm volatile(
+          "{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n"
+          " @q st.shared.v2.f32 [%1], {%2, %3};\n}\n" ::"r"(pr),
+          "r"(a + 8u * t), "f"(h[t].x), "f"(h[t].y)
+          : "memory");
+  }
+}
+__device__ __forceinline__ void halo_arrive_if(bool p, uint64_t *bar) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  asm volatile(
+      "{\n .reg .pred q;\n .reg .b64 st;\n setp.ne.u32 q, %0, 0;\n"
+      " @q mbarrier.arrive.shared::cta.b64 st, [%1];\n}\n" ::"r"(p ? 1u : 0u),
+      "r"(a)
+      : "memory");
+}
 __device__ __forceinline__ void halo_arrive(uint64_t *bar) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a)
@@ -998,6 +1031,13 @@ __device__ __forceinline__ void stream2_mirror_slab(const RunView &r, const int 
   // reader waits on (the seed boundary is set before: list nodes 0..2 sit in
   // threads 0 and 1)
   auto publish_edges = [&](int p) {
+    if constexpr (ASYNC == 1) {  // one CTA: predicated stores and arrivals, no branch
+      put_half_if<P, V4>(lane == 31, Rf[NPT - 1], hi(p, warp + 1));
+      halo_arrive_if(lane == 31 && warp + 1 < W, &s_bar[p][warp + 1 < W ? warp + 1 : 0]);
+      put_half_if<P, V4>(lane == 0, Lf[0], lo(p, warp));
+      halo_arrive_if(lane == 0 && warp > 0, &s_bar[p][warp > 0 ? warp - 1 : 0]);
+      return;
+    }
     if (lane == 31) {
       put_half<P, V4>(Rf[NPT - 1], hi(p, warp + 1),
                       (warp == W - 1 && next_hi0) ? next_hi0 + ((p * 2 + 0) * (W + 1)) * H
