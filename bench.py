@@ -47,7 +47,7 @@ BYTES_PER_CELL_UPDATE = {"fp64": 32.0, "fp32": 16.0}
 # profiles/k_stream_fp64_96streams.txt, profiles/k_focus32_k_change32_fp32_96streams.txt):
 # traffic per launch / 96*1000*50*40 cells; traffic grows with the number of
 # (stream, energy) slabs, so it scales to a full launch by the cells processed.
-NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1600.0832e6 / 192e6,
+NCU_DRAM_BYTES_PER_CELL = {("stream", "fp32"): 1603.9058e6 / 192e6,
                            ("stream", "fp64"): 3054.831e6 / 192e6,
                            ("node", "fp32"): 1488.048e6 / 192e6}
 
