@@ -25,6 +25,9 @@ CASES = {
     "mfpB_damped_noseedcheck": lambda: W.custom(1, 1, 30, 10, 8, num_ep_steps=3, mfp_type=2,
                                                 damp_cooling=0.4, check_seed_population=0),
     "no_boundary_odd_mu": lambda: W.custom(1, 1, 30, 9, 7, num_ep_steps=3, use_ep_boundary=0),
+    # the CPU-runnable plain workload at its full size (24 x 400 x 20 x 20, 30
+    # EP sub-steps per call), whose whole 24 h run the GPU is checked against
+    "cpu_runnable_full_size": W.small_plain,
     # shell diffusion (DiffuseShellData) on the reference's own NEWS links
     "shell_1x1_faces": lambda: W.custom(1, 1, 20, 8, 6, num_ep_steps=2),
     "shell_2x2_faces": lambda: W.custom(2, 2, 24, 10, 8, num_ep_steps=3),
