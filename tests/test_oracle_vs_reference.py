@@ -14,6 +14,16 @@ from eprem_gb300 import abi, workloads as W
 pytestmark = pytest.mark.skipif(not os.path.exists(O.REF_LIB),
                                 reason="reference harness not built here")
 
+def _scale_per_stream():
+    """The precision-at-scale workload's streams (1000 nodes, 50 energies to
+    1000 MeV, 40 mu) on 6 of them, for 3 EP sub-steps of the full call's
+    sub-step length (up to 567 streaming sub-cycles each)."""
+    w = W.with_faces(W.scale_plain(), 1, 1)
+    w.params.t_del = w.params.t_del / w.params.num_ep_steps * 3
+    w.params.num_ep_steps = 3
+    return w
+
+
 CASES = {
     "wind_like_thinned": lambda: W.testsuite_like("wind", 1, 1, 30),
     "cone_like_shock": lambda: W.testsuite_like("cone", 1, 1, 40),
@@ -28,6 +38,7 @@ CASES = {
     # the CPU-runnable plain workload at its full size (24 x 400 x 20 x 20, 30
     # EP sub-steps per call), whose whole 24 h run the GPU is checked against
     "cpu_runnable_full_size": W.small_plain,
+    "precision_at_scale_streams": _scale_per_stream,
     # shell diffusion (DiffuseShellData) on the reference's own NEWS links
     "shell_1x1_faces": lambda: W.custom(1, 1, 20, 8, 6, num_ep_steps=2),
     "shell_2x2_faces": lambda: W.custom(2, 2, 24, 10, 8, num_ep_steps=3),
