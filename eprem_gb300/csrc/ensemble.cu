@@ -109,6 +109,23 @@ extern "C" int eprem_gpu_autotune(eprem_gpu_run *r, int *chosen_variant) {
   return tune_stream(r, chosen_variant);
 }
 
+extern "C" int eprem_gpu_plan_stream(int num_nodes, int num_mu, int m0, int precision,
+                                     int variant, int seed_boundary, int out[6]) {
+  if (!out || num_nodes < 3 || num_mu < 2 || num_mu > 64 || m0 < 0 || m0 > num_mu)
+    return fail(EPREM_GPU_ERR_ARG, "bad sizes");
+  StreamPlan p{};
+  if (plan_stream(precision, num_nodes, num_mu, m0, variant, seed_boundary != 0, &p))
+    return fail(EPREM_GPU_ERR_ARG, "no streaming kernel fits these sizes");
+  const bool s2 = p.reg_coef == 2;
+  out[0] = !s2 ? 0 : p.mirror ? 5 + p.mirror : !p.packed ? 3 : p.filled ? 5 : 4;
+  out[1] = p.mmax;
+  out[2] = p.threads;
+  out[3] = s2 ? p.npt : 1;
+  out[4] = p.cluster;
+  out[5] = p.threads * (s2 ? p.npt : 1) * p.cluster;
+  return EPREM_GPU_OK;
+}
+
 extern "C" const char *eprem_gpu_stream_kernel(eprem_gpu_run *r) {
   if (!r) return "";
   const StreamPlan &p = r->splan;

@@ -71,6 +71,8 @@ EXPORTS = [
     ("eprem_gpu_autotune", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("eprem_gpu_set_stream_variant", C.c_int, [C.c_void_p, C.c_int]),
     ("eprem_gpu_stream_kernel", C.c_char_p, [C.c_void_p]),
+    ("eprem_gpu_plan_stream", C.c_int,
+     [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("eprem_gpu_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int,
                                             C.POINTER(C.c_void_p)]),
     ("eprem_gpu_ensemble_destroy", C.c_int, [C.c_void_p]),
@@ -141,6 +143,20 @@ def alu_peak_tflops(precision: int) -> float:
     if rc:
         raise EpremGpuError(rc, lib.eprem_gpu_last_error().decode())
     return out.value
+
+
+def plan_stream(num_nodes: int, num_mu: int, m0: int, precision: int, variant: int = 0,
+                seed_boundary: bool = True) -> dict:
+    """The streaming kernel a run of these sizes would launch (host only, no
+    device needed): kind, mu bin, threads, list nodes per thread, cluster
+    size and the nodes a cluster holds."""
+    lib = load_library()
+    out = (C.c_int * 6)()
+    rc = lib.eprem_gpu_plan_stream(num_nodes, num_mu, m0, precision, variant,
+                                   1 if seed_boundary else 0, out)
+    if rc:
+        raise EpremGpuError(rc, lib.eprem_gpu_last_error().decode())
+    return dict(zip(("kind", "mmax", "threads", "npt", "cluster", "slots"), list(out)))
 
 
 def _dp(a: np.ndarray):

@@ -508,6 +508,16 @@ int eprem_gpu_init_seed_population(eprem_gpu_run *run, uint64_t seed, double per
 int eprem_gpu_autotune(eprem_gpu_run *run, int *chosen_variant);
 /* Force a streaming-kernel shape (EPREM_GPU_ERR_ARG if it does not fit). */
 int eprem_gpu_set_stream_variant(eprem_gpu_run *run, int variant);
+/* The streaming kernel a run of these sizes would launch, without a run or a
+ * device: num_nodes, num_mu, m0 (the first mu cell with mugrid >= 0),
+ * precision, variant (eprem_params_t.stream_variant) and seed_boundary
+ * (useEPBoundary and useBoundaryFunction both on).  out[0..5]: kind (0 the
+ * FP64 kernel; 3 to 7 as stream_variant), mu bin, threads per CTA, list
+ * nodes per thread (1 for FP64), CTAs per cluster, nodes a cluster holds.
+ * EPREM_GPU_ERR_ARG where no kernel fits.  No counterpart in the
+ * reference. */
+int eprem_gpu_plan_stream(int num_nodes, int num_mu, int m0, int precision, int variant,
+                          int seed_boundary, int out[6]);
 /* The streaming kernel this run launches, with its shape, e.g.
  * "k_stream2_mirror<40,256,4> cluster 1" (a string owned by the run, valid
  * until its next eprem_gpu_set_stream_variant / autotune / destroy).  No

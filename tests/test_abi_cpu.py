@@ -67,3 +67,48 @@ def test_node_field_enum_matches_header():
     body = text[text.index("enum eprem_node_field"):text.index("EPREM_NODE_NFIELDS\n")]
     names = re.findall(r"EPREM_NODE_([A-Z_]+)", body)
     assert names == abi.NODE_FIELDS
+
+
+@pytest.mark.parametrize("nodes,mu,bc,expect", [
+    # the precision-at-scale streams: the mirrored kind on one 256-thread CTA
+    (1000, 40, True, dict(kind=7, mmax=40, threads=256, npt=4, cluster=1)),
+    # the MHD-coupled streams: 128 x 4 in clusters of 3 (1501 slots needed)
+    (1500, 40, True, dict(kind=7, mmax=40, threads=128, npt=4, cluster=3)),
+    # 1022 nodes: list node 0 may start 3 slots in, so 1025 slots -> a cluster
+    (1022, 40, True, dict(kind=7, threads=128, npt=4, cluster=3)),
+    (1021, 40, True, dict(kind=7, threads=256, npt=4, cluster=1)),
+    # the CPU-runnable size: its own 20 bin, a stream on two warps
+    (400, 20, True, dict(kind=7, mmax=20, threads=64, npt=7, cluster=1)),
+    # no seed boundary: the packed kind with compile-time guards
+    (1000, 40, False, dict(kind=5, mmax=40, threads=256, npt=4, cluster=1)),
+    # a mu count between bins: the packed kind with run-time guards
+    (600, 28, True, dict(kind=4, mmax=32)),
+])
+def test_stream_plan_without_a_device(lib, nodes, mu, bc, expect):
+    """The streaming kernel chosen for a run's sizes (kind 0, automatic):
+    the mirrored kind where M is 20 or 40 and the seed boundary is on,
+    otherwise the packed kinds; a cluster holds the stream."""
+    got = runtime.plan_stream(nodes, mu, mu // 2, abi.EPREM_FP32, 0, bc)
+    for k, v in expect.items():
+        assert got[k] == v, (k, got)
+    need = nodes + (got["npt"] - 1 if got["kind"] in (6, 7) else 0)
+    assert got["slots"] >= need
+    assert got["slots"] - need < got["threads"] * got["npt"]  # no idle CTA
+
+
+def test_stream_plan_refusals(lib):
+    # the mirrored kinds need the seed boundary and M = 20 or 40
+    with pytest.raises(runtime.EpremGpuError):
+        runtime.plan_stream(1000, 40, 20, abi.EPREM_FP32, 7, seed_boundary=False)
+    with pytest.raises(runtime.EpremGpuError):
+        runtime.plan_stream(1000, 32, 16, abi.EPREM_FP32, 7)
+    # the FP64 kernel's shapes are not FP32 variants, and the reverse
+    with pytest.raises(runtime.EpremGpuError):
+        runtime.plan_stream(1000, 40, 20, abi.EPREM_FP32, 1)
+    with pytest.raises(runtime.EpremGpuError):
+        runtime.plan_stream(1000, 40, 20, abi.EPREM_FP64, 5)
+    # more than 8 CTAs per cluster
+    with pytest.raises(runtime.EpremGpuError):
+        runtime.plan_stream(100000, 40, 20, abi.EPREM_FP32, 0)
+    fp64 = runtime.plan_stream(1000, 40, 20, abi.EPREM_FP64, 0)
+    assert fp64["kind"] == 0 and fp64["slots"] >= 1000
