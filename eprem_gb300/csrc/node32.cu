@@ -23,6 +23,10 @@
 //   * k_change32, every EP sub-step: one thread per (node, mu) column, whole
 //     nodes per CTA (a warp reads consecutive mu of one energy: coalesced),
 //     ln f in shared memory, each row renormalised to its own exponent.
+// Both take a block of run views (NodeRunViews) and find their run from its
+// first CTA: a run's own launch is one view, a lock-step ensemble's launch
+// all the runs of one mu count -- the same compiled code either way, so an
+// ensemble member's results equal its own run's bit for bit.
 // No block barriers on the sub-cycle paths.  Only the
 // Euler upwind algorithm (alg 1) runs here; RK3 / WENO3 use node.cu.
 #include "common.cuh"
